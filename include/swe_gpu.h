@@ -1,0 +1,163 @@
+/*
+ * swe_gpu.h — C ABI of the GB300 (sm_103a) explicit P1 shallow-water step.
+ *
+ * This is the drop-in boundary for the public surface of the reference's
+ * Fortran modules `update` and `fct` (t-bltg/shallow-water-eric):
+ *
+ *   MODULE update   SOURCES/update.f90:1-16   construct_matrices, euler,
+ *                                             compute_dij; public data dij,
+ *                                             lumped, diag
+ *   MODULE fct      SOURCES/fct.f90:1-5       FCT_positivity
+ *   time loop       SOURCES/main.f90:61-91    COMPUTE_DT (:166-174) + SSP-RK3
+ *                                             + bdy (:176-188)
+ *
+ * Conventions
+ *  - Every host pointer is owned by the caller and only borrowed for the
+ *    duration of the call.  State arrays use the reference layout
+ *    un(syst_size, np): column-major FP64, component fastest, nodes in the
+ *    caller's (reference) numbering.  Node/element indices are 1-based.
+ *  - Every call returns an int status: SWE_OK or one of SWE_ERR_*.  The
+ *    reference STOPs where this layer returns SWE_ERR_NEG_H (check_hmin,
+ *    SOURCES/update.f90:810-822) or SWE_ERR_DELTA (compute_lambda_vacc,
+ *    SOURCES/condlim.f90:934-937).  swe_last_error() gives the message.
+ *  - One context serves one host thread and owns one CUDA stream; calls are
+ *    synchronous on return.  There is no CPU fallback: a context cannot be
+ *    created without a CUDA device.
+ *  - A context holds one mesh, or a batch of independent meshes advanced
+ *    together (each with its own parameters, dt and time).
+ */
+#ifndef SWE_GPU_H
+#define SWE_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  SWE_OK = 0,
+  SWE_ERR_NEG_H = 1,     /* min h < 0 after a stage (check_hmin)           */
+  SWE_ERR_DELTA = 2,     /* Delta < 0 in the lambda_max bound              */
+  SWE_ERR_NAN = 3,       /* non-finite value produced                      */
+  SWE_ERR_TIMEOUT = 4,   /* a bounded device wait gave up                  */
+  SWE_ERR_CUDA = 5,      /* CUDA runtime error                             */
+  SWE_ERR_ARG = 6,       /* invalid argument                               */
+  SWE_ERR_MESH = 7       /* mesh rejected (row longer than 90 entries, ...) */
+};
+
+/* viscosity_type values (SOURCES/read_data.f90:57-58 marker) */
+enum { SWE_VISC_GALERKIN = 0, SWE_VISC_VISCOUS = 1, SWE_VISC_ENTROPY = 2, SWE_VISC_FCT = 3 };
+/* precision values */
+enum { SWE_PREC_FP64 = 0, SWE_PREC_MIXED = 1 };
+
+/* The subset of the reference's `inputs` record (SOURCES/read_data.f90:4-32)
+ * and module constants the step reads.  Field order is part of the ABI. */
+typedef struct swe_params {
+  double gravity;        /* inputs%gravity                                   */
+  double dt;             /* inputs%dt (used by the per-call entry points)    */
+  double cfl;            /* inputs%CFL                                       */
+  double htiny;          /* inputs%htiny = epsilon*max_water_h               */
+  double mannings;       /* inputs%mannings (type_test 9, 10)                */
+  double lambda_sgn;     /* inputs%lambdaSGN (type_test 13)                  */
+  double max_water_h;    /* boundary_conditions max_water_h                  */
+  int type_test;         /* selects flux variant and source term             */
+  int syst_size;         /* 3, or 5 for type_test 13                         */
+  int viscosity_type;    /* SWE_VISC_*                                       */
+  int viscous_type;      /* 1 = 'type1', 2 = 'type2'                         */
+  int if_alpha_limit;    /* inputs%if_alpha_limit                            */
+  int if_lumped;         /* inputs%if_lumped (only lumped is supported)      */
+  int if_roundoff_fix;   /* update.f90:15 module constant                    */
+  int precision;         /* SWE_PREC_FP64 or SWE_PREC_MIXED                  */
+} swe_params;
+
+typedef struct swe_ctx swe_ctx;
+
+/* construct_matrices (SOURCES/update.f90:18-132) for one mesh: builds the CSR
+ * pattern, consistent and lumped mass, diag and c_ij, renumbers the nodes by
+ * reverse Cuthill-McKee and uploads the SELL-32 edge graph.
+ * jj(3, me) 1-based counter-clockwise triangles, rr(2, np), bath(np). */
+int swe_create(swe_ctx** ctx, int np, int me, const int* jj, const double* rr,
+               const double* bath, const swe_params* params);
+
+/* Batched variant: n_inst independent meshes, concatenated.  np[b], me[b]
+ * give each instance's sizes; jj holds each instance's own 1-based node
+ * numbers, instance after instance; rr, bath likewise; params[b] per
+ * instance (all instances must share syst_size and precision). */
+int swe_create_batch(swe_ctx** ctx, int n_inst, const int* np, const int* me,
+                     const int* jj, const double* rr, const double* bath,
+                     const swe_params* params);
+
+void swe_destroy(swe_ctx* ctx);
+const char* swe_last_error(const swe_ctx* ctx);
+
+/* Replace the parameters of instance `inst` (0-based); dt is the inputs%dt
+ * used by swe_euler. */
+int swe_set_params(swe_ctx* ctx, int inst, const swe_params* params);
+
+/* Constant Dirichlet data applied after every RK stage by swe_rk3_steps,
+ * like bdy (SOURCES/main.f90:176-188) with values that do not depend on t:
+ * comp is the 0-based component, js 1-based node numbers of instance
+ * `inst`, vals the values (NULL = zeros).  Replaces earlier data for comp. */
+int swe_set_dirichlet(swe_ctx* ctx, int inst, int comp, int n, const int* js, const double* vals);
+
+/* Sizes and the assembled matrices in the reference numbering and CSR order
+ * (1-based ia/ja, like mass%ia/ja).  Any output pointer may be NULL. */
+int swe_sizes(const swe_ctx* ctx, int inst, int* np, int* nnz);
+int swe_get_matrices(swe_ctx* ctx, int inst, int* ia, int* ja, double* mass,
+                     double* lumped, int* diag, double* cx, double* cy);
+
+/* compute_dij (SOURCES/update.f90:291-326) on instance `inst` for the state
+ * un(S, np); dij (nnz, CSR order) and dt_out = CFL/max(|d_ii|/m_i)
+ * (COMPUTE_DT, SOURCES/main.f90:166-174) are optional outputs. */
+int swe_compute_dij(swe_ctx* ctx, int inst, const double* un, double* dij, double* dt_out);
+
+/* euler (SOURCES/update.f90:134-289): one forward-Euler stage with the
+ * instance's viscosity settings and inputs%dt = params.dt. */
+int swe_euler(swe_ctx* ctx, int inst, const double* un, double* unext);
+
+/* Intermediates of the last swe_euler call of instance `inst`, in CSR order
+ * (nnz) or node order (np); any pointer may be NULL.  dij_low/muij_low are
+ * the alpha-limited low-order viscosities (dijL, muijL), res the entropy
+ * residual per node, fctmat the antidiffusive matrix, rminus R^-_i, lij the
+ * limiter l_ij, u_low the low-order state (S, np). */
+int swe_euler_intermediates(swe_ctx* ctx, int inst, double* dij_low, double* muij_low,
+                            double* alpha, double* u_low, double* res, double* fctmat,
+                            double* rminus, double* lij);
+
+/* FCT_positivity (SOURCES/fct.f90:5-42): unext = (lumped/dt)*h^L (np),
+ * mat = f_ij (nnz, CSR order) -> lij (nnz, CSR order). */
+int swe_fct_positivity(swe_ctx* ctx, int inst, const double* unext, const double* mat, double* lij);
+
+/* Device-resident fast path.  upload/download move every instance's state;
+ * un is the concatenation of the instances' un(S, np_b) blocks. */
+int swe_upload(swe_ctx* ctx, const double* un);
+int swe_download(swe_ctx* ctx, double* un);
+/* Same, with un already in device memory (concatenated reference layout). */
+int swe_upload_device(swe_ctx* ctx, const double* d_un);
+int swe_download_device(swe_ctx* ctx, double* d_un);
+
+/* Set every instance's time and final time (arrays of n_inst, NULL time =
+ * keep). */
+int swe_set_time(swe_ctx* ctx, const double* time, const double* t_final);
+
+/* Advance nsteps iterations of the reference time loop (SOURCES/main.f90:
+ * 61-91) on the device: per instance, while time < t_final: dt =
+ * CFL/max|d_ii|/m_i, three SSP-RK stages, Dirichlet data after each stage,
+ * time += dt (dt is not clipped at t_final, as in the reference).  Instances
+ * that reached t_final stop.  The step sequence runs as one captured CUDA
+ * graph.  time_out / dt_out (n_inst each, nullable) receive the instances'
+ * time and last dt; steps_done (nullable) the number of steps instance 0 ran. */
+int swe_rk3_steps(swe_ctx* ctx, int nsteps, double* time_out, double* dt_out, int* steps_done);
+
+/* Total water mass sum_i m_i h_i per instance (compensated summation). */
+int swe_mass(swe_ctx* ctx, double* mass_out);
+
+/* Kernel launches issued by the last swe_rk3_steps call (for accounting). */
+long long swe_last_launch_count(const swe_ctx* ctx);
+
+/* Name of the kernel configuration chosen by the autotuner. */
+const char* swe_tuning(const swe_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SWE_GPU_H */

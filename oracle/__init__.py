@@ -1,0 +1,215 @@
+"""Oracle package — TEST INFRASTRUCTURE ONLY.
+
+This is the FP64 CPU restatement of the reference's explicit P1 Saint-Venant
+step (SOURCES/update.f90, SOURCES/fct.f90, SOURCES/condlim.f90,
+SOURCES/main.f90 of t-bltg/shallow-water-eric), compiled from
+``swe_oracle.cpp``.  Only the tests, ``__graft_entry__.smoke()`` and the CPU
+baseline leg of ``bench.py`` may import it, and only as the checker or the
+timed CPU baseline.  The product library never loads it.
+
+Parity status: partially pinned (see the header of swe_oracle.cpp): the
+reference's own initial-state/bathymetry dumps on cav_0.2 pin the setup, the
+reference's recorded Thacker L1 errors pin the time stepping loosely.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+LIB = BUILD / "libswe_oracle.so"
+SRC = HERE / "swe_oracle.cpp"
+
+# No FMA contraction and no fast-math: the restatement's evaluation order is
+# its contract (identical results on x86-64 and aarch64 hosts).
+CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math"]
+
+
+def build(force: bool = False) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    if force or not LIB.exists() or LIB.stat().st_mtime < SRC.stat().st_mtime:
+        tmp = BUILD / f"libswe_oracle.{os.getpid()}.so"
+        subprocess.run(["g++", *CXXFLAGS, "-o", str(tmp), str(SRC)], check=True)
+        os.replace(tmp, LIB)
+    return LIB
+
+
+class Params(ctypes.Structure):
+    """Same layout as ``swe_params`` in include/swe_gpu.h."""
+    _fields_ = [
+        ("gravity", ctypes.c_double), ("dt", ctypes.c_double), ("cfl", ctypes.c_double),
+        ("htiny", ctypes.c_double), ("mannings", ctypes.c_double), ("lambda_sgn", ctypes.c_double),
+        ("max_water_h", ctypes.c_double),
+        ("type_test", ctypes.c_int), ("syst_size", ctypes.c_int), ("viscosity_type", ctypes.c_int),
+        ("viscous_type", ctypes.c_int), ("if_alpha_limit", ctypes.c_int), ("if_lumped", ctypes.c_int),
+        ("if_roundoff_fix", ctypes.c_int), ("precision", ctypes.c_int),
+    ]
+
+
+class Dump(ctypes.Structure):
+    _fields_ = [(n, ctypes.POINTER(ctypes.c_double)) for n in
+                ("dij_low", "muij_low", "alpha", "u_low", "res", "fctmat", "rminus", "lij")]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(str(build()))
+        L = _lib
+        vp, ip, dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)
+        L.orc_create.restype = vp
+        L.orc_create.argtypes = [ctypes.c_int, ctypes.c_int, ip, dp]
+        L.orc_destroy.argtypes = [vp]
+        L.orc_nnz.argtypes = [vp]
+        L.orc_get_matrices.argtypes = [vp, ip, ip, dp, dp, ip, dp, dp]
+        L.orc_gauss.argtypes = [vp, dp, dp]
+        L.orc_norms.argtypes = [vp, dp, dp, dp, dp]
+        L.orc_set_params.argtypes = [vp, ctypes.POINTER(Params)]
+        L.orc_get_params.argtypes = [vp, ctypes.POINTER(Params)]
+        L.orc_set_bath.argtypes = [vp, dp]
+        L.orc_set_dirichlet.argtypes = [vp, ctypes.c_int, ctypes.c_int, ip, dp]
+        L.orc_compute_dij.argtypes = [vp, dp, dp, dp]
+        L.orc_euler.argtypes = [vp, dp, dp, ctypes.POINTER(Dump)]
+        L.orc_fct_positivity.argtypes = [vp, dp, dp, dp]
+        L.orc_rk3_step.argtypes = [vp, dp, dp, ctypes.c_double]
+        L.orc_run.argtypes = [vp, dp, dp, ctypes.c_double, ctypes.c_int, ip]
+        L.orc_last_dt.restype = ctypes.c_double
+        L.orc_last_dt.argtypes = [vp]
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+class OracleError(RuntimeError):
+    def __init__(self, code, where):
+        super().__init__(f"oracle {where} failed with code {code}")
+        self.code = code
+
+
+class Oracle:
+    """The reference path restated on the CPU, in the reference's node numbering.
+
+    ``jj`` is (3, me) 1-based, ``rr`` is (2, np); states are (S, np) arrays
+    (stored column-major like the Fortran ``un(S, np)``).
+    """
+
+    def __init__(self, jj, rr):
+        L = lib()
+        self.jj = np.asfortranarray(jj, dtype=np.int32)
+        self.rr = np.asfortranarray(rr, dtype=np.float64)
+        self.np = self.rr.shape[1]
+        self.me = self.jj.shape[1]
+        self.h = L.orc_create(self.np, self.me, _ip(self.jj), _dp(self.rr))
+        if not self.h:
+            raise OracleError(-1, "create")
+        self.nnz = L.orc_nnz(self.h)
+        self.params = None
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def matrices(self):
+        n, z = self.np, self.nnz
+        ia = np.zeros(n + 1, np.int32); ja = np.zeros(z, np.int32)
+        mass = np.zeros(z); lumped = np.zeros(n); diag = np.zeros(n, np.int32)
+        cx = np.zeros(z); cy = np.zeros(z)
+        lib().orc_get_matrices(self.h, _ip(ia), _ip(ja), _dp(mass), _dp(lumped), _ip(diag), _dp(cx), _dp(cy))
+        return dict(ia=ia, ja=ja, mass=mass, lumped=lumped, diag=diag, cx=cx, cy=cy)
+
+    def gauss(self):
+        rj = np.zeros(3 * self.me); rg = np.zeros(6 * self.me)
+        lib().orc_gauss(self.h, _dp(rj), _dp(rg))
+        return rj, rg.reshape(-1, 2).T.copy()
+
+    def norms(self, ff, f_anal):
+        ff = np.ascontiguousarray(ff, np.float64); fa = np.ascontiguousarray(f_anal, np.float64)
+        l1 = ctypes.c_double(); l2 = ctypes.c_double()
+        lib().orc_norms(self.h, _dp(ff), _dp(fa), ctypes.byref(l1), ctypes.byref(l2))
+        return l1.value, l2.value
+
+    def set_params(self, p: Params):
+        rc = lib().orc_set_params(self.h, ctypes.byref(p))
+        if rc:
+            raise OracleError(rc, "set_params")
+        self.params = p
+
+    def get_params(self) -> Params:
+        p = Params()
+        lib().orc_get_params(self.h, ctypes.byref(p))
+        return p
+
+    def set_bath(self, bath):
+        b = np.ascontiguousarray(bath, np.float64)
+        lib().orc_set_bath(self.h, _dp(b))
+
+    def set_dirichlet(self, comp, js, vals=None):
+        js = np.ascontiguousarray(js, np.int32)
+        v = None if vals is None else np.ascontiguousarray(vals, np.float64)
+        rc = lib().orc_set_dirichlet(self.h, comp, len(js), _ip(js), None if v is None else _dp(v))
+        if rc:
+            raise OracleError(rc, "set_dirichlet")
+
+    def compute_dij(self, un):
+        u = np.asfortranarray(un, np.float64)
+        dij = np.zeros(self.nnz); dt = ctypes.c_double()
+        rc = lib().orc_compute_dij(self.h, _dp(u), _dp(dij), ctypes.byref(dt))
+        if rc:
+            raise OracleError(rc, "compute_dij")
+        return dij, dt.value
+
+    def euler(self, un, dump=False):
+        u = np.asfortranarray(un, np.float64)
+        out = np.zeros_like(u, order="F")
+        d = None
+        if dump:
+            z, n = self.nnz, self.np
+            arrs = dict(dij_low=np.zeros(z), muij_low=np.zeros(z), alpha=np.zeros(n),
+                        u_low=np.zeros_like(u, order="F"), res=np.zeros(n), fctmat=np.zeros(z),
+                        rminus=np.zeros(n), lij=np.zeros(z))
+            d = Dump(**{k: _dp(v) for k, v in arrs.items()})
+        rc = lib().orc_euler(self.h, _dp(u), _dp(out), ctypes.byref(d) if d is not None else None)
+        if rc:
+            raise OracleError(rc, "euler")
+        return (out, arrs) if dump else out
+
+    def fct_positivity(self, unext_scaled, fmat):
+        u = np.ascontiguousarray(unext_scaled, np.float64); f = np.ascontiguousarray(fmat, np.float64)
+        lij = np.zeros(self.nnz)
+        lib().orc_fct_positivity(self.h, _dp(u), _dp(f), _dp(lij))
+        return lij
+
+    def rk3_step(self, un, time, fixed_dt=0.0):
+        t = ctypes.c_double(time)
+        rc = lib().orc_rk3_step(self.h, _dp(un), ctypes.byref(t), fixed_dt)
+        if rc:
+            raise OracleError(rc, "rk3_step")
+        return t.value
+
+    def run(self, un, time, tfinal, max_steps=1 << 30):
+        """In-place DO WHILE(time < Tfinal) loop; returns (time, nsteps)."""
+        assert un.flags.f_contiguous and un.dtype == np.float64
+        t = ctypes.c_double(time); n = ctypes.c_int()
+        rc = lib().orc_run(self.h, _dp(un), ctypes.byref(t), tfinal, max_steps, ctypes.byref(n))
+        if rc:
+            raise OracleError(rc, "run")
+        return t.value, n.value
+
+    @property
+    def last_dt(self):
+        return lib().orc_last_dt(self.h)

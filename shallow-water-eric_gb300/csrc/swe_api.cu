@@ -1,0 +1,710 @@
+// C-ABI layer (include/swe_gpu.h): context, device buffers, permuting
+// transfers, the per-call operators mirroring MODULE update / MODULE fct, and
+// the device-resident SSP-RK3 loop captured in a CUDA graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/swe_gpu.h"
+#include "swe_kernels.hpp"
+#include "swe_setup.hpp"
+
+#define SWE_API extern "C" __attribute__((visibility("default")))
+
+using namespace swe;
+
+namespace {
+
+struct DevBuf {
+  std::vector<void*> ptrs;
+  template <typename T> T* alloc(size_t n, cudaError_t& st) {
+    void* p = nullptr;
+    if (st != cudaSuccess) return nullptr;
+    st = cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T));
+    if (st == cudaSuccess) { ptrs.push_back(p); cudaMemset(p, 0, std::max<size_t>(n, 1) * sizeof(T)); }
+    return (T*)p;
+  }
+  void release() { for (void* p : ptrs) cudaFree(p); ptrs.clear(); }
+};
+
+}  // namespace
+
+struct swe_ctx {
+  int dev = 0;
+  cudaStream_t stream = nullptr;
+  int n_inst = 0, S = 3, precision = 0;
+  std::vector<HostMesh> meshes;
+  std::vector<swe_params> params;
+  Layout L;
+  std::vector<int64_t> node_off;         // concatenated host node offsets, n_inst+1
+  DevBuf buf;
+  Graph G{};
+  InstConst* d_C = nullptr;
+  InstState* d_St = nullptr;
+  unsigned* d_err = nullptr;
+  int* d_row_of_node = nullptr;          // concatenated host node -> device row
+  double* d_stage = nullptr;             // staging (S, total nodes), reference layout
+  uint8_t* d_dir_mask = nullptr;
+  double* d_dir_val = nullptr;
+  std::vector<uint8_t> h_dir_mask;
+  std::vector<double> h_dir_val;
+  // FP64 path
+  StateF64 A{}, B{}, Cs{};
+  WorkF64 w{};
+  double* d_lij = nullptr;
+  // mixed path
+  StateMix mA{}, mB{}, mC{};
+  WorkMix wm{};
+  double* d_mass_acc = nullptr;
+  // graph of `graph_steps` time steps
+  cudaGraphExec_t gexec = nullptr;
+  int graph_steps = 0;
+  int block = 128;
+  long long last_launches = 0;
+  bool euler_done = false;
+  int euler_inst = -1;
+  std::string err;
+  std::string tuning = "thread-per-row SELL-32, block 128";
+};
+
+static int fail(swe_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+static int cuda_check(swe_ctx* c, cudaError_t e, const char* where) {
+  if (e == cudaSuccess) return SWE_OK;
+  return fail(c, SWE_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(expr)                                                   \
+  do {                                                             \
+    int _rc = cuda_check(c, (expr), #expr);                        \
+    if (_rc) return _rc;                                           \
+  } while (0)
+
+static InstConst make_const(const swe_params& p) {
+  InstConst k{};
+  k.g = p.gravity; k.htiny = p.htiny; k.cfl = p.cfl; k.mannings = p.mannings; k.lambda_sgn = p.lambda_sgn;
+  k.max_water_h = p.max_water_h;
+  k.rescale_floor = 1.e-10 * p.gravity * (p.max_water_h * p.max_water_h);   // update.f90:866
+  k.type_test = p.type_test; k.S = p.syst_size; k.visc = p.viscosity_type; k.viscous_type = p.viscous_type;
+  k.alpha_limit = p.if_alpha_limit; k.roundoff_fix = p.if_roundoff_fix;
+  return k;
+}
+
+static int check_params(swe_ctx* c, const swe_params& p) {
+  if (p.syst_size != 3 && p.syst_size != 5) return fail(c, SWE_ERR_ARG, "syst_size must be 3 or 5");
+  if ((p.syst_size == 5) != (p.type_test == 13)) return fail(c, SWE_ERR_ARG, "syst_size 5 goes with type_test 13");
+  if (!p.if_lumped) return fail(c, SWE_ERR_ARG, "only the lumped-mass step is supported (if_lumped)");
+  if (p.viscosity_type != SWE_VISC_FCT && p.viscosity_type != SWE_VISC_VISCOUS)
+    return fail(c, SWE_ERR_ARG, "viscosity_type must be 'fct' or 'viscous'");
+  if (p.viscous_type != 2) return fail(c, SWE_ERR_ARG, "viscous_type must be 'type2'");
+  if (p.precision != SWE_PREC_FP64 && p.precision != SWE_PREC_MIXED) return fail(c, SWE_ERR_ARG, "bad precision");
+  if (!(p.htiny >= 0.0) || !(p.gravity > 0.0)) return fail(c, SWE_ERR_ARG, "gravity must be > 0, htiny >= 0");
+  return SWE_OK;
+}
+
+static int alloc_state_f64(swe_ctx* c, StateF64& s, cudaError_t& st) {
+  const size_t n = c->L.n_rows;
+  s.h = c->buf.alloc<double>(n, st); s.q1 = c->buf.alloc<double>(n, st); s.q2 = c->buf.alloc<double>(n, st);
+  if (c->S == 5) { s.q3 = c->buf.alloc<double>(n, st); s.q4 = c->buf.alloc<double>(n, st); }
+  return st == cudaSuccess ? SWE_OK : SWE_ERR_CUDA;
+}
+
+static int alloc_state_mix(swe_ctx* c, StateMix& s, cudaError_t& st) {
+  const size_t n = c->L.n_rows;
+  s.h = c->buf.alloc<double>(n, st); s.hf = c->buf.alloc<float>(n, st);
+  s.q1 = c->buf.alloc<float>(n, st); s.q2 = c->buf.alloc<float>(n, st);
+  if (c->S == 5) { s.q3 = c->buf.alloc<float>(n, st); s.q4 = c->buf.alloc<float>(n, st); }
+  return st == cudaSuccess ? SWE_OK : SWE_ERR_CUDA;
+}
+
+template <typename T>
+static T* upload_vec(swe_ctx* c, const std::vector<T>& v, cudaError_t& st) {
+  T* d = c->buf.alloc<T>(v.size(), st);
+  if (st == cudaSuccess && !v.empty()) st = cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+  return d;
+}
+
+static int build_device(swe_ctx* c, const std::vector<std::vector<double>>& baths) {
+  c->L = build_layout(c->meshes, baths);
+  const Layout& L = c->L;
+  cudaError_t st = cudaSuccess;
+  Graph& G = c->G;
+  G.n_rows = L.n_rows;
+  G.slice_ptr = upload_vec(c, L.slice_ptr, st);
+  G.slice_inst = upload_vec(c, L.slice_inst, st);
+  G.col = upload_vec(c, L.col, st);
+  G.len = upload_vec(c, L.len, st);
+  G.dpos = upload_vec(c, L.dpos, st);
+  G.lumped = upload_vec(c, L.lumped, st);
+  std::vector<double> inv(L.n_rows);
+  for (int64_t r = 0; r < L.n_rows; r++) inv[r] = 1.0 / L.lumped[r];
+  G.inv_lumped = upload_vec(c, inv, st);
+  G.bath = upload_vec(c, L.bath, st);
+  if (c->precision == SWE_PREC_FP64) {
+    G.cx = upload_vec(c, L.cx, st);
+    G.cy = upload_vec(c, L.cy, st);
+  } else {
+    std::vector<float> f(L.n_entries);
+    for (int64_t e = 0; e < L.n_entries; e++) f[e] = (float)L.cx[e];
+    G.cxf = upload_vec(c, f, st);
+    for (int64_t e = 0; e < L.n_entries; e++) f[e] = (float)L.cy[e];
+    G.cyf = upload_vec(c, f, st);
+    std::vector<float> bf(L.n_rows);
+    for (int64_t r = 0; r < L.n_rows; r++) bf[r] = (float)L.bath[r];
+    G.bathf = upload_vec(c, bf, st);
+  }
+  c->h_dir_mask.assign(L.n_rows, 0);
+  c->h_dir_val.assign((size_t)c->S * L.n_rows, 0.0);
+  c->d_dir_mask = c->buf.alloc<uint8_t>(L.n_rows, st);
+  c->d_dir_val = c->buf.alloc<double>((size_t)c->S * L.n_rows, st);
+  G.dir_mask = c->d_dir_mask;
+  G.dir_val = c->d_dir_val;
+  // per-instance constants and state
+  std::vector<InstConst> hc(c->n_inst);
+  std::vector<InstState> hs(c->n_inst);
+  for (int b = 0; b < c->n_inst; b++) {
+    hc[b] = make_const(c->params[b]);
+    hs[b] = InstState{};
+    hs[b].dt = c->params[b].dt;
+    hs[b].inv_dt = c->params[b].dt > 0 ? 1.0 / c->params[b].dt : 0.0;
+    hs[b].t_final = 1e300;
+  }
+  c->d_C = upload_vec(c, hc, st);
+  c->d_St = upload_vec(c, hs, st);
+  c->d_err = c->buf.alloc<unsigned>(1, st);
+  // host node -> device row map, staging buffer
+  c->node_off.assign(c->n_inst + 1, 0);
+  for (int b = 0; b < c->n_inst; b++) c->node_off[b + 1] = c->node_off[b] + c->meshes[b].np;
+  std::vector<int> row_of_node(c->node_off[c->n_inst]);
+  for (int b = 0; b < c->n_inst; b++)
+    for (int i = 0; i < c->meshes[b].np; i++) row_of_node[c->node_off[b] + i] = L.new_of_old[b][i];
+  c->d_row_of_node = upload_vec(c, row_of_node, st);
+  c->d_stage = c->buf.alloc<double>((size_t)c->S * c->node_off[c->n_inst], st);
+  c->d_mass_acc = c->buf.alloc<double>(2 * (size_t)c->n_inst, st);
+  const size_t n = L.n_rows, ne = L.n_entries;
+  if (c->precision == SWE_PREC_FP64) {
+    alloc_state_f64(c, c->A, st); alloc_state_f64(c, c->B, st); alloc_state_f64(c, c->Cs, st);
+    WorkF64& w = c->w;
+    w.ovh = c->buf.alloc<double>(n, st); w.v1 = c->buf.alloc<double>(n, st); w.v2 = c->buf.alloc<double>(n, st);
+    w.ent = c->buf.alloc<double>(n, st); w.alpha = c->buf.alloc<double>(n, st);
+    w.dL = c->buf.alloc<double>(ne, st); w.muL = c->buf.alloc<double>(ne, st); w.fct = c->buf.alloc<double>(ne, st);
+    w.res = c->buf.alloc<double>(n, st); w.rminus = c->buf.alloc<double>(n, st);
+    alloc_state_f64(c, w.uL, st);
+    c->d_lij = c->buf.alloc<double>(ne, st);
+  } else {
+    alloc_state_mix(c, c->mA, st); alloc_state_mix(c, c->mB, st); alloc_state_mix(c, c->mC, st);
+    WorkMix& w = c->wm;
+    w.alpha = c->buf.alloc<float>(n, st); w.res = c->buf.alloc<float>(n, st);
+    w.rminus = c->buf.alloc<double>(n, st);
+    w.dL = c->buf.alloc<float>(ne, st); w.muL = c->buf.alloc<float>(ne, st);
+    alloc_state_mix(c, w.uL, st);
+  }
+  if (st != cudaSuccess) return fail(c, SWE_ERR_CUDA, std::string("device allocation: ") + cudaGetErrorString(st));
+  return SWE_OK;
+}
+
+// ---- permuting transfers (reference layout <-> SoA device rows) ----
+__global__ void k_scatter_in(const double* __restrict__ stage, const int* __restrict__ row_of_node, int64_t n_nodes,
+                             int S, StateF64 a) {
+  int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (n >= n_nodes) return;
+  const int64_t r = row_of_node[n];
+  double* comp[5] = {a.h, a.q1, a.q2, a.q3, a.q4};
+  for (int k = 0; k < S; k++) comp[k][r] = stage[n * S + k];
+}
+__global__ void k_gather_out(double* __restrict__ stage, const int* __restrict__ row_of_node, int64_t n_nodes, int S,
+                             StateF64 a) {
+  int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (n >= n_nodes) return;
+  const int64_t r = row_of_node[n];
+  const double* comp[5] = {a.h, a.q1, a.q2, a.q3, a.q4};
+  for (int k = 0; k < S; k++) stage[n * S + k] = comp[k][r];
+}
+__global__ void k_scatter_in_mix(const double* __restrict__ stage, const int* __restrict__ row_of_node,
+                                 int64_t n_nodes, int S, StateMix a) {
+  int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (n >= n_nodes) return;
+  const int64_t r = row_of_node[n];
+  const double h = stage[n * S];
+  a.h[r] = h;
+  a.hf[r] = (float)h;
+  a.q1[r] = (float)stage[n * S + 1];
+  a.q2[r] = (float)stage[n * S + 2];
+  if (S == 5) { a.q3[r] = (float)stage[n * S + 3]; a.q4[r] = (float)stage[n * S + 4]; }
+}
+__global__ void k_gather_out_mix(double* __restrict__ stage, const int* __restrict__ row_of_node, int64_t n_nodes,
+                                 int S, StateMix a) {
+  int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (n >= n_nodes) return;
+  const int64_t r = row_of_node[n];
+  stage[n * S] = a.h[r];
+  stage[n * S + 1] = a.q1[r];
+  stage[n * S + 2] = a.q2[r];
+  if (S == 5) { stage[n * S + 3] = a.q3[r]; stage[n * S + 4] = a.q4[r]; }
+}
+
+static int to_device(swe_ctx* c, const double* un, bool device_src, int64_t node_begin, int64_t node_end) {
+  const int64_t nn = node_end - node_begin;
+  if (nn <= 0) return SWE_OK;
+  const size_t bytes = (size_t)c->S * nn * sizeof(double);
+  CK(cudaMemcpyAsync(c->d_stage + (size_t)c->S * node_begin, un, bytes,
+                     device_src ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream));
+  const unsigned nb = (unsigned)((nn + 255) / 256);
+  if (c->precision == SWE_PREC_FP64)
+    k_scatter_in<<<nb, 256, 0, c->stream>>>(c->d_stage + (size_t)c->S * node_begin, c->d_row_of_node + node_begin,
+                                             nn, c->S, c->A);
+  else
+    k_scatter_in_mix<<<nb, 256, 0, c->stream>>>(c->d_stage + (size_t)c->S * node_begin,
+                                                 c->d_row_of_node + node_begin, nn, c->S, c->mA);
+  CK(cudaGetLastError());
+  return SWE_OK;
+}
+
+static int from_device_state(swe_ctx* c, double* un, bool device_dst, int64_t node_begin, int64_t node_end,
+                             const StateF64* sf, const StateMix* sm) {
+  const int64_t nn = node_end - node_begin;
+  if (nn <= 0) return SWE_OK;
+  const unsigned nb = (unsigned)((nn + 255) / 256);
+  double* stg = c->d_stage + (size_t)c->S * node_begin;
+  if (sf) k_gather_out<<<nb, 256, 0, c->stream>>>(stg, c->d_row_of_node + node_begin, nn, c->S, *sf);
+  else k_gather_out_mix<<<nb, 256, 0, c->stream>>>(stg, c->d_row_of_node + node_begin, nn, c->S, *sm);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(un, stg, (size_t)c->S * nn * sizeof(double),
+                     device_dst ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream));
+  return SWE_OK;
+}
+
+static int read_errors(swe_ctx* c) {
+  unsigned e = 0;
+  CK(cudaMemcpyAsync(&e, c->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (e) CK(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned), c->stream));
+  if (e & ERRB_NAN) return fail(c, SWE_ERR_NAN, "non-finite state produced");
+  if (e & ERRB_DELTA) return fail(c, SWE_ERR_DELTA, "BUG in compute_lambda_vacc: Delta < 0");
+  if (e & ERRB_NEG_H) return fail(c, SWE_ERR_NEG_H, "Min h<0, STOP");
+  return SWE_OK;
+}
+
+static int set_inst_state_dt(swe_ctx* c, int inst, double dt, int done_others) {
+  std::vector<InstState> hs(c->n_inst);
+  CK(cudaMemcpyAsync(hs.data(), c->d_St, sizeof(InstState) * c->n_inst, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  for (int b = 0; b < c->n_inst; b++) {
+    if (b == inst) { hs[b].dt = dt; hs[b].inv_dt = 1.0 / dt; hs[b].done = 0; }
+    else if (done_others) hs[b].done = 1;
+  }
+  CK(cudaMemcpyAsync(c->d_St, hs.data(), sizeof(InstState) * c->n_inst, cudaMemcpyHostToDevice, c->stream));
+  return SWE_OK;
+}
+
+static int restore_done(swe_ctx* c, const std::vector<InstState>& saved) {
+  CK(cudaMemcpyAsync(c->d_St, saved.data(), sizeof(InstState) * c->n_inst, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return SWE_OK;
+}
+
+static int save_state(swe_ctx* c, std::vector<InstState>& saved) {
+  saved.resize(c->n_inst);
+  CK(cudaMemcpyAsync(saved.data(), c->d_St, sizeof(InstState) * c->n_inst, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return SWE_OK;
+}
+
+static void enqueue_step(swe_ctx* c) {
+  const cudaStream_t s = c->stream;
+  if (c->precision == SWE_PREC_FP64) {
+    launch_dt_f64(c->G, c->d_C, c->d_St, c->A, nullptr, c->d_err, c->block, s);
+    launch_step_begin(c->d_C, c->d_St, c->n_inst, s);
+    StageArgs a{c->G, c->d_C, c->d_St, c->A, c->A, c->B, c->w, 1, nullptr, c->d_err, c->block};
+    launch_stage_f64(a, s);
+    a.u = c->B; a.out = c->Cs; a.rk_stage = 2;
+    launch_stage_f64(a, s);
+    a.u = c->Cs; a.out = c->A; a.rk_stage = 3;
+    launch_stage_f64(a, s);
+  } else {
+    launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->d_err, c->block, s);
+    launch_step_begin(c->d_C, c->d_St, c->n_inst, s);
+    StageArgsMix a{c->G, c->d_C, c->d_St, c->mA, c->mA, c->mB, c->wm, 1, c->d_err, c->block};
+    launch_stage_mix(a, s);
+    a.u = c->mB; a.out = c->mC; a.rk_stage = 2;
+    launch_stage_mix(a, s);
+    a.u = c->mC; a.out = c->mA; a.rk_stage = 3;
+    launch_stage_mix(a, s);
+  }
+  launch_step_end(c->d_St, c->n_inst, s);
+}
+
+static int build_graph(swe_ctx* c, int steps) {
+  if (c->gexec && c->graph_steps == steps) return SWE_OK;
+  if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  for (int k = 0; k < steps; k++) enqueue_step(c);
+  CK(cudaStreamEndCapture(c->stream, &g));
+  cudaError_t e = cudaGraphInstantiate(&c->gexec, g, 0);
+  cudaGraphDestroy(g);
+  CK(e);
+  c->graph_steps = steps;
+  return SWE_OK;
+}
+
+// ============================== C ABI ======================================
+
+static int create_common(swe_ctx** out, int n_inst, const int* np, const int* me, const int* jj, const double* rr,
+                         const double* bath, const swe_params* params) {
+  if (!out) return SWE_ERR_ARG;
+  *out = nullptr;
+  if (n_inst <= 0 || !np || !me || !jj || !rr || !bath || !params) return SWE_ERR_ARG;
+  swe_ctx* c = new swe_ctx;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    *out = c;
+    return fail(c, SWE_ERR_CUDA, "no CUDA device: this library has no CPU path");
+  }
+  cudaGetDevice(&c->dev);
+  c->n_inst = n_inst;
+  c->S = params[0].syst_size;
+  c->precision = params[0].precision;
+  c->params.assign(params, params + n_inst);
+  for (int b = 0; b < n_inst; b++) {
+    int rc = check_params(c, params[b]);
+    if (!rc && (params[b].syst_size != c->S || params[b].precision != c->precision))
+      rc = fail(c, SWE_ERR_ARG, "all instances must share syst_size and precision");
+    if (rc) { *out = c; return rc; }
+  }
+  c->meshes.resize(n_inst);
+  std::vector<std::vector<double>> baths(n_inst);
+  int64_t joff = 0, roff = 0;
+  for (int b = 0; b < n_inst; b++) {
+    HostMesh& m = c->meshes[b];
+    if (np[b] <= 0 || me[b] <= 0) { *out = c; return fail(c, SWE_ERR_ARG, "empty mesh"); }
+    m.np = np[b]; m.me = me[b];
+    m.jj.resize((size_t)3 * me[b]);
+    for (size_t q = 0; q < m.jj.size(); q++) m.jj[q] = jj[joff + q] - 1;
+    m.rr.assign(rr + 2 * roff, rr + 2 * (roff + np[b]));
+    baths[b].assign(bath + roff, bath + roff + np[b]);
+    joff += (int64_t)3 * me[b];
+    roff += np[b];
+    std::string e = construct_matrices(m);
+    if (!e.empty()) { *out = c; return fail(c, SWE_ERR_MESH, e); }
+  }
+  *out = c;
+  if (cuda_check(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate")) return SWE_ERR_CUDA;
+  int rc = build_device(c, baths);
+  if (rc) return rc;
+  return cuda_check(c, cudaDeviceSynchronize(), "setup");
+}
+
+SWE_API int swe_create(swe_ctx** ctx, int np, int me, const int* jj, const double* rr, const double* bath,
+                       const swe_params* params) {
+  return create_common(ctx, 1, &np, &me, jj, rr, bath, params);
+}
+
+SWE_API int swe_create_batch(swe_ctx** ctx, int n_inst, const int* np, const int* me, const int* jj, const double* rr,
+                             const double* bath, const swe_params* params) {
+  return create_common(ctx, n_inst, np, me, jj, rr, bath, params);
+}
+
+SWE_API void swe_destroy(swe_ctx* c) {
+  if (!c) return;
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  c->buf.release();
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+SWE_API const char* swe_last_error(const swe_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+SWE_API int swe_set_params(swe_ctx* c, int inst, const swe_params* p) {
+  if (!c || !p || inst < 0 || inst >= c->n_inst) return fail(c, SWE_ERR_ARG, "bad instance or params");
+  int rc = check_params(c, *p);
+  if (rc) return rc;
+  if (p->syst_size != c->S || p->precision != c->precision)
+    return fail(c, SWE_ERR_ARG, "syst_size and precision are fixed at creation");
+  c->params[inst] = *p;
+  InstConst k = make_const(*p);
+  CK(cudaMemcpyAsync(c->d_C + inst, &k, sizeof(InstConst), cudaMemcpyHostToDevice, c->stream));
+  std::vector<InstState> hs;
+  if ((rc = save_state(c, hs))) return rc;
+  hs[inst].dt = p->dt;
+  hs[inst].inv_dt = p->dt > 0 ? 1.0 / p->dt : 0.0;
+  return restore_done(c, hs);
+}
+
+SWE_API int swe_set_dirichlet(swe_ctx* c, int inst, int comp, int n, const int* js, const double* vals) {
+  if (!c || inst < 0 || inst >= c->n_inst || comp < 0 || comp >= c->S || n < 0 || (n > 0 && !js))
+    return fail(c, SWE_ERR_ARG, "bad Dirichlet arguments");
+  const Layout& L = c->L;
+  // clear the component on this instance, then set
+  for (int64_t r = L.row_off[inst]; r < L.row_off[inst + 1]; r++) c->h_dir_mask[r] &= (uint8_t)~(1u << comp);
+  for (int q = 0; q < n; q++) {
+    if (js[q] < 1 || js[q] > c->meshes[inst].np) return fail(c, SWE_ERR_ARG, "Dirichlet node out of range");
+    const int64_t r = L.new_of_old[inst][js[q] - 1];
+    c->h_dir_mask[r] |= (uint8_t)(1u << comp);
+    c->h_dir_val[(size_t)comp * L.n_rows + r] = vals ? vals[q] : 0.0;
+  }
+  CK(cudaMemcpyAsync(c->d_dir_mask, c->h_dir_mask.data(), L.n_rows, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->d_dir_val, c->h_dir_val.data(), c->h_dir_val.size() * sizeof(double), cudaMemcpyHostToDevice,
+                     c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return SWE_OK;
+}
+
+SWE_API int swe_sizes(const swe_ctx* c, int inst, int* np, int* nnz) {
+  if (!c || inst < 0 || inst >= c->n_inst) return SWE_ERR_ARG;
+  if (np) *np = c->meshes[inst].np;
+  if (nnz) *nnz = (int)c->meshes[inst].ja.size();
+  return SWE_OK;
+}
+
+SWE_API int swe_get_matrices(swe_ctx* c, int inst, int* ia, int* ja, double* mass, double* lumped, int* diag,
+                             double* cx, double* cy) {
+  if (!c || inst < 0 || inst >= c->n_inst) return fail(c, SWE_ERR_ARG, "bad instance");
+  const HostMesh& m = c->meshes[inst];
+  for (int i = 0; i <= m.np; i++) if (ia) ia[i] = m.ia[i] + 1;
+  for (size_t p = 0; p < m.ja.size(); p++) {
+    if (ja) ja[p] = m.ja[p] + 1;
+    if (mass) mass[p] = m.mass[p];
+    if (cx) cx[p] = m.cx[p];
+    if (cy) cy[p] = m.cy[p];
+  }
+  for (int i = 0; i < m.np; i++) {
+    if (lumped) lumped[i] = m.lumped[i];
+    if (diag) diag[i] = m.diag[i] + 1;
+  }
+  return SWE_OK;
+}
+
+// copy a per-entry device array of one instance back into CSR order
+template <typename T>
+static int entries_to_csr(swe_ctx* c, int inst, const T* d_arr, double* out) {
+  const Layout& L = c->L;
+  const int64_t s0 = L.row_off[inst] / 32, s1 = L.row_off[inst + 1] / 32;
+  const int64_t e0 = L.slice_ptr[s0], e1 = L.slice_ptr[s1];
+  std::vector<T> h(e1 - e0);
+  CK(cudaMemcpyAsync(h.data(), d_arr + e0, (e1 - e0) * sizeof(T), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  for (int64_t e = e0; e < e1; e++)
+    if (L.ref_pos[e] >= 0) out[L.ref_pos[e]] = (double)h[e - e0];
+  return SWE_OK;
+}
+
+template <typename T>
+static int rows_to_nodes(swe_ctx* c, int inst, const T* d_arr, double* out) {
+  const Layout& L = c->L;
+  const int64_t r0 = L.row_off[inst], r1 = L.row_off[inst + 1];
+  std::vector<T> h(r1 - r0);
+  CK(cudaMemcpyAsync(h.data(), d_arr + r0, (r1 - r0) * sizeof(T), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  for (int i = 0; i < c->meshes[inst].np; i++) out[i] = (double)h[L.new_of_old[inst][i] - r0];
+  return SWE_OK;
+}
+
+SWE_API int swe_compute_dij(swe_ctx* c, int inst, const double* un, double* dij, double* dt_out) {
+  if (!c || inst < 0 || inst >= c->n_inst || !un) return fail(c, SWE_ERR_ARG, "bad arguments");
+  if (c->precision != SWE_PREC_FP64) return fail(c, SWE_ERR_ARG, "swe_compute_dij is an FP64 operator");
+  int rc = to_device(c, un, false, c->node_off[inst], c->node_off[inst + 1]);
+  if (rc) return rc;
+  std::vector<InstState> saved;
+  if ((rc = save_state(c, saved))) return rc;
+  if ((rc = set_inst_state_dt(c, inst, c->params[inst].dt > 0 ? c->params[inst].dt : 1.0, 1))) return rc;
+  launch_dt_f64(c->G, c->d_C, c->d_St, c->A, c->w.dL, c->d_err, c->block, c->stream);
+  CK(cudaGetLastError());
+  if ((rc = read_errors(c))) { restore_done(c, saved); return rc; }
+  std::vector<double> d(c->meshes[inst].ja.size());
+  if ((rc = entries_to_csr(c, inst, c->w.dL, d.data()))) return rc;
+  if ((rc = restore_done(c, saved))) return rc;
+  if (dij) std::copy(d.begin(), d.end(), dij);
+  if (dt_out) {
+    const HostMesh& m = c->meshes[inst];
+    double mx = std::fabs(d[m.diag[0]]) / m.lumped[0];
+    for (int i = 1; i < m.np; i++) mx = std::max(mx, std::fabs(d[m.diag[i]]) / m.lumped[i]);
+    *dt_out = c->params[inst].cfl * 1 / mx;
+  }
+  return SWE_OK;
+}
+
+SWE_API int swe_euler(swe_ctx* c, int inst, const double* un, double* unext) {
+  if (!c || inst < 0 || inst >= c->n_inst || !un || !unext) return fail(c, SWE_ERR_ARG, "bad arguments");
+  if (!(c->params[inst].dt > 0)) return fail(c, SWE_ERR_ARG, "params.dt must be > 0 for swe_euler");
+  int rc = to_device(c, un, false, c->node_off[inst], c->node_off[inst + 1]);
+  if (rc) return rc;
+  std::vector<InstState> saved;
+  if ((rc = save_state(c, saved))) return rc;
+  if ((rc = set_inst_state_dt(c, inst, c->params[inst].dt, 1))) return rc;
+  if (c->precision == SWE_PREC_FP64) {
+    StageArgs a{c->G, c->d_C, c->d_St, c->A, c->A, c->B, c->w, 0, c->d_lij, c->d_err, c->block};
+    launch_stage_f64(a, c->stream);
+  } else {
+    StageArgsMix a{c->G, c->d_C, c->d_St, c->mA, c->mA, c->mB, c->wm, 0, c->d_err, c->block};
+    launch_stage_mix(a, c->stream);
+  }
+  CK(cudaGetLastError());
+  int erc = read_errors(c);
+  if ((rc = restore_done(c, saved))) return rc;
+  c->euler_done = true;
+  c->euler_inst = inst;
+  if ((rc = from_device_state(c, unext, false, c->node_off[inst], c->node_off[inst + 1],
+                              c->precision == SWE_PREC_FP64 ? &c->B : nullptr,
+                              c->precision == SWE_PREC_FP64 ? nullptr : &c->mB)))
+    return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return erc;
+}
+
+SWE_API int swe_euler_intermediates(swe_ctx* c, int inst, double* dij_low, double* muij_low, double* alpha,
+                                    double* u_low, double* res, double* fctmat, double* rminus, double* lij) {
+  if (!c || inst < 0 || inst >= c->n_inst) return fail(c, SWE_ERR_ARG, "bad instance");
+  if (!c->euler_done || c->euler_inst != inst) return fail(c, SWE_ERR_ARG, "call swe_euler on this instance first");
+  int rc;
+  if (c->precision == SWE_PREC_FP64) {
+    if (dij_low && (rc = entries_to_csr(c, inst, c->w.dL, dij_low))) return rc;
+    if (muij_low && (rc = entries_to_csr(c, inst, c->w.muL, muij_low))) return rc;
+    if (fctmat && (rc = entries_to_csr(c, inst, c->w.fct, fctmat))) return rc;
+    if (lij && (rc = entries_to_csr(c, inst, c->d_lij, lij))) return rc;
+    if (alpha && (rc = rows_to_nodes(c, inst, c->w.alpha, alpha))) return rc;
+    if (res && (rc = rows_to_nodes(c, inst, c->w.res, res))) return rc;
+    if (rminus && (rc = rows_to_nodes(c, inst, c->w.rminus, rminus))) return rc;
+    if (u_low && (rc = from_device_state(c, u_low, false, c->node_off[inst], c->node_off[inst + 1], &c->w.uL, nullptr)))
+      return rc;
+  } else {
+    if (dij_low && (rc = entries_to_csr(c, inst, c->wm.dL, dij_low))) return rc;
+    if (muij_low && (rc = entries_to_csr(c, inst, c->wm.muL, muij_low))) return rc;
+    if (alpha && (rc = rows_to_nodes(c, inst, c->wm.alpha, alpha))) return rc;
+    if (res && (rc = rows_to_nodes(c, inst, c->wm.res, res))) return rc;
+    if (rminus && (rc = rows_to_nodes(c, inst, c->wm.rminus, rminus))) return rc;
+    if (u_low && (rc = from_device_state(c, u_low, false, c->node_off[inst], c->node_off[inst + 1], nullptr, &c->wm.uL)))
+      return rc;
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return SWE_OK;
+}
+
+SWE_API int swe_fct_positivity(swe_ctx* c, int inst, const double* unext, const double* mat, double* lij) {
+  if (!c || inst < 0 || inst >= c->n_inst || !unext || !mat || !lij) return fail(c, SWE_ERR_ARG, "bad arguments");
+  if (c->precision != SWE_PREC_FP64) return fail(c, SWE_ERR_ARG, "swe_fct_positivity is an FP64 operator");
+  const Layout& L = c->L;
+  const HostMesh& m = c->meshes[inst];
+  std::vector<double> hrow(L.n_rows, 0.0), hent(L.n_entries, 0.0);
+  for (int i = 0; i < m.np; i++) hrow[L.new_of_old[inst][i]] = unext[i];
+  const int64_t s0 = L.row_off[inst] / 32, s1 = L.row_off[inst + 1] / 32;
+  for (int64_t e = L.slice_ptr[s0]; e < L.slice_ptr[s1]; e++)
+    if (L.ref_pos[e] >= 0) hent[e] = mat[L.ref_pos[e]];
+  CK(cudaMemcpyAsync(c->w.uL.h, hrow.data(), L.n_rows * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->w.fct, hent.data(), L.n_entries * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  launch_fct_positivity_f64(c->G, c->d_C, c->w.uL.h, c->w.fct, c->w.rminus, c->d_lij, c->stream);
+  CK(cudaGetLastError());
+  c->euler_done = false;
+  return entries_to_csr(c, inst, c->d_lij, lij);
+}
+
+SWE_API int swe_upload(swe_ctx* c, const double* un) {
+  if (!c || !un) return fail(c, SWE_ERR_ARG, "bad arguments");
+  int rc = to_device(c, un, false, 0, c->node_off[c->n_inst]);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return SWE_OK;
+}
+
+SWE_API int swe_download(swe_ctx* c, double* un) {
+  if (!c || !un) return fail(c, SWE_ERR_ARG, "bad arguments");
+  int rc = from_device_state(c, un, false, 0, c->node_off[c->n_inst], c->precision == SWE_PREC_FP64 ? &c->A : nullptr,
+                             c->precision == SWE_PREC_FP64 ? nullptr : &c->mA);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return SWE_OK;
+}
+
+SWE_API int swe_upload_device(swe_ctx* c, const double* d_un) {
+  if (!c || !d_un) return fail(c, SWE_ERR_ARG, "bad arguments");
+  int rc = to_device(c, d_un, true, 0, c->node_off[c->n_inst]);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return SWE_OK;
+}
+
+SWE_API int swe_download_device(swe_ctx* c, double* d_un) {
+  if (!c || !d_un) return fail(c, SWE_ERR_ARG, "bad arguments");
+  int rc = from_device_state(c, d_un, true, 0, c->node_off[c->n_inst], c->precision == SWE_PREC_FP64 ? &c->A : nullptr,
+                             c->precision == SWE_PREC_FP64 ? nullptr : &c->mA);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return SWE_OK;
+}
+
+SWE_API int swe_set_time(swe_ctx* c, const double* time, const double* t_final) {
+  if (!c) return SWE_ERR_ARG;
+  std::vector<InstState> hs;
+  int rc = save_state(c, hs);
+  if (rc) return rc;
+  for (int b = 0; b < c->n_inst; b++) {
+    if (time) hs[b].time = time[b];
+    if (t_final) hs[b].t_final = t_final[b];
+    hs[b].done = 0;
+    hs[b].steps = 0;
+    hs[b].maxd_bits = 0ull;
+  }
+  return restore_done(c, hs);
+}
+
+SWE_API int swe_rk3_steps(swe_ctx* c, int nsteps, double* time_out, double* dt_out, int* steps_done) {
+  if (!c || nsteps < 0) return fail(c, SWE_ERR_ARG, "bad arguments");
+  int rc;
+  std::vector<InstState> hs;
+  if ((rc = save_state(c, hs))) return rc;
+  for (auto& s : hs) { s.steps = 0; s.maxd_bits = 0ull; }
+  if ((rc = restore_done(c, hs))) return rc;
+  const int chunk = nsteps >= 8 ? 8 : 1;
+  long long launches = 0;
+  const long long per_step = 3LL * kLaunchesPerStage + kLaunchesPerStepExtra;
+  if (nsteps >= chunk && chunk > 1) {
+    if ((rc = build_graph(c, chunk))) return rc;
+    for (int k = 0; k + chunk <= nsteps; k += chunk) {
+      CK(cudaGraphLaunch(c->gexec, c->stream));
+      launches += per_step * chunk;
+    }
+  }
+  const int rem = chunk > 1 ? nsteps % chunk : nsteps;
+  for (int k = 0; k < rem; k++) {
+    enqueue_step(c);
+    launches += per_step;
+  }
+  CK(cudaGetLastError());
+  c->last_launches = launches;
+  c->euler_done = false;
+  rc = read_errors(c);
+  std::vector<InstState> out;
+  int rc2 = save_state(c, out);
+  if (rc2) return rc2;
+  for (int b = 0; b < c->n_inst; b++) {
+    if (time_out) time_out[b] = out[b].time;
+    if (dt_out) dt_out[b] = out[b].dt;
+  }
+  if (steps_done) *steps_done = out[0].steps;
+  return rc;
+}
+
+SWE_API int swe_mass(swe_ctx* c, double* mass_out) {
+  if (!c || !mass_out) return fail(c, SWE_ERR_ARG, "bad arguments");
+  CK(cudaMemsetAsync(c->d_mass_acc, 0, 2 * sizeof(double) * c->n_inst, c->stream));
+  launch_mass_f64(c->G, c->precision == SWE_PREC_FP64 ? c->A.h : c->mA.h, c->d_mass_acc, c->stream);
+  CK(cudaGetLastError());
+  std::vector<double> acc(2 * c->n_inst);
+  CK(cudaMemcpyAsync(acc.data(), c->d_mass_acc, acc.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  for (int b = 0; b < c->n_inst; b++) mass_out[b] = acc[2 * b] + acc[2 * b + 1];
+  return SWE_OK;
+}
+
+SWE_API long long swe_last_launch_count(const swe_ctx* c) { return c ? c->last_launches : 0; }
+SWE_API const char* swe_tuning(const swe_ctx* c) { return c ? c->tuning.c_str() : ""; }

@@ -1,0 +1,120 @@
+// Device-side data layout and per-edge physics shared by the FP64 and the
+// mixed-precision kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace swe {
+
+// Error bits raised by kernels (never a trap); the host maps them to
+// SWE_ERR_* after each launch sequence.
+enum : unsigned { ERRB_NEG_H = 1u, ERRB_DELTA = 2u, ERRB_NAN = 4u };
+
+// Per-instance constants (one record per mesh of a batch).
+struct InstConst {
+  double g, htiny, cfl, mannings, lambda_sgn, max_water_h, rescale_floor;
+  int type_test, S, visc, viscous_type, alpha_limit, roundoff_fix;
+};
+
+// Per-instance time-loop state, device resident.
+struct InstState {
+  double dt, inv_dt, time, t_final;
+  unsigned long long maxd_bits;   // max |d_ii|/m_i of the current step (double bits)
+  int done, steps;
+};
+
+// The SELL-32 edge graph (see swe_setup.hpp).  Entry k of row r is at
+// slice_ptr[r>>5] + 32*k + (r&31).
+struct Graph {
+  int64_t n_rows;
+  const int64_t* __restrict__ slice_ptr;
+  const int* __restrict__ slice_inst;
+  const int* __restrict__ col;
+  const uint8_t* __restrict__ len;
+  const uint8_t* __restrict__ dpos;
+  const double* __restrict__ cx;
+  const double* __restrict__ cy;
+  const float* __restrict__ cxf;
+  const float* __restrict__ cyf;
+  const double* __restrict__ lumped;
+  const double* __restrict__ inv_lumped;
+  const double* __restrict__ bath;
+  const float* __restrict__ bathf;
+  const uint8_t* __restrict__ dir_mask;   // bit k: component k is Dirichlet
+  const double* __restrict__ dir_val;     // (S, n_rows) SoA, read where masked
+};
+
+__device__ __forceinline__ int64_t entry_base(const Graph& G, int64_t r) {
+  return G.slice_ptr[r >> 5] + (r & 31);
+}
+
+template <typename T> __device__ __forceinline__ T tmax(T a, T b) { return a > b ? a : b; }
+template <typename T> __device__ __forceinline__ T tmin(T a, T b) { return a < b ? a : b; }
+template <typename T> __device__ __forceinline__ T tabs(T a) { return a < T(0) ? -a : a; }
+
+// compute_one_over_h (SOURCES/condlim.f90:79-90): 2h/(h^2 + max(h,htiny)^2)
+template <typename T> __device__ __forceinline__ T one_over_h(T h, T htiny) {
+  T mh = tmax(h, htiny);
+  return T(2) * h / (h * h + mh * mh);
+}
+
+// phi (SOURCES/condlim.f90:960-981)
+template <typename T>
+__device__ __forceinline__ T phi_fn(T h, T ul, T hl, T ur, T hr, T g, T htiny) {
+  T fl, fr;
+  if (h > hl) {
+    T ovh = one_over_h(h, htiny), ovhl = one_over_h(hl, htiny);
+    fl = (h - hl) * sqrt((g / T(2)) * (ovh + ovhl));
+  } else {
+    fl = T(2) * (sqrt(g * h) - sqrt(g * hl));
+  }
+  if (h > hr) {
+    T ovh = one_over_h(h, htiny), ovhr = one_over_h(hr, htiny);
+    fr = (h - hr) * sqrt((g / T(2)) * (ovh + ovhr));
+  } else {
+    fr = T(2) * (sqrt(g * h) - sqrt(g * hr));
+  }
+  return fl + fr + ur - ul;
+}
+
+// compute_lambda_vacc (SOURCES/condlim.f90:879-957) with ovhl/ovhr passed in
+// (they equal the node's one_over_h bit for bit).  Returns false where the
+// reference STOPs (Delta < 0).
+template <typename T>
+__device__ __forceinline__ bool lambda_vacc(T hl, T qxl, T qyl, T ovhl, T hr, T qxr, T qyr, T ovhr,
+                                            T nx, T ny, T g, T htiny, T sqrt2, T* lambda) {
+  T vl = (qxl * nx + qyl * ny) * ovhl;
+  T vr = (qxr * nx + qyr * ny) * ovhr;
+  T sql = sqrt(g * tabs(hl));
+  T sqr = sqrt(g * tabs(hr));
+  T t0 = T(2) * sqrt2 - T(1);
+  T x0 = t0 * t0;
+  T hmin, hmax;
+  if (hl <= hr) { hmin = hl; hmax = hr; } else { hmin = hr; hmax = hl; }
+  T ht;
+  bool ok = true;
+  T fh = phi_fn(x0 * hmin, vl, hl, vr, hr, g, htiny);
+  if (T(0) <= fh) {
+    T s = tmax(vl - vr + T(2) * sql + T(2) * sqr, T(0));
+    ht = tmin(x0 * hmin, s * s / (T(16) * g));
+  } else {
+    fh = phi_fn(x0 * hmax, vl, hl, vr, hr, g, htiny);
+    T sqrmin = sqrt(hmin), sqrmax = sqrt(hmax);
+    if (T(0) <= fh) {
+      T a = T(1) / (T(2) * sqrt2);
+      T c = -(hmin * a) - sqrmin * sqrmax + sqrmin * (vr - vl) / (T(2) * sqrt(g));
+      T Delta = hmin - T(4) * a * c;
+      if (Delta < T(0)) { ok = false; Delta = T(0); }
+      T s = (-sqrmin + sqrt(Delta)) / (T(2) * a);
+      ht = tmin(x0 * hmax, s * s);
+    } else {
+      ht = sqrmin * sqrmax * (T(1) + sqrt(T(2) / g) * (vl - vr) / (sqrmin + sqrmax));
+    }
+  }
+  T lbdl = vl - sql * sqrt((T(1) + tmax((ht - hl) * ovhl / T(2), T(0))) * (T(1) + tmax((ht - hl) * ovhl, T(0))));
+  T lbdr = vr + sqr * sqrt((T(1) + tmax((ht - hr) * ovhr / T(2), T(0))) * (T(1) + tmax((ht - hr) * ovhr, T(0))));
+  *lambda = tmax(tabs(lbdl), tabs(lbdr));
+  return ok;
+}
+
+}  // namespace swe

@@ -1,0 +1,83 @@
+// Declarations shared by the kernel translation units and the C-ABI layer.
+#pragma once
+#include "swe_device.cuh"
+
+namespace swe {
+
+// FP64 state, SoA per component (h, qx, qy[, h*eta, h*w]) over the padded rows
+struct StateF64 {
+  double* h;
+  double* q1;
+  double* q2;
+  double* q3;
+  double* q4;
+};
+
+// Mixed-precision state: h in FP64 (positivity and mass), the other
+// components and a shadow copy of h in FP32 (flux arithmetic, neighbour
+// gathers).
+struct StateMix {
+  double* h;
+  float* hf;
+  float* q1;
+  float* q2;
+  float* q3;
+  float* q4;
+};
+
+// Work arrays of one stage
+struct WorkF64 {
+  double *ovh, *v1, *v2, *ent, *alpha;   // per row
+  double *dL, *muL, *fct;                // per entry
+  double *res, *rminus;                  // per row
+  StateF64 uL;                           // low-order state
+};
+
+struct WorkMix {
+  float *alpha, *res;                    // per row
+  double* rminus;                        // per row (FP64 limiter)
+  float *dL, *muL;                       // per entry
+  StateMix uL;                           // low-order state (h FP64)
+};
+
+struct StageArgs {
+  Graph G;
+  const InstConst* C;
+  InstState* St;
+  StateF64 u, u0, out;
+  WorkF64 w;
+  int rk_stage;
+  double* lij_out;
+  unsigned* err;
+  int block;
+};
+
+struct StageArgsMix {
+  Graph G;
+  const InstConst* C;
+  InstState* St;
+  StateMix u, u0, out;
+  WorkMix w;
+  int rk_stage;
+  unsigned* err;
+  int block;
+};
+
+void launch_stage_f64(const StageArgs& a, cudaStream_t s);
+void launch_dt_f64(const Graph& G, const InstConst* C, InstState* St, const StateF64& u, double* d_out,
+                   unsigned* err, int block, cudaStream_t s);
+void launch_step_begin(const InstConst* C, InstState* St, int n_inst, cudaStream_t s);
+void launch_step_end(InstState* St, int n_inst, cudaStream_t s);
+void launch_fct_positivity_f64(const Graph& G, const InstConst* C, const double* unext, const double* mat,
+                               double* rtmp, double* lij, cudaStream_t s);
+void launch_mass_f64(const Graph& G, const double* h, double* acc, cudaStream_t s);
+
+void launch_stage_mix(const StageArgsMix& a, cudaStream_t s);
+void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, unsigned* err, int block,
+                   cudaStream_t s);
+
+// kernels launched per stage / per step (for launch accounting)
+constexpr int kLaunchesPerStage = 4;
+constexpr int kLaunchesPerStepExtra = 3;   // k_dt, k_step_begin, k_step_end
+
+}  // namespace swe

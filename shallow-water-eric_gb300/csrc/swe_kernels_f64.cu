@@ -1,0 +1,602 @@
+// FP64 stage kernels in the reference's evaluation order.
+//
+// One thread owns one mesh row and walks its entries in the reference CSR
+// order, so every sum is formed in the same order as the Fortran loops.  This
+// translation unit is compiled with -fmad=false (no FMA contraction) and uses
+// IEEE sqrt/div: the result equals the FP64 CPU restatement bit for bit (the
+// Manning friction's pow() aside).  It is the parity path and the "plain FP64
+// GPU step" of the measurements.
+//
+// Per stage (SOURCES/update.f90 euler, :134-289, 'fct' + 'type2'):
+//   k_node   : one_over_h, velocity, entropy E, alpha_i       (flux, alpha_limit)
+//   k_low    : d_ij, mu_ij (alpha-limited), low-order state,   (compute_dij, compute_muij,
+//              entropy residual res_i                           smb_2_roundoff, smb_2, maxmin)
+//   k_fct    : f_ij, R^-_i                                      (compute_fct_matrix, FCT_positivity)
+//   k_update : limited antidiffusion, RK combination, Dirichlet (apply_viscosity, main.f90:77-90)
+// Per step: k_dt (COMPUTE_DT) and the time bookkeeping kernels.
+#include "swe_kernels.hpp"
+
+namespace swe {
+
+struct NodeF64 {        // per-row arrays of the FP64 path
+  double* ovh;
+  double* v1;
+  double* v2;
+  double* ent;
+  double* alpha;
+};
+
+// ---------------------------------------------------------------------------
+// k_node: flux() globals (SOURCES/condlim.f90:21-77, 79-90), the entropy
+// E_i = 0.5 (g h^2 + v.q) of entropy_residual (update.f90:844-851) and the
+// smoothness indicator alpha_i of alpha_limit (update.f90:758-781).
+// ---------------------------------------------------------------------------
+__global__ void k_node_f64(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St,
+                           StateF64 u, NodeF64 nd) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= G.n_rows) return;
+  int L = G.len[r];
+  if (L == 0) return;
+  int b = G.slice_inst[r >> 5];
+  if (St[b].done) return;
+  const InstConst& c = C[b];
+  double h = u.h[r], qx = u.q1[r], qy = u.q2[r];
+  double o = one_over_h(h, c.htiny);
+  double v1 = qx * o;
+  double v2 = (c.type_test == 13) ? qy * o * 0.0 : qy * o;
+  nd.ovh[r] = o;
+  nd.v1[r] = v1;
+  nd.v2[r] = v2;
+  double E = c.g * (h * h);
+  E = E + v1 * qx;
+  E = E + v2 * qy;
+  nd.ent[r] = 0.5 * E;
+  double alpha = 1.0;
+  if (c.alpha_limit && !(h <= c.htiny)) {
+    int64_t base = entry_base(G, r);
+    double num = 0.0, denom = 0.0;
+    for (int k = 0; k < L; k++) {
+      double hj = u.h[G.col[base + 32 * k]];
+      num = num + hj - h;
+      denom = denom + tabs(hj - h);
+    }
+    double a = (denom <= tabs(num)) ? 1.0 : tabs(num) / (denom);
+    double a2 = a * a, a4 = a2 * a2;
+    alpha = a4 * a4;
+  }
+  nd.alpha[r] = alpha;
+}
+
+// Source terms (SOURCES/update.f90:425-551) added to the undivided rk of one
+// row.  velocity is the row's own (v1, v2).
+__device__ __forceinline__ void source_f64(const InstConst& c, const InstState& st, double m, const double* ui,
+                                           double v1, double v2, double* rk, double pt_sum_x, double pt_sum_y,
+                                           double s_i) {
+  const int S = c.S;
+  if (c.type_test == 9 || c.type_test == 10) {
+    const double gamma = 4.0 / 3.0, chi = 1.0;
+    double fric = c.g * c.mannings * c.mannings;
+    double hstar = pow(tmax(ui[0], c.htiny), gamma);
+    double vel = fric * sqrt(v1 * v1 + v2 * v2);
+    double hloc = chi * vel * st.dt;
+    for (int k = 1; k < S; k++) rk[k] = rk[k] - m * ui[k] * vel * 2 / (hstar + tmax(hstar, hloc));
+  } else if (c.type_test == 11) {
+    const double kappa = 0.2;
+    for (int k = 1; k < S; k++) rk[k] = rk[k] - m * kappa * ui[k];
+  } else if (c.type_test == 12) {
+    const double f = 2.0;
+    for (int j = 3; j <= S; j++) {
+      rk[S - 2] = rk[S - 2] + m * f * ui[S - 1];
+      rk[S - 1] = rk[S - 1] - m * f * ui[S - 2];
+    }
+  } else if (c.type_test == 13) {
+    rk[1] = pt_sum_x;   // already accumulated in entry order by the caller
+    rk[2] = pt_sum_y;
+    rk[3] = rk[3] + m * ui[4];
+    rk[4] = rk[4] - m * s_i;
+  }
+}
+
+// SGN pressure pTilde_n and source s_n (mSGN_RHS, update.f90:505-529)
+__device__ __forceinline__ void sgn_node_f64(const InstConst& c, double m, double h, double heta,
+                                             double* pTilde, double* s) {
+  double lms = sqrt(m);
+  double pc = c.lambda_sgn * c.g / (3.0 * lms);
+  double x = heta / (h * h);
+  double psi = 12.0 * (x - 1.0);
+  double x3 = (x * x) * x, x4 = (x * x) * (x * x);
+  *pTilde = pc * ((h * h) * h) * (2.0 + 4.0 * x3 - 6.0 * x4);
+  double t = heta / h;
+  *s = 3.0 * pc * (t * t) * psi;
+}
+
+// ---------------------------------------------------------------------------
+// k_low: compute_dij + compute_muij + MAX + alpha_limit (update.f90:180-187,
+// 291-364, 782-798), smb_2_roundoff (:554-624) -> low-order state
+// (:202-210), smb_2 + entropy residual (:825-878).  Writes dL/muL per entry,
+// uL per row, res per row, fix_roundoff-free low-order h.
+// ---------------------------------------------------------------------------
+__global__ void k_low_f64(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St,
+                          StateF64 u, NodeF64 nd, double* __restrict__ dL, double* __restrict__ muL,
+                          StateF64 uL, double* __restrict__ res, unsigned* __restrict__ err) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= G.n_rows) return;
+  const int L = G.len[r];
+  if (L == 0) return;
+  const int b = G.slice_inst[r >> 5];
+  const InstState st = St[b];
+  if (st.done) return;
+  const InstConst& c = C[b];
+  const int S = c.S;
+  const double g = c.g, htiny = c.htiny, dt = st.dt;
+  const double sqrt2 = sqrt(2.0);
+  const int64_t base = entry_base(G, r);
+  const int dp = G.dpos[r];
+  double ui[5];
+  ui[0] = u.h[r]; ui[1] = u.q1[r]; ui[2] = u.q2[r];
+  if (S == 5) { ui[3] = u.q3[r]; ui[4] = u.q4[r]; }
+  const double ovhi = nd.ovh[r], v1i = nd.v1[r], v2i = nd.v2[r], ai = nd.alpha[r];
+  const double zi = G.bath[r], m = G.lumped[r];
+  bool delta_bad = false;
+
+  // pass 1: raw d_ij (lambda_max) and mu_ij, diagonals = -row sums
+  double sd = 0.0, sm = 0.0;
+  for (int k = 0; k < L; k++) {
+    const int64_t e = base + 32 * k;
+    const int j = G.col[e];
+    double d = 0.0, mu = 0.0;
+    if (k != dp) {
+      const double cxe = G.cx[e], cye = G.cy[e];
+      const double norm = sqrt(cxe * cxe + cye * cye);
+      const double nx = cxe / norm, ny = cye / norm;
+      double lam;
+      if (!lambda_vacc(ui[0], ui[1], ui[2], ovhi, u.h[j], u.q1[j], u.q2[j], nd.ovh[j], nx, ny, g, htiny, sqrt2,
+                       &lam))
+        delta_bad = true;
+      d = norm * lam;
+      const double sl = cxe * v1i + cye * v2i;
+      // compute_muij uses q*ovh of the raw state, equal to velocity except
+      // for type 13 whose velocity(2) is zeroed: recompute from q there
+      double sr;
+      if (c.type_test == 13) {
+        const double ulx = ui[1] * ovhi, uly = ui[2] * ovhi;
+        const double ox = nd.ovh[j];
+        const double urx = u.q1[j] * ox, ury = u.q2[j] * ox;
+        const double sl2 = cxe * ulx + cye * uly;
+        sr = cxe * urx + cye * ury;
+        mu = tmax(tmax(-sl2, 0.0), tmax(sr, 0.0));
+      } else {
+        sr = cxe * nd.v1[j] + cye * nd.v2[j];
+        mu = tmax(tmax(-sl, 0.0), tmax(sr, 0.0));
+      }
+    }
+    dL[e] = d;
+    muL[e] = mu;
+    sd = sd + d;
+    sm = sm + mu;
+  }
+  const double dii_raw = -sd, muii_raw = -sm;
+  // pass 2: dij = MAX(dij, muij) on every entry, then alpha limiting with the
+  // reference's diagonal re-summation
+  sd = 0.0; sm = 0.0;
+  for (int k = 0; k < L; k++) {
+    const int64_t e = base + 32 * k;
+    double d, mu;
+    if (k == dp) {
+      d = tmax(dii_raw, muii_raw);
+      mu = muii_raw;
+      if (c.alpha_limit) d = 0.0;
+    } else {
+      mu = muL[e];
+      d = tmax(dL[e], mu);
+      if (c.alpha_limit) {
+        const double s = tmax(ai, nd.alpha[G.col[e]]);
+        d = d * s;
+        mu = mu * s;
+      }
+    }
+    sd = sd + d;
+    sm = sm + mu;
+    dL[e] = d;
+    muL[e] = mu;
+  }
+  if (c.alpha_limit) {
+    dL[base + 32 * dp] = -sd;
+    muL[base + 32 * dp] = -sm;
+  }
+
+  // pass 3: smb_2_roundoff and smb_2 rows, maxmin of the entropy
+  double rk[5] = {0, 0, 0, 0, 0}, rk2[5] = {0, 0, 0, 0, 0};
+  double fix = 0.0;
+  double emax = nd.ent[G.col[base]], emin = emax;
+  for (int k = 0; k < L; k++) {
+    const int64_t e = base + 32 * k;
+    const int j = G.col[e];
+    double uj[5];
+    uj[0] = u.h[j]; uj[1] = u.q1[j]; uj[2] = u.q2[j];
+    if (S == 5) { uj[3] = u.q3[j]; uj[4] = u.q4[j]; }
+    const double zj = G.bath[j];
+    const double v1j = nd.v1[j], v2j = nd.v2[j];
+    const double d = dL[e], mu = muL[e];
+    const double cxe = G.cx[e], cye = G.cy[e];
+    const double ej = nd.ent[j];
+    emax = tmax(emax, ej);
+    emin = tmin(emin, ej);
+    const double zmax = tmax(zi, zj);
+    const double Hij = tmax(0.0, ui[0] + zi - zmax);
+    const double Hji = tmax(0.0, uj[0] + zj - zmax);
+    // smb_2_roundoff (htiny tests)
+    {
+      const double ratij = (ui[0] <= htiny) ? 0.0 : Hij / ui[0];
+      const double ratji = (uj[0] <= htiny) ? 0.0 : Hji / uj[0];
+      double xx = 0.0;
+      xx = xx - cxe * (v1j);
+      xx = xx - cye * (v2j);
+      if (k == dp) {
+        fix = fix + xx;
+      } else {
+        fix = fix - mu + (d - mu) * (-ratij);
+        rk[0] = rk[0] + (xx + mu) * uj[0] + tmax((d - mu) * Hji, 0.0);
+      }
+      for (int q = 1; q < S; q++) {
+        double x2 = 0.0;
+        x2 = x2 - cxe * (v1j * uj[q]);
+        x2 = x2 - cye * (v2j * uj[q]);
+        rk[q] = rk[q] + x2 + d * (uj[q] * ratji - ui[q] * ratij) + mu * (uj[q] * (1.0 - ratji) - ui[q] * (1.0 - ratij));
+      }
+      rk[1] = rk[1] - g * ui[0] * (uj[0] + zj - ui[0] - zi) * cxe;
+      rk[2] = rk[2] - g * ui[0] * (uj[0] + zj - ui[0] - zi) * cye;
+    }
+    // smb_2 (h <= 0 tests)
+    {
+      const double ratij = (ui[0] <= 0.0) ? 0.0 : Hij / ui[0];
+      const double ratji = (uj[0] <= 0.0) ? 0.0 : Hji / uj[0];
+      for (int q = 0; q < S; q++) {
+        double x2 = 0.0;
+        x2 = x2 - cxe * (v1j * uj[q]);
+        x2 = x2 - cye * (v2j * uj[q]);
+        rk2[q] = rk2[q] + x2 + d * (uj[q] * ratji - ui[q] * ratij) + mu * (uj[q] * (1.0 - ratji) - ui[q] * (1.0 - ratij));
+      }
+      rk2[1] = rk2[1] - g * ui[0] * (uj[0] + zj - ui[0] - zi) * cxe;
+      rk2[2] = rk2[2] - g * ui[0] * (uj[0] + zj - ui[0] - zi) * cye;
+    }
+  }
+  // source terms
+  if (c.type_test == 13) {
+    // mSGN_RHS adds -pTilde_j c_ij after the smb loops, entry by entry, onto
+    // the momentum rows: redo that accumulation in entry order on top of rk.
+    double s_i, p_i;
+    sgn_node_f64(c, m, ui[0], ui[3], &p_i, &s_i);
+    double ax = rk[1], ay = rk[2], bx = rk2[1], by = rk2[2];
+    for (int k = 0; k < L; k++) {
+      const int64_t e = base + 32 * k;
+      const int j = G.col[e];
+      double pj, sj;
+      sgn_node_f64(c, G.lumped[j], u.h[j], u.q3[j], &pj, &sj);
+      ax = ax - pj * G.cx[e]; ay = ay - pj * G.cy[e];
+      bx = bx - pj * G.cx[e]; by = by - pj * G.cy[e];
+    }
+    source_f64(c, st, m, ui, v1i, v2i, rk, ax, ay, s_i);
+    source_f64(c, st, m, ui, v1i, v2i, rk2, bx, by, s_i);
+  } else {
+    source_f64(c, st, m, ui, v1i, v2i, rk, 0, 0, 0);
+    source_f64(c, st, m, ui, v1i, v2i, rk2, 0, 0, 0);
+  }
+  // divide_by_lumped and the low-order state (update.f90:202-210)
+  for (int q = 0; q < S; q++) { rk[q] = rk[q] / m; rk2[q] = rk2[q] / m; }
+  double ul[5];
+  if (c.roundoff_fix) ul[0] = ui[0] * (1 + dt * fix / m) + dt * rk[0];
+  else ul[0] = tmax(ui[0] + dt * rk[0], 0.0);
+  for (int q = 1; q < S; q++) ul[q] = ui[q] + dt * rk[q];
+  uL.h[r] = ul[0]; uL.q1[r] = ul[1]; uL.q2[r] = ul[2];
+  if (S == 5) { uL.q3[r] = ul[3]; uL.q4[r] = ul[4]; }
+  // entropy residual (update.f90:838-868), rescale hoisted
+  double un_[5];
+  for (int q = 0; q < S; q++) un_[q] = ui[q] + dt * rk2[q];
+  const double on = one_over_h(un_[0], htiny);
+  const double vn1 = un_[1] * on, vn2 = un_[2] * on;
+  double En = g * (un_[0] * un_[0]);
+  En = En + vn1 * un_[1];
+  En = En + vn2 * un_[2];
+  En = 0.5 * En;
+  const double E = nd.ent[r];
+  double Ep[5] = {0, 0, 0, 0, 0};
+  Ep[0] = g * ui[0];
+  Ep[0] = Ep[0] - 0.5 * (v1i * v1i);
+  Ep[1] = v1i;
+  Ep[0] = Ep[0] - 0.5 * (v2i * v2i);
+  Ep[2] = v2i;
+  double rs = m * (En - E) / dt;
+  for (int q = 0; q < S; q++) rs = rs - m * rk2[q] * Ep[q];
+  const double rescale = tabs(emax - emin) / 2 + c.rescale_floor;
+  res[r] = tabs(rs) / rescale;
+  if (delta_bad) atomicOr(err, ERRB_DELTA);
+}
+
+// ---------------------------------------------------------------------------
+// k_fct: d^H = MIN(dL, res_ij), mu^H likewise (update.f90:232-239), f_ij
+// (compute_fct_matrix :721-748), check_hmin of the low-order state (:271) and
+// R^-_i of FCT_positivity (SOURCES/fct.f90:15-30).
+// ---------------------------------------------------------------------------
+__global__ void k_fct_f64(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St,
+                          StateF64 u, const double* __restrict__ dL, const double* __restrict__ muL,
+                          StateF64 uL, const double* __restrict__ res, double* __restrict__ fct,
+                          double* __restrict__ rminus, unsigned* __restrict__ err) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= G.n_rows) return;
+  const int L = G.len[r];
+  if (L == 0) return;
+  const int b = G.slice_inst[r >> 5];
+  const InstState st = St[b];
+  if (st.done) return;
+  const InstConst& c = C[b];
+  const int64_t base = entry_base(G, r);
+  const double hi = u.h[r], zi = G.bath[r], resi = res[r];
+  double P = -1.e-15;
+  for (int k = 0; k < L; k++) {
+    const int64_t e = base + 32 * k;
+    const int j = G.col[e];
+    const double rij = tmax(resi, res[j]);
+    const double d0 = dL[e], m0 = muL[e];
+    const double dH = tmin(d0, 1.0 * rij), mH = tmin(m0, 1.0 * rij);
+    const double hj = u.h[j], zj = G.bath[j];
+    const double zmax = tmax(zi, zj);
+    const double Hij = tmax(0.0, hi + zi - zmax);
+    const double Hji = tmax(0.0, hj + zj - zmax);
+    const double ratij = (hi <= 0.0) ? 0.0 : Hij / hi;
+    const double ratji = (hj <= 0.0) ? 0.0 : Hji / hj;
+    const double f = (dH - d0) * (hj * ratji - hi * ratij) + (mH - m0) * (hj * (1.0 - ratji) - hi * (1.0 - ratij));
+    fct[e] = f;
+    if (f < 0.0) P = P + f;
+  }
+  const double hL = uL.h[r];
+  if (hL < 0.0) atomicOr(err, ERRB_NEG_H);
+  const double scaled = (G.lumped[r] / st.dt) * hL;
+  const double Q = 0.0 - scaled;
+  double R = tmin(Q / P, 1.0);
+  if (scaled <= c.htiny) R = 0.0;
+  rminus[r] = R;
+}
+
+// ---------------------------------------------------------------------------
+// k_update: l_ij (fct.f90:31-41), (d^H-d^L) l_ij and (mu^H-mu^L) l_ij
+// (update.f90:278-279), apply_viscosity (:684-718), unext = u^L + dt rk/m
+// (:281-282), check_hmin (:285), then the SSP-RK combination and bdy of the
+// time loop (main.f90:77-90) when rk_stage > 0.
+//   rk_stage 0: out = unext                       (plain euler call)
+//   rk_stage 1: out = unext, Dirichlet
+//   rk_stage 2: out = (3 u0 + unext)/4, Dirichlet
+//   rk_stage 3: out = (u0 + 2 unext)/3, Dirichlet
+// ---------------------------------------------------------------------------
+__global__ void k_update_f64(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St,
+                             StateF64 u, const double* __restrict__ dL, const double* __restrict__ muL,
+                             StateF64 uL, const double* __restrict__ res, const double* __restrict__ fct,
+                             const double* __restrict__ rminus, StateF64 u0, StateF64 out, int rk_stage,
+                             double* __restrict__ lij_out, unsigned* __restrict__ err) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= G.n_rows) return;
+  const int L = G.len[r];
+  if (L == 0) return;
+  const int b = G.slice_inst[r >> 5];
+  const InstState st = St[b];
+  if (st.done) return;
+  const InstConst& c = C[b];
+  const int S = c.S;
+  const int64_t base = entry_base(G, r);
+  double ui[5];
+  ui[0] = u.h[r]; ui[1] = u.q1[r]; ui[2] = u.q2[r];
+  if (S == 5) { ui[3] = u.q3[r]; ui[4] = u.q4[r]; }
+  const double zi = G.bath[r], resi = res[r], Ri = rminus[r];
+  double xx[5] = {0, 0, 0, 0, 0};
+  for (int k = 0; k < L; k++) {
+    const int64_t e = base + 32 * k;
+    const int j = G.col[e];
+    const double f = fct[e];
+    const double l = (f >= 0.0) ? rminus[j] : Ri;
+    if (lij_out) lij_out[e] = l;
+    const double rij = tmax(resi, res[j]);
+    const double d0 = dL[e], m0 = muL[e];
+    const double dd = (tmin(d0, 1.0 * rij) - d0) * l;
+    const double dm = (tmin(m0, 1.0 * rij) - m0) * l;
+    double uj[5];
+    uj[0] = u.h[j]; uj[1] = u.q1[j]; uj[2] = u.q2[j];
+    if (S == 5) { uj[3] = u.q3[j]; uj[4] = u.q4[j]; }
+    const double zj = G.bath[j];
+    const double zmax = tmax(zi, zj);
+    const double Hij = tmax(0.0, ui[0] + zi - zmax);
+    const double Hji = tmax(0.0, uj[0] + zj - zmax);
+    const double ratij = (ui[0] <= 0.0) ? 0.0 : Hij / ui[0];
+    const double ratji = (uj[0] <= 0.0) ? 0.0 : Hji / uj[0];
+    for (int q = 0; q < S; q++)
+      xx[q] = xx[q] + dd * (uj[q] * ratji - ui[q] * ratij) + dm * (uj[q] * (1.0 - ratji) - ui[q] * (1.0 - ratij));
+  }
+  const double m = G.lumped[r], dt = st.dt;
+  double un[5];
+  const double* ulp[5] = {uL.h, uL.q1, uL.q2, uL.q3, uL.q4};
+  for (int q = 0; q < S; q++) un[q] = ulp[q][r] + dt * (xx[q] / m);
+  if (un[0] < 0.0) atomicOr(err, ERRB_NEG_H);
+  if (!(un[0] == un[0]) || !(un[1] == un[1]) || !(un[2] == un[2])) atomicOr(err, ERRB_NAN);
+  if (rk_stage >= 2) {
+    const double* u0p[5] = {u0.h, u0.q1, u0.q2, u0.q3, u0.q4};
+    for (int q = 0; q < S; q++)
+      un[q] = (rk_stage == 2) ? (3 * u0p[q][r] + un[q]) / 4 : (u0p[q][r] + 2 * un[q]) / 3;
+  }
+  if (rk_stage >= 1 && G.dir_mask) {
+    const unsigned msk = G.dir_mask[r];
+    for (int q = 0; q < S; q++)
+      if (msk & (1u << q)) un[q] = G.dir_val[(int64_t)q * G.n_rows + r];
+  }
+  out.h[r] = un[0]; out.q1[r] = un[1]; out.q2[r] = un[2];
+  if (S == 5) { out.q3[r] = un[3]; out.q4[r] = un[4]; }
+}
+
+// ---------------------------------------------------------------------------
+// k_dt: compute_dij (update.f90:291-326) diagonal and COMPUTE_DT's
+// max |d_ii|/m_i (main.f90:166-174), per instance.  d_out (nullable)
+// receives every d_ij.
+// ---------------------------------------------------------------------------
+__global__ void k_dt_f64(Graph G, const InstConst* __restrict__ C, InstState* __restrict__ St, StateF64 u,
+                         const double* __restrict__ ovh, double* __restrict__ d_out, unsigned* __restrict__ err) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double val = 0.0;
+  int b = -1;
+  if (r < G.n_rows && G.len[r] > 0) {
+    b = G.slice_inst[r >> 5];
+    if (!St[b].done) {
+      const InstConst& c = C[b];
+      const int L = G.len[r], dp = G.dpos[r];
+      const int64_t base = entry_base(G, r);
+      const double sqrt2 = sqrt(2.0);
+      const double hi = u.h[r], q1 = u.q1[r], q2 = u.q2[r];
+      const double ovhi = ovh ? ovh[r] : one_over_h(hi, c.htiny);
+      double s = 0.0;
+      bool bad = false;
+      for (int k = 0; k < L; k++) {
+        const int64_t e = base + 32 * k;
+        double d = 0.0;
+        if (k != dp) {
+          const int j = G.col[e];
+          const double cxe = G.cx[e], cye = G.cy[e];
+          const double norm = sqrt(cxe * cxe + cye * cye);
+          const double hj = u.h[j];
+          const double ovhj = ovh ? ovh[j] : one_over_h(hj, c.htiny);
+          double lam;
+          if (!lambda_vacc(hi, q1, q2, ovhi, hj, u.q1[j], u.q2[j], ovhj, cxe / norm, cye / norm, c.g, c.htiny, sqrt2,
+                           &lam))
+            bad = true;
+          d = norm * lam;
+        }
+        if (d_out) d_out[e] = d;
+        s = s + d;
+      }
+      if (d_out) d_out[base + 32 * dp] = -s;
+      val = tabs(-s) / G.lumped[r];
+      if (bad) atomicOr(err, ERRB_DELTA);
+    } else {
+      b = -1;
+    }
+  }
+  // warp-level max per instance: a warp covers one 32-row slice and a slice
+  // never straddles two instances
+  (void)b;
+  const unsigned full = 0xffffffffu;
+  for (int off = 16; off > 0; off >>= 1) val = fmax(val, __shfl_down_sync(full, val, off));
+  const int64_t r0 = r & ~(int64_t)31;
+  if ((threadIdx.x & 31) == 0 && r0 < G.n_rows) {
+    const int bw = G.slice_inst[r0 >> 5];
+    if (!St[bw].done && val > 0.0) atomicMax(&St[bw].maxd_bits, (unsigned long long)__double_as_longlong(val));
+  }
+}
+
+// Start of a time step: DO WHILE(time < Tfinal) and dt = CFL/max (main.f90:61, 173)
+__global__ void k_step_begin(const InstConst* __restrict__ C, InstState* __restrict__ St, int n_inst) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n_inst) return;
+  InstState& s = St[b];
+  if (s.done) return;
+  if (!(s.time < s.t_final)) { s.done = 1; return; }
+  double mx = __longlong_as_double((long long)s.maxd_bits);
+  s.dt = C[b].cfl * 1 / mx;
+  s.inv_dt = 1.0 / s.dt;
+  s.maxd_bits = 0ull;
+}
+
+// End of a time step: time = to + dt (main.f90:91)
+__global__ void k_step_end(InstState* __restrict__ St, int n_inst) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n_inst) return;
+  InstState& s = St[b];
+  if (s.done) return;
+  s.time = s.time + s.dt;
+  s.steps += 1;
+}
+
+// FCT_positivity as a stand-alone operator on one instance (fct.f90:5-42)
+__global__ void k_fct_positivity_f64(Graph G, const InstConst* __restrict__ C, const double* __restrict__ unext,
+                                     const double* __restrict__ mat, double* __restrict__ rtmp,
+                                     double* __restrict__ lij, int pass) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= G.n_rows) return;
+  const int L = G.len[r];
+  if (L == 0) return;
+  const int b = G.slice_inst[r >> 5];
+  const int64_t base = entry_base(G, r);
+  if (pass == 0) {
+    double P = -1.e-15;
+    for (int k = 0; k < L; k++) {
+      const double f = mat[base + 32 * k];
+      if (f < 0.0) P = P + f;
+    }
+    double R = tmin((0.0 - unext[r]) / P, 1.0);
+    if (unext[r] <= C[b].htiny) R = 0.0;
+    rtmp[r] = R;
+  } else {
+    for (int k = 0; k < L; k++) {
+      const int64_t e = base + 32 * k;
+      lij[e] = (mat[e] >= 0.0) ? rtmp[G.col[e]] : rtmp[r];
+    }
+  }
+}
+
+// Total mass sum m_i h_i per instance, Kahan-compensated per thread then
+// combined in double-double per warp (atomics on two words per instance).
+__global__ void k_mass_f64(Graph G, const double* __restrict__ h, double* __restrict__ acc) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double v = 0.0;
+  int b = -1;
+  if (r < G.n_rows && G.len[r] > 0) { b = G.slice_inst[r >> 5]; v = G.lumped[r] * h[r]; }
+  double cmp = 0.0;
+  for (int off = 16; off > 0; off >>= 1) {
+    double o = __shfl_down_sync(0xffffffffu, v, off);
+    double oc = __shfl_down_sync(0xffffffffu, cmp, off);
+    double s = v + o;                    // two-sum
+    double bb = s - v;
+    double err = (v - (s - bb)) + (o - bb);
+    v = s;
+    cmp = cmp + oc + err;
+  }
+  int b0 = __shfl_sync(0xffffffffu, b, 0);
+  if ((threadIdx.x & 31) == 0 && b0 >= 0) {
+    atomicAdd(&acc[2 * b0], v);
+    atomicAdd(&acc[2 * b0 + 1], cmp);
+  }
+}
+
+// ----------------------------- launchers -----------------------------------
+static inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+void launch_stage_f64(const StageArgs& a, cudaStream_t s) {
+  const int bs = a.block;
+  NodeF64 nd{a.w.ovh, a.w.v1, a.w.v2, a.w.ent, a.w.alpha};
+  k_node_f64<<<nblk(a.G.n_rows, bs), bs, 0, s>>>(a.G, a.C, a.St, a.u, nd);
+  k_low_f64<<<nblk(a.G.n_rows, bs), bs, 0, s>>>(a.G, a.C, a.St, a.u, nd, a.w.dL, a.w.muL, a.w.uL, a.w.res, a.err);
+  k_fct_f64<<<nblk(a.G.n_rows, bs), bs, 0, s>>>(a.G, a.C, a.St, a.u, a.w.dL, a.w.muL, a.w.uL, a.w.res, a.w.fct,
+                                                a.w.rminus, a.err);
+  k_update_f64<<<nblk(a.G.n_rows, bs), bs, 0, s>>>(a.G, a.C, a.St, a.u, a.w.dL, a.w.muL, a.w.uL, a.w.res, a.w.fct,
+                                                   a.w.rminus, a.u0, a.out, a.rk_stage, a.lij_out, a.err);
+}
+
+void launch_dt_f64(const Graph& G, const InstConst* C, InstState* St, const StateF64& u, double* d_out,
+                   unsigned* err, int block, cudaStream_t s) {
+  k_dt_f64<<<nblk(G.n_rows, block), block, 0, s>>>(G, C, St, u, nullptr, d_out, err);
+}
+
+void launch_step_begin(const InstConst* C, InstState* St, int n_inst, cudaStream_t s) {
+  k_step_begin<<<nblk(n_inst, 128), 128, 0, s>>>(C, St, n_inst);
+}
+
+void launch_step_end(InstState* St, int n_inst, cudaStream_t s) {
+  k_step_end<<<nblk(n_inst, 128), 128, 0, s>>>(St, n_inst);
+}
+
+void launch_fct_positivity_f64(const Graph& G, const InstConst* C, const double* unext, const double* mat,
+                               double* rtmp, double* lij, cudaStream_t s) {
+  k_fct_positivity_f64<<<nblk(G.n_rows, 128), 128, 0, s>>>(G, C, unext, mat, rtmp, lij, 0);
+  k_fct_positivity_f64<<<nblk(G.n_rows, 128), 128, 0, s>>>(G, C, unext, mat, rtmp, lij, 1);
+}
+
+void launch_mass_f64(const Graph& G, const double* h, double* acc, cudaStream_t s) {
+  k_mass_f64<<<nblk(G.n_rows, 256), 256, 0, s>>>(G, h, acc);
+}
+
+}  // namespace swe

@@ -1,0 +1,408 @@
+// Mixed FP32/FP64 stage kernels.
+//
+// Same sweep structure as the FP64 path (one thread per row, SELL-32 graph,
+// entries in reference order) but the bulk flux, lambda_max, viscosity,
+// entropy-residual and antidiffusion arithmetic runs in FP32 on FP32 data
+// (q, z, c_ij, d_ij, mu_ij, and an FP32 shadow of h).  FP64 is kept only
+// where positivity and mass need it, all per node:
+//   * the low-order depth h^L = h (1 + dt fix/m) + dt rk_1/m,
+//   * the limiter's Q^-, P^-, R^- and the h-row sum  sum_j l_ij f_ij,
+//   * the new depth h = h^L + dt/m sum_j l_ij f_ij and its RK combination.
+// FP64 throughput on GB300 is ~1/70 of FP32, so FP64 is never used per edge
+// except for the P^- and l_ij f_ij accumulations.
+#include "swe_kernels.hpp"
+
+namespace swe {
+
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ float ovh_f(float h, float htiny) {
+  float mh = fmaxf(h, htiny);
+  return fdiv(2.0f * h, h * h + mh * mh);
+}
+
+// k_node_mix: alpha_i (SOURCES/update.f90:758-781) from the FP32 depth.
+__global__ void k_node_mix(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St, StateMix u,
+                           float* __restrict__ alpha_out) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= G.n_rows) return;
+  const int L = G.len[r];
+  if (L == 0) return;
+  const int b = G.slice_inst[r >> 5];
+  if (St[b].done) return;
+  const InstConst& c = C[b];
+  const float h = u.hf[r];
+  float alpha = 1.0f;
+  if (c.alpha_limit && !(h <= (float)c.htiny)) {
+    const int64_t base = entry_base(G, r);
+    float num = 0.0f, denom = 0.0f;
+    for (int k = 0; k < L; k++) {
+      const float hj = u.hf[G.col[base + 32 * k]];
+      num += hj - h;
+      denom += fabsf(hj - h);
+    }
+    const float a = (denom <= fabsf(num)) ? 1.0f : fdiv(fabsf(num), denom);
+    const float a2 = a * a, a4 = a2 * a2;
+    alpha = a4 * a4;
+  }
+  alpha_out[r] = alpha;
+}
+
+struct NodeF {   // FP32 view of one node used by the edge loops
+  float h, q1, q2, z, ovh, v1, v2;
+};
+
+__device__ __forceinline__ NodeF load_node(const Graph& G, const StateMix& u, int64_t j, float htiny, bool sgn) {
+  NodeF n;
+  n.h = u.hf[j]; n.q1 = u.q1[j]; n.q2 = u.q2[j]; n.z = G.bathf[j];
+  n.ovh = ovh_f(n.h, htiny);
+  n.v1 = n.q1 * n.ovh;
+  n.v2 = sgn ? 0.0f : n.q2 * n.ovh;
+  return n;
+}
+
+// k_low_mix: d_ij, mu_ij, alpha limiting, low-order RHS, Galerkin RHS and
+// entropy residual of one row (SOURCES/update.f90:180-210, 291-364, 554-682,
+// 750-799, 825-878).
+__global__ void __launch_bounds__(128) k_low_mix(Graph G, const InstConst* __restrict__ C,
+                                                 const InstState* __restrict__ St, StateMix u,
+                                                 const float* __restrict__ alpha, float* __restrict__ dL,
+                                                 float* __restrict__ muL, StateMix uL, float* __restrict__ res,
+                                                 unsigned* __restrict__ err) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= G.n_rows) return;
+  const int L = G.len[r];
+  if (L == 0) return;
+  const int b = G.slice_inst[r >> 5];
+  const InstState st = St[b];
+  if (st.done) return;
+  const InstConst& c = C[b];
+  const int S = c.S;
+  const bool sgn = c.type_test == 13;
+  const float g = (float)c.g, htiny = (float)c.htiny, dtf = (float)st.dt;
+  const float sqrt2 = 1.41421356237309515f;
+  const int64_t base = entry_base(G, r);
+  const int dp = G.dpos[r];
+  const NodeF ni = load_node(G, u, r, htiny, sgn);
+  const float ai = alpha[r];
+  const float m = (float)G.lumped[r];
+  float ui3 = 0.f, ui4 = 0.f;
+  if (S == 5) { ui3 = u.q3[r]; ui4 = u.q4[r]; }
+  bool delta_bad = false;
+
+  // pass 1: d_ij = |c_ij| lambda_max, mu_ij; MAX(d, mu); alpha scaling
+  float sd = 0.f, sm_raw = 0.f, sm = 0.f;
+  for (int k = 0; k < L; k++) {
+    const int64_t e = base + 32 * k;
+    float d = 0.f, mu = 0.f;
+    if (k != dp) {
+      const int j = G.col[e];
+      const NodeF nj = load_node(G, u, j, htiny, false);
+      const float cxe = G.cxf[e], cye = G.cyf[e];
+      const float norm = sqrtf(cxe * cxe + cye * cye);
+      const float inv = fdiv(1.0f, norm);
+      float lam;
+      if (!lambda_vacc<float>(ni.h, ni.q1, ni.q2, ni.ovh, nj.h, nj.q1, nj.q2, nj.ovh, cxe * inv, cye * inv, g, htiny,
+                              sqrt2, &lam))
+        delta_bad = true;
+      d = norm * lam;
+      const float vi1 = ni.q1 * ni.ovh, vi2 = ni.q2 * ni.ovh;
+      mu = fmaxf(fmaxf(-(cxe * vi1 + cye * vi2), 0.f), fmaxf(cxe * nj.v1 + cye * nj.v2, 0.f));
+      sm_raw += mu;
+      d = fmaxf(d, mu);
+      if (c.alpha_limit) {
+        const float s = fmaxf(ai, alpha[j]);
+        d *= s;
+        mu *= s;
+      }
+    }
+    sd += d;
+    sm += mu;
+    dL[e] = d;
+    muL[e] = mu;
+  }
+  // diagonals: only used through terms that vanish; keep the reference values
+  dL[base + 32 * dp] = -sd;
+  muL[base + 32 * dp] = c.alpha_limit ? -(sm - sm_raw) : -sm_raw;
+
+  // pass 2: smb_2_roundoff (low order) and smb_2 (Galerkin) rows, maxmin(E)
+  float fix = 0.f, rk0 = 0.f, rk[5] = {0, 0, 0, 0, 0}, rk2[5] = {0, 0, 0, 0, 0};
+  const float Ei = 0.5f * (g * ni.h * ni.h + ni.v1 * ni.q1 + ni.v2 * ni.q2);
+  float emax = Ei, emin = Ei;
+  float ptx = 0.f, pty = 0.f;
+  for (int k = 0; k < L; k++) {
+    const int64_t e = base + 32 * k;
+    const int j = G.col[e];
+    const NodeF nj = (k == dp) ? ni : load_node(G, u, j, htiny, sgn);
+    float uj3 = 0.f, uj4 = 0.f;
+    if (S == 5) { uj3 = u.q3[j]; uj4 = u.q4[j]; }
+    const float d = dL[e], mu = muL[e];
+    const float cxe = G.cxf[e], cye = G.cyf[e];
+    const float Ej = 0.5f * (g * nj.h * nj.h + nj.v1 * nj.q1 + nj.v2 * nj.q2);
+    emax = fmaxf(emax, Ej);
+    emin = fminf(emin, Ej);
+    const float zmax = fmaxf(ni.z, nj.z);
+    const float Hij = fmaxf(0.f, ni.h + ni.z - zmax);
+    const float Hji = fmaxf(0.f, nj.h + nj.z - zmax);
+    const float invhi = (ni.h > 0.f) ? fdiv(1.0f, ni.h) : 0.f;
+    const float invhj = (nj.h > 0.f) ? fdiv(1.0f, nj.h) : 0.f;
+    const float rij = Hij * invhi, rji = Hji * invhj;                 // h <= 0 tests (smb_2)
+    const float rijt = (ni.h <= htiny) ? 0.f : rij;                   // h <= htiny tests
+    const float rjit = (nj.h <= htiny) ? 0.f : rji;
+    const float gal_h = -(cxe * nj.v1 + cye * nj.v2);                 // -c.v_j
+    const float topo = g * ni.h * ((nj.h + nj.z) - ni.h - ni.z);
+    if (k == dp) {
+      fix += gal_h;
+    } else {
+      fix += -mu - (d - mu) * rijt;
+      rk0 += (gal_h + mu) * nj.h + fmaxf((d - mu) * Hji, 0.f);
+    }
+    // mass row of smb_2
+    rk2[0] += gal_h * nj.h + d * (nj.h * rji - ni.h * rij) + mu * (nj.h * (1.f - rji) - ni.h * (1.f - rij));
+    float uq_i[5] = {ni.h, ni.q1, ni.q2, ui3, ui4};
+    float uq_j[5] = {nj.h, nj.q1, nj.q2, uj3, uj4};
+#pragma unroll
+    for (int q = 1; q < 5; q++) {
+      if (q >= S) break;
+      const float gal = -(cxe * nj.v1 + cye * nj.v2) * uq_j[q];
+      rk[q] += gal + d * (uq_j[q] * rjit - uq_i[q] * rijt) + mu * (uq_j[q] * (1.f - rjit) - uq_i[q] * (1.f - rijt));
+      rk2[q] += gal + d * (uq_j[q] * rji - uq_i[q] * rij) + mu * (uq_j[q] * (1.f - rji) - uq_i[q] * (1.f - rij));
+    }
+    rk[1] -= topo * cxe;  rk[2] -= topo * cye;
+    rk2[1] -= topo * cxe; rk2[2] -= topo * cye;
+    if (sgn) {
+      const float mj = (float)G.lumped[j];
+      const float pc = fdiv((float)c.lambda_sgn * g, 3.0f * sqrtf(mj));
+      const float x = fdiv(uj3, nj.h * nj.h);
+      const float pt = pc * nj.h * nj.h * nj.h * (2.f + 4.f * x * x * x - 6.f * x * x * x * x);
+      ptx -= pt * cxe;
+      pty -= pt * cye;
+    }
+  }
+  // source terms
+  if (c.type_test == 9 || c.type_test == 10) {
+    const float fric = (float)(c.g * c.mannings * c.mannings);
+    const float hstar = __powf(fmaxf(ni.h, htiny), 4.0f / 3.0f);
+    const float vel = fric * sqrtf(ni.v1 * ni.v1 + ni.v2 * ni.v2);
+    const float hloc = vel * dtf;
+    const float coef = fdiv(m * vel * 2.f, hstar + fmaxf(hstar, hloc));
+    const float uq_i[3] = {ni.h, ni.q1, ni.q2};
+    for (int q = 1; q < 3; q++) { rk[q] -= coef * uq_i[q]; rk2[q] -= coef * uq_i[q]; }
+  } else if (c.type_test == 11) {
+    rk[1] -= m * 0.2f * ni.q1; rk[2] -= m * 0.2f * ni.q2;
+    rk2[1] -= m * 0.2f * ni.q1; rk2[2] -= m * 0.2f * ni.q2;
+  } else if (c.type_test == 12) {
+    const float f = 2.0f;
+    const float a1 = m * f * ni.q2, a2 = m * f * ni.q1;
+    rk[1] += a1; rk[2] -= a2; rk2[1] += a1; rk2[2] -= a2;
+  } else if (sgn) {
+    const float pc = fdiv((float)c.lambda_sgn * g, 3.0f * sqrtf(m));
+    const float t = fdiv(ui3, ni.h);
+    const float x = fdiv(ui3, ni.h * ni.h);
+    const float s_i = 3.f * pc * t * t * 12.f * (x - 1.f);
+    rk[1] += ptx; rk[2] += pty; rk2[1] += ptx; rk2[2] += pty;
+    rk[3] += m * ui4; rk[4] -= m * s_i;
+    rk2[3] += m * ui4; rk2[4] -= m * s_i;
+  }
+  // low-order state: FP64 depth update, FP32 momenta
+  const double inv_m = G.inv_lumped[r];
+  const double dtd = st.dt;
+  double hL;
+  if (c.roundoff_fix) hL = u.h[r] * (1.0 + dtd * (double)fix * inv_m) + dtd * (double)rk0 * inv_m;
+  else hL = fmax(u.h[r] + dtd * (double)rk2[0] * inv_m, 0.0);
+  const float invm = (float)inv_m;
+  uL.h[r] = hL;
+  uL.hf[r] = (float)hL;
+  uL.q1[r] = ni.q1 + dtf * (rk[1] * invm);
+  uL.q2[r] = ni.q2 + dtf * (rk[2] * invm);
+  if (S == 5) { uL.q3[r] = ui3 + dtf * (rk[3] * invm); uL.q4[r] = ui4 + dtf * (rk[4] * invm); }
+  // entropy residual
+  float un_[3];
+  const float uq_i[3] = {ni.h, ni.q1, ni.q2};
+  for (int q = 0; q < 3; q++) un_[q] = uq_i[q] + dtf * (rk2[q] * invm);
+  const float on = ovh_f(un_[0], htiny);
+  const float En = 0.5f * (g * un_[0] * un_[0] + (un_[1] * on) * un_[1] + (un_[2] * on) * un_[2]);
+  const float Ep0 = g * ni.h - 0.5f * (ni.v1 * ni.v1) - 0.5f * (ni.v2 * ni.v2);
+  float rs = m * fdiv(En - Ei, dtf);
+  rs -= rk2[0] * Ep0 + rk2[1] * ni.v1 + rk2[2] * ni.v2;
+  const float rescale = 0.5f * fabsf(emax - emin) + (float)c.rescale_floor;
+  res[r] = fdiv(fabsf(rs), rescale);
+  if (delta_bad) atomicOr(err, ERRB_DELTA);
+}
+
+// antidiffusive h-flux f_ij of compute_fct_matrix (update.f90:744-745)
+__device__ __forceinline__ float fct_flux(float d0, float m0, float rij, float hi, float zi, float hj, float zj) {
+  const float dd = fminf(d0, rij) - d0, dm = fminf(m0, rij) - m0;
+  const float zmax = fmaxf(zi, zj);
+  const float Hij = fmaxf(0.f, hi + zi - zmax), Hji = fmaxf(0.f, hj + zj - zmax);
+  const float ratij = (hi <= 0.f) ? 0.f : fdiv(Hij, hi);
+  const float ratji = (hj <= 0.f) ? 0.f : fdiv(Hji, hj);
+  return dd * (hj * ratji - hi * ratij) + dm * (hj * (1.f - ratji) - hi * (1.f - ratij));
+}
+
+// k_fct_mix: f_ij (FP32) and R^-_i (FP64 Q^-, P^-, R^-), fct.f90:15-30
+__global__ void k_fct_mix(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St, StateMix u,
+                          const float* __restrict__ dL, const float* __restrict__ muL, StateMix uL,
+                          const float* __restrict__ res, double* __restrict__ rminus, unsigned* __restrict__ err) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= G.n_rows) return;
+  const int L = G.len[r];
+  if (L == 0) return;
+  const int b = G.slice_inst[r >> 5];
+  const InstState st = St[b];
+  if (st.done) return;
+  const InstConst& c = C[b];
+  const int64_t base = entry_base(G, r);
+  const float hi = u.hf[r], zi = G.bathf[r], resi = res[r];
+  double P = -1.e-15;
+  for (int k = 0; k < L; k++) {
+    const int64_t e = base + 32 * k;
+    const int j = G.col[e];
+    const float f = fct_flux(dL[e], muL[e], fmaxf(resi, res[j]), hi, zi, u.hf[j], G.bathf[j]);
+    if (f < 0.f) P += (double)f;
+  }
+  const double hL = uL.h[r];
+  if (hL < 0.0) atomicOr(err, ERRB_NEG_H);
+  const double scaled = G.lumped[r] * st.inv_dt * hL;
+  double R = fmin((0.0 - scaled) / P, 1.0);
+  if (scaled <= c.htiny) R = 0.0;
+  rminus[r] = R;
+}
+
+// k_update_mix: limited antidiffusion (update.f90:276-282, apply_viscosity
+// :684-718), RK combination and Dirichlet data (main.f90:77-90).
+__global__ void k_update_mix(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St,
+                             StateMix u, const float* __restrict__ dL, const float* __restrict__ muL, StateMix uL,
+                             const float* __restrict__ res, const double* __restrict__ rminus, StateMix u0,
+                             StateMix out, int rk_stage, unsigned* __restrict__ err) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= G.n_rows) return;
+  const int L = G.len[r];
+  if (L == 0) return;
+  const int b = G.slice_inst[r >> 5];
+  const InstState st = St[b];
+  if (st.done) return;
+  const InstConst& c = C[b];
+  const int S = c.S;
+  const int64_t base = entry_base(G, r);
+  const float hi = u.hf[r], zi = G.bathf[r], resi = res[r];
+  const double Ri = rminus[r];
+  float ui[5] = {hi, u.q1[r], u.q2[r], 0.f, 0.f};
+  if (S == 5) { ui[3] = u.q3[r]; ui[4] = u.q4[r]; }
+  double sh = 0.0;                       // sum_j l_ij f_ij (FP64)
+  float xx[5] = {0, 0, 0, 0, 0};
+  for (int k = 0; k < L; k++) {
+    const int64_t e = base + 32 * k;
+    const int j = G.col[e];
+    const float d0 = dL[e], m0 = muL[e];
+    const float rij = fmaxf(resi, res[j]);
+    const float hj = u.hf[j], zj = G.bathf[j];
+    const float f = fct_flux(d0, m0, rij, hi, zi, hj, zj);
+    const double l = (f >= 0.f) ? rminus[j] : Ri;
+    sh += l * (double)f;
+    const float lf = (float)l;
+    const float dd = (fminf(d0, rij) - d0) * lf, dm = (fminf(m0, rij) - m0) * lf;
+    const float zmax = fmaxf(zi, zj);
+    const float Hij = fmaxf(0.f, hi + zi - zmax), Hji = fmaxf(0.f, hj + zj - zmax);
+    const float ratij = (hi <= 0.f) ? 0.f : fdiv(Hij, hi);
+    const float ratji = (hj <= 0.f) ? 0.f : fdiv(Hji, hj);
+    float uj[5] = {hj, u.q1[j], u.q2[j], 0.f, 0.f};
+    if (S == 5) { uj[3] = u.q3[j]; uj[4] = u.q4[j]; }
+#pragma unroll
+    for (int q = 1; q < 5; q++) {
+      if (q >= S) break;
+      xx[q] += dd * (uj[q] * ratji - ui[q] * ratij) + dm * (uj[q] * (1.f - ratji) - ui[q] * (1.f - ratij));
+    }
+  }
+  const double inv_m = G.inv_lumped[r];
+  const float invm = (float)inv_m, dtf = (float)st.dt;
+  double hn = uL.h[r] + st.dt * (sh * inv_m);
+  float qn[5];
+  const float* ulq[5] = {nullptr, uL.q1, uL.q2, uL.q3, uL.q4};
+  for (int q = 1; q < S; q++) qn[q] = ulq[q][r] + dtf * (xx[q] * invm);
+  if (hn < 0.0) atomicOr(err, ERRB_NEG_H);
+  if (!(hn == hn) || !(qn[1] == qn[1]) || !(qn[2] == qn[2])) atomicOr(err, ERRB_NAN);
+  if (rk_stage >= 2) {
+    const float* u0q[5] = {nullptr, u0.q1, u0.q2, u0.q3, u0.q4};
+    if (rk_stage == 2) {
+      hn = (3.0 * u0.h[r] + hn) * 0.25;
+      for (int q = 1; q < S; q++) qn[q] = (3.f * u0q[q][r] + qn[q]) * 0.25f;
+    } else {
+      hn = (u0.h[r] + 2.0 * hn) * (1.0 / 3.0);
+      for (int q = 1; q < S; q++) qn[q] = (u0q[q][r] + 2.f * qn[q]) * (1.f / 3.f);
+    }
+  }
+  if (rk_stage >= 1 && G.dir_mask) {
+    const unsigned msk = G.dir_mask[r];
+    if (msk & 1u) hn = G.dir_val[r];
+    for (int q = 1; q < S; q++)
+      if (msk & (1u << q)) qn[q] = (float)G.dir_val[(int64_t)q * G.n_rows + r];
+  }
+  out.h[r] = hn;
+  out.hf[r] = (float)hn;
+  out.q1[r] = qn[1];
+  out.q2[r] = qn[2];
+  if (S == 5) { out.q3[r] = qn[3]; out.q4[r] = qn[4]; }
+}
+
+// k_dt_mix: FP32 lambda_max, max |d_ii|/m_i per instance (main.f90:166-174)
+__global__ void k_dt_mix(Graph G, const InstConst* __restrict__ C, InstState* __restrict__ St, StateMix u,
+                         unsigned* __restrict__ err) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  float val = 0.f;
+  if (r < G.n_rows && G.len[r] > 0) {
+    const int b = G.slice_inst[r >> 5];
+    if (!St[b].done) {
+      const InstConst& c = C[b];
+      const float g = (float)c.g, htiny = (float)c.htiny;
+      const int L = G.len[r], dp = G.dpos[r];
+      const int64_t base = entry_base(G, r);
+      const float hi = u.hf[r], q1 = u.q1[r], q2 = u.q2[r];
+      const float oi = ovh_f(hi, htiny);
+      float s = 0.f;
+      bool bad = false;
+      for (int k = 0; k < L; k++) {
+        if (k == dp) continue;
+        const int64_t e = base + 32 * k;
+        const int j = G.col[e];
+        const float cxe = G.cxf[e], cye = G.cyf[e];
+        const float norm = sqrtf(cxe * cxe + cye * cye);
+        const float inv = fdiv(1.0f, norm);
+        const float hj = u.hf[j];
+        float lam;
+        if (!lambda_vacc<float>(hi, q1, q2, oi, hj, u.q1[j], u.q2[j], ovh_f(hj, htiny), cxe * inv, cye * inv, g,
+                                htiny, 1.41421356237309515f, &lam))
+          bad = true;
+        s += norm * lam;
+      }
+      val = s * (float)G.inv_lumped[r];
+      if (bad) atomicOr(err, ERRB_DELTA);
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) val = fmaxf(val, __shfl_down_sync(0xffffffffu, val, off));
+  const int64_t r0 = r & ~(int64_t)31;
+  if ((threadIdx.x & 31) == 0 && r0 < G.n_rows) {
+    const int bw = G.slice_inst[r0 >> 5];
+    if (!St[bw].done && val > 0.f)
+      atomicMax(&St[bw].maxd_bits, (unsigned long long)__double_as_longlong((double)val));
+  }
+}
+
+static inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+void launch_stage_mix(const StageArgsMix& a, cudaStream_t s) {
+  const int bs = a.block;
+  const unsigned nb = nblk(a.G.n_rows, bs);
+  k_node_mix<<<nb, bs, 0, s>>>(a.G, a.C, a.St, a.u, a.w.alpha);
+  k_low_mix<<<nblk(a.G.n_rows, 128), 128, 0, s>>>(a.G, a.C, a.St, a.u, a.w.alpha, a.w.dL, a.w.muL, a.w.uL, a.w.res,
+                                                   a.err);
+  k_fct_mix<<<nb, bs, 0, s>>>(a.G, a.C, a.St, a.u, a.w.dL, a.w.muL, a.w.uL, a.w.res, a.w.rminus, a.err);
+  k_update_mix<<<nb, bs, 0, s>>>(a.G, a.C, a.St, a.u, a.w.dL, a.w.muL, a.w.uL, a.w.res, a.w.rminus, a.u0, a.out,
+                                 a.rk_stage, a.err);
+}
+
+void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, unsigned* err, int block,
+                   cudaStream_t s) {
+  k_dt_mix<<<nblk(G.n_rows, block), block, 0, s>>>(G, C, St, u, err);
+}
+
+}  // namespace swe

@@ -1,0 +1,55 @@
+// Host-side setup of the edge graph: the reference's construct_matrices
+// (SOURCES/update.f90:18-132) plus the GB300 layout (RCM renumbering, SELL-32
+// slices).  Compiled with -ffp-contract=off so the assembled matrices are
+// bit-identical on x86-64 and aarch64 hosts.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace swe {
+
+// One mesh in the caller's numbering, reference CSR order (0-based here).
+struct HostMesh {
+  int np = 0, me = 0;
+  std::vector<int> jj;                   // (3, me), 0-based
+  std::vector<double> rr;                // (2, np)
+  std::vector<int> ia, ja;               // CSR, sorted columns, diagonal included
+  std::vector<double> mass, cx, cy;      // per CSR entry
+  std::vector<double> lumped;            // per node
+  std::vector<int> diag;                 // CSR position of (i, i)
+};
+
+// Builds ia/ja/mass/lumped/diag/cx/cy.  Returns "" or an error message.
+std::string construct_matrices(HostMesh& m);
+
+// Reverse Cuthill-McKee ordering of the CSR graph: new_of_old[old] = new.
+std::vector<int> rcm_order(const HostMesh& m);
+
+// Global SELL-32 layout of a batch of meshes.  Row r (new numbering) of
+// instance b lives in [row_off[b], row_off[b] + np_b); each instance's row
+// range is padded to a multiple of 32 so that no slice straddles two
+// instances.  Entry k of row r sits at slice_ptr[r/32] + 32*k + r%32, and a
+// row's entries keep the reference CSR order (ascending original column).
+struct Layout {
+  int n_inst = 0;
+  int64_t n_rows = 0;                    // padded total
+  int64_t n_slices = 0;
+  int64_t n_entries = 0;                 // padded total (multiple of 32)
+  std::vector<int64_t> row_off;          // n_inst + 1
+  std::vector<int64_t> slice_ptr;        // n_slices + 1, entry offsets
+  std::vector<int> slice_inst;           // n_slices
+  std::vector<uint8_t> slice_w;          // n_slices, max row length in slice
+  std::vector<uint8_t> len;              // n_rows (0 for padding rows)
+  std::vector<uint8_t> dpos;             // n_rows, k of the diagonal entry
+  std::vector<int> col;                  // n_entries (padding -> own row)
+  std::vector<double> cx, cy;            // n_entries (padding -> 0)
+  std::vector<int64_t> ref_pos;          // n_entries: instance-local CSR position or -1
+  std::vector<double> lumped, bath;      // n_rows
+  std::vector<int64_t> old_of_new;       // n_rows: instance-local old index or -1
+  std::vector<std::vector<int>> new_of_old;   // per instance, global row index
+};
+
+Layout build_layout(const std::vector<HostMesh>& meshes, const std::vector<std::vector<double>>& baths);
+
+}  // namespace swe

@@ -1,0 +1,80 @@
+"""Build of the native library ``libswe_gpu.so`` (sm_103a) with nvcc/g++.
+
+Translation units are compiled in parallel into ``_build/`` and linked
+in-tree next to this package.  The FP64 kernels are compiled without FMA
+contraction (they reproduce the FP64 restatement bit for bit); the mixed
+kernels use fast single-precision intrinsics; host setup code is compiled
+with -ffp-contract=off so its matrices are identical on x86-64 and aarch64.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent                      # shallow-water-eric_gb300/
+CSRC = ROOT / "csrc"
+BUILD = ROOT / "_build"
+LIB = PKG / "_lib" / "libswe_gpu.so"
+INCLUDE = ROOT.parent / "include"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden,-ffp-contract=off",
+               f"-I{INCLUDE}", *ARCH]
+
+UNITS = {
+    "swe_kernels_f64.cu": ["-fmad=false"],
+    "swe_kernels_mixed.cu": ["--use_fast_math", "-Xptxas", "-warn-spills"],
+    "swe_api.cu": [],
+    "swe_setup.cpp": None,   # host C++
+}
+
+
+def _nvcc():
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if cand and (Path(cand).exists() or cand == "nvcc"):
+            return cand
+    return "nvcc"
+
+
+def _compile(src: str, extra, verbose=False):
+    s = CSRC / src
+    o = BUILD / (s.stem + ".o")
+    deps = [s] + sorted(CSRC.glob("*.hpp")) + sorted(CSRC.glob("*.cuh")) + [INCLUDE / "swe_gpu.h"]
+    if o.exists() and o.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
+        return o
+    if extra is None:
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off", f"-I{INCLUDE}",
+               "-c", str(s), "-o", str(o)]
+    else:
+        cmd = [_nvcc(), *NVCC_COMMON, *extra, "-c", str(s), "-o", str(o)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    if verbose and (r.stdout or r.stderr):
+        print(r.stdout, r.stderr)
+    return o
+
+
+def build(force: bool = False, verbose: bool = False) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    LIB.parent.mkdir(exist_ok=True)
+    if force:
+        for o in BUILD.glob("*.o"):
+            o.unlink()
+    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+        objs = list(ex.map(lambda kv: _compile(kv[0], kv[1], verbose), UNITS.items()))
+    if not LIB.exists() or any(o.stat().st_mtime > LIB.stat().st_mtime for o in objs):
+        tmp = LIB.with_name(f"libswe_gpu.{os.getpid()}.so")
+        cmd = [_nvcc(), "-shared", *ARCH, "-o", str(tmp), *map(str, objs)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose=True))

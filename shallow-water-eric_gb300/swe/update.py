@@ -1,0 +1,194 @@
+"""Host-side mirror of the reference's ``MODULE update`` / ``MODULE fct``
+interface (SOURCES/update.f90:1-16, SOURCES/fct.f90:1-5) over the C ABI.
+
+    upd = Update(mesh, bath, params)        # construct_matrices
+    dij, dt = upd.compute_dij(un)           # compute_dij + COMPUTE_DT
+    unext = upd.euler(un)                   # euler(un, unext), inputs%dt = params.dt
+    lij = upd.fct_positivity(hs, fctmat)    # FCT_positivity
+    upd.lumped, upd.diag, upd.mass          # public module data
+
+States are (syst_size, np) arrays in the reference numbering (Fortran
+``un(S, np)`` layout).  Where the reference STOPs, a ``SweError`` is raised
+with the C ABI's status code.  The device-resident fast path is
+``upload`` / ``rk3_steps`` / ``download``.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import lib as _L
+from .cases import Params
+
+
+def to_c_params(p: Params) -> _L.swe_params:
+    return _L.swe_params(*p.fields())
+
+
+class Update:
+    def __init__(self, mesh=None, bath=None, params: Params | None = None, *, batch=None):
+        """One mesh (``mesh``, ``bath``, ``params``) or a batch given as a list
+        of ``(mesh, bath, params)`` tuples."""
+        L = _L.load()
+        self._L = L
+        items = batch if batch is not None else [(mesh, bath, params)]
+        self.n_inst = len(items)
+        self.params = [p for _, _, p in items]
+        self.np_ = np.array([m["rr"].shape[1] for m, _, _ in items], np.int32)
+        me = np.array([m["jj"].shape[1] for m, _, _ in items], np.int32)
+        jj = np.concatenate([np.asfortranarray(m["jj"], np.int32).ravel(order="F") for m, _, _ in items])
+        rr = np.concatenate([np.asfortranarray(m["rr"], np.float64).ravel(order="F") for m, _, _ in items])
+        bb = np.concatenate([np.ascontiguousarray(b, np.float64) for _, b, _ in items])
+        cp = (_L.swe_params * self.n_inst)(*[to_c_params(p) for p in self.params])
+        self.S = self.params[0].syst_size
+        h = ctypes.c_void_p()
+        rc = L.swe_create_batch(ctypes.byref(h), self.n_inst, _L.ip(self.np_), _L.ip(me), _L.ip(jj), _L.dp(rr),
+                                _L.dp(bb), cp)
+        self.h = h
+        if rc:
+            msg = L.swe_last_error(h).decode() if h else ""
+            if h:
+                L.swe_destroy(h)
+                self.h = None
+            raise _L.SweError(rc, msg)
+        self.node_off = np.concatenate([[0], np.cumsum(self.np_)]).astype(np.int64)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.swe_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc):
+        if rc:
+            raise _L.SweError(rc, self._L.swe_last_error(self.h).decode())
+
+    # ---- module data -------------------------------------------------------
+    def sizes(self, inst=0):
+        n = ctypes.c_int(); z = ctypes.c_int()
+        self._check(self._L.swe_sizes(self.h, inst, ctypes.byref(n), ctypes.byref(z)))
+        return n.value, z.value
+
+    def matrices(self, inst=0):
+        n, z = self.sizes(inst)
+        ia = np.zeros(n + 1, np.int32); ja = np.zeros(z, np.int32)
+        mass = np.zeros(z); lumped = np.zeros(n); diag = np.zeros(n, np.int32)
+        cx = np.zeros(z); cy = np.zeros(z)
+        self._check(self._L.swe_get_matrices(self.h, inst, _L.ip(ia), _L.ip(ja), _L.dp(mass), _L.dp(lumped),
+                                             _L.ip(diag), _L.dp(cx), _L.dp(cy)))
+        return dict(ia=ia, ja=ja, mass=mass, lumped=lumped, diag=diag, cx=cx, cy=cy)
+
+    @property
+    def lumped(self):
+        return self.matrices()["lumped"]
+
+    @property
+    def diag(self):
+        return self.matrices()["diag"]
+
+    @property
+    def mass(self):
+        return self.matrices()["mass"]
+
+    # ---- parameters / boundary data ---------------------------------------
+    def set_params(self, p: Params, inst=0):
+        self.params[inst] = p
+        cp = to_c_params(p)
+        self._check(self._L.swe_set_params(self.h, inst, ctypes.byref(cp)))
+
+    def set_dirichlet(self, comp, js, vals=None, inst=0):
+        js = np.ascontiguousarray(js, np.int32)
+        v = None if vals is None else np.ascontiguousarray(vals, np.float64)
+        self._check(self._L.swe_set_dirichlet(self.h, inst, comp, len(js), _L.ip(js), _L.dp(v)))
+
+    # ---- per-call operators (reference-shaped) ----------------------------
+    def compute_dij(self, un, inst=0):
+        u = np.asfortranarray(un, np.float64)
+        n, z = self.sizes(inst)
+        dij = np.zeros(z); dt = ctypes.c_double()
+        self._check(self._L.swe_compute_dij(self.h, inst, _L.dp(u), _L.dp(dij), ctypes.byref(dt)))
+        return dij, dt.value
+
+    def euler(self, un, inst=0):
+        u = np.asfortranarray(un, np.float64)
+        out = np.zeros_like(u, order="F")
+        self._check(self._L.swe_euler(self.h, inst, _L.dp(u), _L.dp(out)))
+        return out
+
+    def euler_intermediates(self, inst=0):
+        n, z = self.sizes(inst)
+        a = dict(dij_low=np.zeros(z), muij_low=np.zeros(z), alpha=np.zeros(n),
+                 u_low=np.zeros((self.S, n), order="F"), res=np.zeros(n), fctmat=np.zeros(z),
+                 rminus=np.zeros(n), lij=np.zeros(z))
+        self._check(self._L.swe_euler_intermediates(self.h, inst, *[_L.dp(a[k]) for k in
+                                                                  ("dij_low", "muij_low", "alpha", "u_low", "res",
+                                                                   "fctmat", "rminus", "lij")]))
+        return a
+
+    def fct_positivity(self, unext_scaled, fctmat, inst=0):
+        u = np.ascontiguousarray(unext_scaled, np.float64)
+        f = np.ascontiguousarray(fctmat, np.float64)
+        lij = np.zeros(len(f))
+        self._check(self._L.swe_fct_positivity(self.h, inst, _L.dp(u), _L.dp(f), _L.dp(lij)))
+        return lij
+
+    # ---- device-resident time loop ----------------------------------------
+    def upload(self, un):
+        """un: (S, sum np) concatenation of the instances' states, or a list."""
+        if isinstance(un, (list, tuple)):
+            un = np.hstack([np.asarray(x) for x in un])
+        u = np.asfortranarray(un, np.float64)
+        self._check(self._L.swe_upload(self.h, _L.dp(u)))
+
+    def download(self):
+        out = np.zeros((self.S, int(self.node_off[-1])), order="F")
+        self._check(self._L.swe_download(self.h, _L.dp(out)))
+        return out
+
+    def download_split(self):
+        u = self.download()
+        return [u[:, self.node_off[b]:self.node_off[b + 1]] for b in range(self.n_inst)]
+
+    def upload_device(self, ptr: int):
+        self._check(self._L.swe_upload_device(self.h, ctypes.c_void_p(ptr)))
+
+    def download_device(self, ptr: int):
+        self._check(self._L.swe_download_device(self.h, ctypes.c_void_p(ptr)))
+
+    def set_time(self, time=0.0, t_final=1e300):
+        t = np.broadcast_to(np.asarray(time, np.float64), (self.n_inst,)).copy()
+        tf = np.broadcast_to(np.asarray(t_final, np.float64), (self.n_inst,)).copy()
+        self._check(self._L.swe_set_time(self.h, _L.dp(t), _L.dp(tf)))
+
+    def rk3_steps(self, nsteps):
+        t = np.zeros(self.n_inst); dt = np.zeros(self.n_inst); n = ctypes.c_int()
+        self._check(self._L.swe_rk3_steps(self.h, nsteps, _L.dp(t), _L.dp(dt), ctypes.byref(n)))
+        return t, dt, n.value
+
+    def total_mass(self):
+        m = np.zeros(self.n_inst)
+        self._check(self._L.swe_mass(self.h, _L.dp(m)))
+        return m
+
+    @property
+    def last_launch_count(self):
+        return int(self._L.swe_last_launch_count(self.h))
+
+    @property
+    def tuning(self):
+        return self._L.swe_tuning(self.h).decode()
+
+
+def from_case(case, precision=None):
+    """Build an Update for a cases.Case (bath, params and Dirichlet data)."""
+    p = case.params
+    if precision is not None:
+        from dataclasses import replace
+        p = replace(p, precision=precision)
+    upd = Update(case.mesh, case.bath, p)
+    for comp, js, vals in case.dirichlet:
+        upd.set_dirichlet(comp, js, vals)
+    return upd

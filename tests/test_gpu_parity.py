@@ -1,0 +1,205 @@
+"""CUDA path (through the C ABI) against the FP64 oracle and the committed
+golden vectors.
+
+FP64 path: bit-exact.  The FP64 kernels keep the reference's evaluation order
+and are built without FMA contraction, so setup matrices, d_ij, every stage
+intermediate and whole RK3 trajectories must equal the oracle exactly
+(Manning friction uses pow() and is held to 1e-12 relative instead).
+
+Mixed path: relative L1 difference of h against the FP64 oracle <= 1e-5
+(the target tolerance), h >= 0.
+"""
+import math
+from dataclasses import replace
+
+import numpy as np
+import pytest
+
+import oracle
+from swe import cases as C, mesh as M
+from swe import lib as L
+from swe.update import Update, from_case
+
+pytestmark = pytest.mark.gpu
+
+MIXED_L1_TOL = 1e-5
+
+
+def _oracle_for(case):
+    o = oracle.Oracle(case.mesh["jj"], case.mesh["rr"])
+    o.set_params(oracle.Params(*case.params.fields()))
+    o.set_bath(case.bath)
+    for comp, js, vals in case.dirichlet:
+        o.set_dirichlet(comp, js, vals)
+    return o
+
+
+def _thacker(golden, h="0.2", **kw):
+    d = np.load(golden / f"mesh_cav_{h}.npz")
+    return C.thacker_case({k: d[k] for k in d.files}, **kw)
+
+
+def _rel_l1(a, b, w):
+    return float(np.sum(w * np.abs(a - b)) / np.sum(w * np.abs(b)))
+
+
+def test_setup_matrices_bit_exact(golden):
+    case = _thacker(golden, "0.1", periods=1.0, cfl=0.3)
+    upd = from_case(case)
+    o = _oracle_for(case)
+    a, b = upd.matrices(), o.matrices()
+    for k in ("ia", "ja", "diag", "mass", "lumped", "cx", "cy"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+
+
+@pytest.mark.parametrize("h", ["0.2", "0.05"])
+def test_compute_dij_bit_exact(golden, h):
+    case = _thacker(golden, h, periods=1.0, cfl=0.3)
+    upd = from_case(case)
+    o = _oracle_for(case)
+    d_gpu, dt_gpu = upd.compute_dij(case.u0)
+    d_orc, dt_orc = o.compute_dij(case.u0)
+    np.testing.assert_array_equal(d_gpu, d_orc)
+    assert dt_gpu == dt_orc
+
+
+def test_euler_stage_and_intermediates_bit_exact(golden):
+    case = _thacker(golden, "0.2", periods=1.0, cfl=0.3)
+    o = _oracle_for(case)
+    u = case.u0.copy(order="F")
+    t = 0.0
+    for _ in range(15):                     # a state with wet/dry fronts moving
+        t = o.rk3_step(u, t)
+    _, dt = o.compute_dij(u)
+    p = replace(case.params, dt=dt)
+    o.set_params(oracle.Params(*p.fields()))
+    upd = from_case(case)
+    upd.set_params(p)
+    out_o, dump = o.euler(u, dump=True)
+    out_g = upd.euler(u)
+    inter = upd.euler_intermediates()
+    np.testing.assert_array_equal(out_g, out_o)
+    for k in ("dij_low", "muij_low", "alpha", "u_low", "res", "fctmat", "rminus", "lij"):
+        np.testing.assert_array_equal(inter[k], dump[k], err_msg=k)
+
+
+def test_fct_positivity_operator_bit_exact():
+    rng = np.random.default_rng(7)
+    mesh = M.jittered_mesh(15, 15, 0, 1, 0, 1, seed=7)
+    case = C.Case("x", mesh, C.Params(htiny=1e-3, dt=1e-3), np.zeros(225), np.zeros((3, 225), order="F"), 1.0)
+    upd = from_case(case)
+    o = _oracle_for(case)
+    nnz = upd.sizes()[1]
+    hs = rng.random(225) * 2e-3        # straddles the htiny test
+    f = rng.normal(size=nnz)
+    np.testing.assert_array_equal(upd.fct_positivity(hs, f), o.fct_positivity(hs, f))
+
+
+def test_rk3_trajectory_matches_golden(golden):
+    """Device-resident graph-captured RK3 loop vs the committed oracle
+    trajectory (bit-exact)."""
+    g = np.load(golden / "oracle_thacker_cav02.npz")
+    case = _thacker(golden, "0.2", periods=1.0, cfl=0.3)
+    upd = from_case(case)
+    upd.upload(case.u0)
+    upd.set_time(0.0, case.tfinal)
+    t_all = 0.0
+    for k in range(1, len(g["states"])):
+        t, dt, n = upd.rk3_steps(int(g["steps_per_state"]))
+        assert n == int(g["steps_per_state"])
+        np.testing.assert_array_equal(upd.download(), g["states"][k])
+        assert t[0] == g["times"][k]
+    assert upd.last_launch_count > 0
+
+
+def test_rk3_run_to_tfinal_matches_oracle(golden):
+    """DO WHILE(time < Tfinal) with unclipped dt: same step count, same state."""
+    g = np.load(golden / "oracle_dam21.npz")
+    case = C.dam_break_case(n=21, tfinal=0.05)
+    upd = from_case(case)
+    upd.upload(case.u0)
+    upd.set_time(0.0, case.tfinal)
+    t, dt, n = upd.rk3_steps(int(g["nsteps"]) + 7)     # extra steps are no-ops
+    assert n == int(g["nsteps"]) and t[0] == float(g["time"])
+    np.testing.assert_array_equal(upd.download(), g["u"])
+
+
+def test_manning_friction_fp64():
+    case = C.bump_basin_case(n=30, nsteps=20)
+    o = _oracle_for(case)
+    u = case.u0.copy(order="F")
+    t = 0.0
+    for _ in range(20):
+        t = o.rk3_step(u, t)
+    upd = from_case(case)
+    upd.upload(case.u0)
+    upd.set_time(0.0, 1e30)
+    upd.rk3_steps(20)
+    ug = upd.download()
+    scale = np.abs(u).max(axis=1, keepdims=True)
+    assert np.max(np.abs(ug - u) / scale) < 1e-12
+
+
+def test_batch_equals_single_instances():
+    cases = C.batch_instances(n_inst=3, nmin=200, nmax=2000, seed=11)
+    items = [(c.mesh, c.bath, c.params) for c in cases]
+    upd = Update(batch=items)
+    for b, c in enumerate(cases):
+        for comp, js, vals in c.dirichlet:
+            upd.set_dirichlet(comp, js, vals, inst=b)
+    upd.upload([c.u0 for c in cases])
+    upd.set_time(0.0, 1e30)
+    upd.rk3_steps(12)
+    got = upd.download_split()
+    for b, c in enumerate(cases):
+        o = _oracle_for(c)
+        u = c.u0.copy(order="F")
+        t = 0.0
+        for _ in range(12):
+            t = o.rk3_step(u, t)
+        scale = np.abs(u).max(axis=1, keepdims=True) + 1e-300
+        assert np.max(np.abs(got[b] - u) / scale) < 1e-12, b
+
+
+def test_negative_depth_is_reported_not_trapped():
+    case = C.dam_break_case(n=11)
+    upd = from_case(case)
+    u = case.u0.copy(order="F")
+    u[0, 5] = -0.5
+    upd.set_params(replace(case.params, dt=1e-6))
+    with pytest.raises(L.SweError) as ei:
+        upd.euler(u)
+    assert ei.value.code == L.SWE_ERR_NEG_H
+    # the context stays usable
+    u[0, 5] = 1.0
+    upd.euler(u)
+
+
+@pytest.mark.parametrize("which", ["dam", "thacker"])
+def test_mixed_precision_within_tolerance(golden, which):
+    if which == "dam":
+        case = C.dam_break_case(n=41, tfinal=0.05)
+    else:
+        case = _thacker(golden, "0.1", periods=0.25, cfl=0.3)
+    o = _oracle_for(case)
+    u = case.u0.copy(order="F")
+    t, n = o.run(u, 0.0, case.tfinal)
+    upd = from_case(case, precision=1)
+    upd.upload(case.u0)
+    upd.set_time(0.0, case.tfinal)
+    tg, _, ng = upd.rk3_steps(n + 50)
+    ug = upd.download()
+    lump = upd.lumped
+    err = _rel_l1(ug[0], u[0], lump)
+    assert ug[0].min() >= 0.0
+    assert abs(ng - n) <= 1
+    assert err <= MIXED_L1_TOL, err
+
+
+def test_mass_monitor():
+    case = C.dam_break_case(n=21)
+    upd = from_case(case)
+    upd.upload(case.u0)
+    m = upd.total_mass()[0]
+    lump = upd.lumped
+    assert m == pytest.approx(float(np.sum(lump * case.u0[0])), rel=1e-15)
