@@ -93,6 +93,12 @@ const char* swe_last_error(const swe_ctx* ctx);
  * used by swe_euler. */
 int swe_set_params(swe_ctx* ctx, int inst, const swe_params* params);
 
+/* Replace the bathymetry of instance `inst` (np values, caller numbering).
+ * The reference's driver builds the matrices (construct_matrices,
+ * SOURCES/main.f90:21) before init() sets bath (:31), so a Fortran shim
+ * creates the context with a zero bathymetry and sets it here. */
+int swe_set_bath(swe_ctx* ctx, int inst, const double* bath);
+
 /* Constant Dirichlet data applied after every RK stage by swe_rk3_steps,
  * like bdy (SOURCES/main.f90:176-188) with values that do not depend on t:
  * comp is the 0-based component, js 1-based node numbers of instance
@@ -153,6 +159,16 @@ int swe_mass(swe_ctx* ctx, double* mass_out);
 
 /* Kernel launches issued by the last swe_rk3_steps call (for accounting). */
 long long swe_last_launch_count(const swe_ctx* ctx);
+
+/* Device time (ms, CUDA events on the context's stream) of the kernels of the
+ * last swe_rk3_steps call. */
+double swe_last_device_ms(const swe_ctx* ctx);
+
+/* Runs nsteps time steps kernel by kernel with a CUDA event pair around every
+ * launch and returns the average duration (ms) per launch of each kernel
+ * kind in ms_out[SWE_NKERNELS] (order: dt, node, low, fct, update). */
+enum { SWE_NKERNELS = 5 };
+int swe_profile_kernels(swe_ctx* ctx, int nsteps, double* ms_out);
 
 /* Name of the kernel configuration chosen by the autotuner. */
 const char* swe_tuning(const swe_ctx* ctx);

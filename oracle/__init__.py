@@ -26,8 +26,10 @@ LIB = BUILD / "libswe_oracle.so"
 SRC = HERE / "swe_oracle.cpp"
 
 # No FMA contraction and no fast-math: the restatement's evaluation order is
-# its contract (identical results on x86-64 and aarch64 hosts).
-CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math"]
+# its contract (identical results on x86-64 and aarch64 hosts).  Row loops are
+# OpenMP-parallel; every row is still summed by one thread in CSR order, so
+# results do not depend on the thread count.
+CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-fopenmp"]
 
 
 def build(force: bool = False) -> Path:

@@ -211,10 +211,12 @@ inline double ovh_of(double h, double htiny) {
 void flux(Oracle& o, const double* un, std::vector<double>& vv) {
   const int S = o.P.syst_size;
   vv.assign((size_t)o.np * S * 2, 0.0);
+#pragma omp parallel for schedule(static)
   for (int n = 0; n < o.np; n++) {
     const double* u = un + (size_t)n * S;
     o.one_over_h[n] = ovh_of(u[0], o.P.htiny);
   }
+#pragma omp parallel for schedule(static)
   for (int n = 0; n < o.np; n++) {
     const double* u = un + (size_t)n * S;
     double* ve = &o.velocity[(size_t)n * 4];
@@ -294,6 +296,8 @@ int lambda_vacc(const double* ul, const double* ur, const double n[2], double g,
 // compute_dij: SOURCES/update.f90:291-326
 int compute_dij(Oracle& o, const double* un) {
   const int S = o.P.syst_size;
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
   for (int i = 0; i < o.np; i++) {
     for (int p = o.ia[i]; p < o.ia[i + 1]; p++) {
       int j = o.ja[p];
@@ -302,17 +306,19 @@ int compute_dij(Oracle& o, const double* un) {
         double norm_cij = std::sqrt(nij[0] * nij[0] + nij[1] * nij[1]);
         nij[0] = nij[0] / norm_cij;
         nij[1] = nij[1] / norm_cij;
-        double lambda;
-        if (lambda_vacc(un + (size_t)i * S, un + (size_t)j * S, nij, o.P.gravity, o.P.htiny, &lambda)) {
-          o.err = ORC_ERR_DELTA;
-          return ORC_ERR_DELTA;
-        }
+        double lambda = 0.0;
+        if (lambda_vacc(un + (size_t)i * S, un + (size_t)j * S, nij, o.P.gravity, o.P.htiny, &lambda)) bad = 1;
         o.dij[p] = norm_cij * lambda;
       } else {
         o.dij[p] = 0.0;
       }
     }
   }
+  if (bad) {
+    o.err = ORC_ERR_DELTA;
+    return ORC_ERR_DELTA;
+  }
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < o.np; i++) {
     double s = 0.0;
     for (int p = o.ia[i]; p < o.ia[i + 1]; p++) s = s + o.dij[p];
@@ -325,6 +331,7 @@ int compute_dij(Oracle& o, const double* un) {
 void compute_muij(Oracle& o, const double* un) {
   const int S = o.P.syst_size;
   const double ht = o.P.htiny;
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < o.np; i++) {
     for (int p = o.ia[i]; p < o.ia[i + 1]; p++) {
       int j = o.ja[p];
@@ -343,6 +350,7 @@ void compute_muij(Oracle& o, const double* un) {
       }
     }
   }
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < o.np; i++) {
     double s = 0.0;
     for (int p = o.ia[i]; p < o.ia[i + 1]; p++) s = s + o.muij[p];
@@ -355,6 +363,7 @@ void compute_muij(Oracle& o, const double* un) {
 void alpha_limit(Oracle& o, const double* un, std::vector<double>* alpha_out) {
   const int S = o.P.syst_size;
   std::vector<double> alpha(o.np);
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < o.np; i++) {
     double hi = un[(size_t)i * S];
     if (hi <= o.P.htiny) { alpha[i] = 1.0; continue; }
@@ -370,6 +379,7 @@ void alpha_limit(Oracle& o, const double* un, std::vector<double>* alpha_out) {
     double a2 = a * a, a4 = a2 * a2;   // alpha**8 (integer power by squaring)
     alpha[i] = a4 * a4;
   }
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < o.np; i++)
     for (int p = o.ia[i]; p < o.ia[i + 1]; p++) {
       int j = o.ja[p];
@@ -381,6 +391,7 @@ void alpha_limit(Oracle& o, const double* un, std::vector<double>* alpha_out) {
         o.dij[p] = 0.0;
       }
     }
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < o.np; i++) {
     double s = 0.0;
     for (int p = o.ia[i]; p < o.ia[i + 1]; p++) s = s + o.dij[p];
@@ -453,6 +464,7 @@ void smb_2_roundoff(Oracle& o, const double* un, std::vector<double>& rk) {
   rk.assign((size_t)o.np * S, 0.0);
   std::fill(o.fix_roundoff.begin(), o.fix_roundoff.end(), 0.0);
   const double ht = o.P.htiny, g = o.P.gravity;
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < o.np; i++) {
     const double* ui = un + (size_t)i * S;
     double* r = &rk[(size_t)i * S];
@@ -495,6 +507,7 @@ void smb_2(Oracle& o, const double* un, std::vector<double>& rk) {
   rk.assign((size_t)o.np * S, 0.0);
   std::fill(o.fix_roundoff.begin(), o.fix_roundoff.end(), 0.0);
   const double g = o.P.gravity;
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < o.np; i++) {
     const double* ui = un + (size_t)i * S;
     double* r = &rk[(size_t)i * S];
@@ -528,6 +541,7 @@ void smb_1(Oracle& o, const double* un, std::vector<double>& rk) {
   flux(o, un, vv);
   rk.assign((size_t)o.np * S, 0.0);
   const double ht = o.P.htiny, g = o.P.gravity;
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < o.np; i++) {
     const double* ui = un + (size_t)i * S;
     double* r = &rk[(size_t)i * S];
@@ -577,6 +591,7 @@ void entropy_residual(Oracle& o, const double* un, std::vector<double>* res_out)
   std::vector<double> unext((size_t)o.np * S);
   for (size_t q = 0; q < unext.size(); q++) unext[q] = un[q] + dt * rk[q];
   std::vector<double> Ent(o.np), res(o.np), maxn(o.np), minn(o.np);
+#pragma omp parallel for schedule(static)
   for (int n = 0; n < o.np; n++) {
     const double* u = un + (size_t)n * S;
     const double* w = &unext[(size_t)n * S];
@@ -595,6 +610,7 @@ void entropy_residual(Oracle& o, const double* un, std::vector<double>* res_out)
     Ent[n] = E;
     res[n] = r;
   }
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < o.np; i++) {
     double mx = Ent[o.ja[o.ia[i]]], mn = mx;
     for (int p = o.ia[i] + 1; p < o.ia[i + 1]; p++) { mx = std::max(mx, Ent[o.ja[p]]); mn = std::min(mn, Ent[o.ja[p]]); }
@@ -613,6 +629,7 @@ void entropy_residual(Oracle& o, const double* un, std::vector<double>* res_out)
 // compute_fct_matrix: SOURCES/update.f90:721-748
 void compute_fct_matrix(Oracle& o, const double* un) {
   const int S = o.P.syst_size;
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < o.np; i++)
     for (int p = o.ia[i]; p < o.ia[i + 1]; p++) {
       int j = o.ja[p];
@@ -631,6 +648,7 @@ void compute_fct_matrix(Oracle& o, const double* un) {
 void fct_positivity(const Oracle& o, const double* unext, const double* fmat, double* lij, double* Rm_out) {
   const double smallminus = -1.e-15;
   std::vector<double> Rminus(o.np);
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < o.np; i++) {
     double Q = 0.0 - unext[i];
     double P = smallminus;
@@ -638,6 +656,7 @@ void fct_positivity(const Oracle& o, const double* unext, const double* fmat, do
     Rminus[i] = fmin_(Q / P, 1.0);
     if (unext[i] <= o.P.htiny) Rminus[i] = 0.0;
   }
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < o.np; i++)
     for (int p = o.ia[i]; p < o.ia[i + 1]; p++)
       lij[p] = (fmat[p] >= 0.0) ? Rminus[o.ja[p]] : Rminus[i];
@@ -648,6 +667,7 @@ void fct_positivity(const Oracle& o, const double* unext, const double* fmat, do
 void apply_viscosity(Oracle& o, const double* un, std::vector<double>& rk) {
   const int S = o.P.syst_size;
   rk.assign((size_t)o.np * S, 0.0);
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < o.np; i++) {
     double xx[5] = {0, 0, 0, 0, 0};
     const double* ui = un + (size_t)i * S;

@@ -66,6 +66,8 @@ struct swe_ctx {
   int graph_steps = 0;
   int block = 128;
   long long last_launches = 0;
+  double last_ms = 0.0;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
   bool euler_done = false;
   int euler_inst = -1;
   std::string err;
@@ -229,13 +231,14 @@ __global__ void k_gather_out(double* __restrict__ stage, const int* __restrict__
   for (int k = 0; k < S; k++) stage[n * S + k] = comp[k][r];
 }
 __global__ void k_scatter_in_mix(const double* __restrict__ stage, const int* __restrict__ row_of_node,
-                                 int64_t n_nodes, int S, StateMix a) {
+                                 int64_t n_nodes, int S, StateMix a, const int* __restrict__ slice_inst,
+                                 const InstConst* __restrict__ C) {
   int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (n >= n_nodes) return;
   const int64_t r = row_of_node[n];
   const double h = stage[n * S];
   a.h[r] = h;
-  a.hf[r] = (float)h;
+  a.hf[r] = shadow_depth(h, C[slice_inst[r >> 5]].htiny);
   a.q1[r] = (float)stage[n * S + 1];
   a.q2[r] = (float)stage[n * S + 2];
   if (S == 5) { a.q3[r] = (float)stage[n * S + 3]; a.q4[r] = (float)stage[n * S + 4]; }
@@ -263,7 +266,8 @@ static int to_device(swe_ctx* c, const double* un, bool device_src, int64_t node
                                              nn, c->S, c->A);
   else
     k_scatter_in_mix<<<nb, 256, 0, c->stream>>>(c->d_stage + (size_t)c->S * node_begin,
-                                                 c->d_row_of_node + node_begin, nn, c->S, c->mA);
+                                                 c->d_row_of_node + node_begin, nn, c->S, c->mA, c->G.slice_inst,
+                                                 c->d_C);
   CK(cudaGetLastError());
   return SWE_OK;
 }
@@ -318,26 +322,38 @@ static int save_state(swe_ctx* c, std::vector<InstState>& saved) {
   return SWE_OK;
 }
 
-static void enqueue_step(swe_ctx* c) {
+// One time step.  With kev/acc (profiling), every kernel is bracketed by an
+// event pair and its duration added to acc[kind] after a synchronisation.
+static void enqueue_step(swe_ctx* c, const KernelEvents* kev = nullptr, double* acc = nullptr) {
   const cudaStream_t s = c->stream;
-  if (c->precision == SWE_PREC_FP64) {
-    launch_dt_f64(c->G, c->d_C, c->d_St, c->A, nullptr, c->d_err, c->block, s);
-    launch_step_begin(c->d_C, c->d_St, c->n_inst, s);
-    StageArgs a{c->G, c->d_C, c->d_St, c->A, c->A, c->B, c->w, 1, nullptr, c->d_err, c->block};
-    launch_stage_f64(a, s);
-    a.u = c->B; a.out = c->Cs; a.rk_stage = 2;
-    launch_stage_f64(a, s);
-    a.u = c->Cs; a.out = c->A; a.rk_stage = 3;
-    launch_stage_f64(a, s);
-  } else {
-    launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->d_err, c->block, s);
-    launch_step_begin(c->d_C, c->d_St, c->n_inst, s);
-    StageArgsMix a{c->G, c->d_C, c->d_St, c->mA, c->mA, c->mB, c->wm, 1, c->d_err, c->block};
-    launch_stage_mix(a, s);
-    a.u = c->mB; a.out = c->mC; a.rk_stage = 2;
-    launch_stage_mix(a, s);
-    a.u = c->mC; a.out = c->mA; a.rk_stage = 3;
-    launch_stage_mix(a, s);
+  auto harvest = [&](int first, int last) {
+    if (!kev) return;
+    cudaEventSynchronize(kev->ev[2 * last + 1]);
+    for (int k = first; k <= last; k++) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, kev->ev[2 * k], kev->ev[2 * k + 1]);
+      acc[k] += ms;
+    }
+  };
+  if (kev) cudaEventRecord(kev->ev[0], s);
+  if (c->precision == SWE_PREC_FP64) launch_dt_f64(c->G, c->d_C, c->d_St, c->A, nullptr, c->d_err, c->block, s);
+  else launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->d_err, c->block, s);
+  if (kev) cudaEventRecord(kev->ev[1], s);
+  harvest(0, 0);
+  launch_step_begin(c->d_C, c->d_St, c->n_inst, s);
+  for (int stage = 1; stage <= 3; stage++) {
+    if (c->precision == SWE_PREC_FP64) {
+      StageArgs a{c->G, c->d_C, c->d_St, c->A, c->A, c->B, c->w, stage, nullptr, c->d_err, c->block};
+      if (stage == 2) { a.u = c->B; a.out = c->Cs; }
+      if (stage == 3) { a.u = c->Cs; a.out = c->A; }
+      launch_stage_f64(a, s, kev);
+    } else {
+      StageArgsMix a{c->G, c->d_C, c->d_St, c->mA, c->mA, c->mB, c->wm, stage, c->d_err, c->block};
+      if (stage == 2) { a.u = c->mB; a.out = c->mC; }
+      if (stage == 3) { a.u = c->mC; a.out = c->mA; }
+      launch_stage_mix(a, s, kev);
+    }
+    harvest(1, 4);
   }
   launch_step_end(c->d_St, c->n_inst, s);
 }
@@ -418,6 +434,8 @@ SWE_API void swe_destroy(swe_ctx* c) {
   if (!c) return;
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->t0) cudaEventDestroy(c->t0);
+  if (c->t1) cudaEventDestroy(c->t1);
   c->buf.release();
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -439,6 +457,25 @@ SWE_API int swe_set_params(swe_ctx* c, int inst, const swe_params* p) {
   hs[inst].dt = p->dt;
   hs[inst].inv_dt = p->dt > 0 ? 1.0 / p->dt : 0.0;
   return restore_done(c, hs);
+}
+
+SWE_API int swe_set_bath(swe_ctx* c, int inst, const double* bath) {
+  if (!c || !bath || inst < 0 || inst >= c->n_inst) return fail(c, SWE_ERR_ARG, "bad arguments");
+  Layout& L = c->L;
+  for (int i = 0; i < c->meshes[inst].np; i++) L.bath[L.new_of_old[inst][i]] = bath[i];
+  const int64_t r0 = L.row_off[inst], nr = L.row_off[inst + 1] - r0;
+  if (c->precision == SWE_PREC_FP64) {
+    CK(cudaMemcpyAsync((double*)c->G.bath + r0, L.bath.data() + r0, nr * sizeof(double), cudaMemcpyHostToDevice,
+                       c->stream));
+  } else {
+    std::vector<float> bf(nr);
+    for (int64_t r = 0; r < nr; r++) bf[r] = (float)L.bath[r0 + r];
+    CK(cudaMemcpyAsync((double*)c->G.bath + r0, L.bath.data() + r0, nr * sizeof(double), cudaMemcpyHostToDevice,
+                       c->stream));
+    CK(cudaMemcpyAsync((float*)c->G.bathf + r0, bf.data(), nr * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return SWE_OK;
 }
 
 SWE_API int swe_set_dirichlet(swe_ctx* c, int inst, int comp, int n, const int* js, const double* vals) {
@@ -666,9 +703,11 @@ SWE_API int swe_rk3_steps(swe_ctx* c, int nsteps, double* time_out, double* dt_o
   if ((rc = restore_done(c, hs))) return rc;
   const int chunk = nsteps >= 8 ? 8 : 1;
   long long launches = 0;
+  if (!c->t0) { CK(cudaEventCreate(&c->t0)); CK(cudaEventCreate(&c->t1)); }
+  if (nsteps >= chunk && chunk > 1 && (rc = build_graph(c, chunk))) return rc;
+  CK(cudaEventRecord(c->t0, c->stream));
   const long long per_step = 3LL * kLaunchesPerStage + kLaunchesPerStepExtra;
   if (nsteps >= chunk && chunk > 1) {
-    if ((rc = build_graph(c, chunk))) return rc;
     for (int k = 0; k + chunk <= nsteps; k += chunk) {
       CK(cudaGraphLaunch(c->gexec, c->stream));
       launches += per_step * chunk;
@@ -679,6 +718,7 @@ SWE_API int swe_rk3_steps(swe_ctx* c, int nsteps, double* time_out, double* dt_o
     enqueue_step(c);
     launches += per_step;
   }
+  CK(cudaEventRecord(c->t1, c->stream));
   CK(cudaGetLastError());
   c->last_launches = launches;
   c->euler_done = false;
@@ -691,7 +731,25 @@ SWE_API int swe_rk3_steps(swe_ctx* c, int nsteps, double* time_out, double* dt_o
     if (dt_out) dt_out[b] = out[b].dt;
   }
   if (steps_done) *steps_done = out[0].steps;
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, c->t0, c->t1));
+  c->last_ms = ms;
   return rc;
+}
+
+SWE_API double swe_last_device_ms(const swe_ctx* c) { return c ? c->last_ms : 0.0; }
+
+SWE_API int swe_profile_kernels(swe_ctx* c, int nsteps, double* ms_out) {
+  if (!c || nsteps <= 0 || !ms_out) return fail(c, SWE_ERR_ARG, "bad arguments");
+  KernelEvents kev;
+  for (int k = 0; k < 10; k++) CK(cudaEventCreate(&kev.ev[k]));
+  double acc[SWE_NKERNELS] = {0, 0, 0, 0, 0};
+  for (int n = 0; n < nsteps; n++) enqueue_step(c, &kev, acc);
+  CK(cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < 10; k++) cudaEventDestroy(kev.ev[k]);
+  ms_out[0] = acc[0] / nsteps;
+  for (int k = 1; k < SWE_NKERNELS; k++) ms_out[k] = acc[k] / (3.0 * nsteps);
+  return read_errors(c);
 }
 
 SWE_API int swe_mass(swe_ctx* c, double* mass_out) {

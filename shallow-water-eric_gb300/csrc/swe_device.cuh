@@ -48,6 +48,17 @@ __device__ __forceinline__ int64_t entry_base(const Graph& G, int64_t r) {
   return G.slice_ptr[r >> 5] + (r & 31);
 }
 
+// FP32 shadow of an FP64 depth that keeps the sign of (h - htiny) and of h:
+// the mixed kernels branch on h <= htiny and h <= 0 (SOURCES/update.f90:572-582,
+// 644-655) with the shadow, so both branch decisions must match the FP64 depth.
+__device__ __forceinline__ float shadow_depth(double h, double htiny) {
+  float f = (float)h;
+  const float ft = (float)htiny;
+  if (h > htiny && !(f > ft)) f = nextafterf(ft, 3.4e38f);
+  if (h > 0.0 && !(f > 0.0f)) f = 1.17549435e-38f;   // smallest normal (FTZ-safe)
+  return f;
+}
+
 template <typename T> __device__ __forceinline__ T tmax(T a, T b) { return a > b ? a : b; }
 template <typename T> __device__ __forceinline__ T tmin(T a, T b) { return a < b ? a : b; }
 template <typename T> __device__ __forceinline__ T tabs(T a) { return a < T(0) ? -a : a; }

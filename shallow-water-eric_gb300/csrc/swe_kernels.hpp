@@ -63,7 +63,13 @@ struct StageArgsMix {
   int block;
 };
 
-void launch_stage_f64(const StageArgs& a, cudaStream_t s);
+// Optional per-kernel event timing: when non-null, ev[2k], ev[2k+1] bracket
+// the launch of kernel kind k (0 dt, 1 node, 2 low, 3 fct, 4 update).
+struct KernelEvents {
+  cudaEvent_t ev[10];
+};
+
+void launch_stage_f64(const StageArgs& a, cudaStream_t s, const KernelEvents* kev = nullptr);
 void launch_dt_f64(const Graph& G, const InstConst* C, InstState* St, const StateF64& u, double* d_out,
                    unsigned* err, int block, cudaStream_t s);
 void launch_step_begin(const InstConst* C, InstState* St, int n_inst, cudaStream_t s);
@@ -72,7 +78,7 @@ void launch_fct_positivity_f64(const Graph& G, const InstConst* C, const double*
                                double* rtmp, double* lij, cudaStream_t s);
 void launch_mass_f64(const Graph& G, const double* h, double* acc, cudaStream_t s);
 
-void launch_stage_mix(const StageArgsMix& a, cudaStream_t s);
+void launch_stage_mix(const StageArgsMix& a, cudaStream_t s, const KernelEvents* kev = nullptr);
 void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, unsigned* err, int block,
                    cudaStream_t s);
 

@@ -565,15 +565,23 @@ __global__ void k_mass_f64(Graph G, const double* __restrict__ h, double* __rest
 // ----------------------------- launchers -----------------------------------
 static inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
-void launch_stage_f64(const StageArgs& a, cudaStream_t s) {
+#define EV_BEGIN(k) if (kev) cudaEventRecord(kev->ev[2 * (k)], s)
+#define EV_END(k) if (kev) cudaEventRecord(kev->ev[2 * (k) + 1], s)
+
+void launch_stage_f64(const StageArgs& a, cudaStream_t s, const KernelEvents* kev) {
   const int bs = a.block;
   NodeF64 nd{a.w.ovh, a.w.v1, a.w.v2, a.w.ent, a.w.alpha};
+  EV_BEGIN(1);
   k_node_f64<<<nblk(a.G.n_rows, bs), bs, 0, s>>>(a.G, a.C, a.St, a.u, nd);
+  EV_END(1); EV_BEGIN(2);
   k_low_f64<<<nblk(a.G.n_rows, bs), bs, 0, s>>>(a.G, a.C, a.St, a.u, nd, a.w.dL, a.w.muL, a.w.uL, a.w.res, a.err);
+  EV_END(2); EV_BEGIN(3);
   k_fct_f64<<<nblk(a.G.n_rows, bs), bs, 0, s>>>(a.G, a.C, a.St, a.u, a.w.dL, a.w.muL, a.w.uL, a.w.res, a.w.fct,
                                                 a.w.rminus, a.err);
+  EV_END(3); EV_BEGIN(4);
   k_update_f64<<<nblk(a.G.n_rows, bs), bs, 0, s>>>(a.G, a.C, a.St, a.u, a.w.dL, a.w.muL, a.w.uL, a.w.res, a.w.fct,
                                                    a.w.rminus, a.u0, a.out, a.rk_stage, a.lij_out, a.err);
+  EV_END(4);
 }
 
 void launch_dt_f64(const Graph& G, const InstConst* C, InstState* St, const StateF64& u, double* d_out,

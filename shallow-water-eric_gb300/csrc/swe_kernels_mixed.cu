@@ -15,6 +15,31 @@
 namespace swe {
 
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
+
+// c . v with an explicit rounding sequence.  The low-order mass flux
+// (-c.v_j + mu_ij) h_j is non-negative only if mu_ij >= c.v_j holds bit for
+// bit; FMA contraction chosen independently at two sites would break that.
+__device__ __forceinline__ float dotc(float cx, float cy, float vx, float vy) {
+  return __fmaf_rn(cx, vx, __fmul_rn(cy, vy));
+}
+
+// Hydrostatic reconstruction H*_ij = max(0, h_i + z_i - max(z_i, z_j))
+// (SOURCES/update.f90:569-570) in the algebraically equal, cancellation-free
+// form max(0, h_i - max(0, z_j - z_i)).  In FP32 the reference form loses
+// (h_i + z_i) - z_i to rounding at the scale of z, which for thin layers on
+// high bathymetry is a large relative error in H*/h.  rat = H*/h is 1
+// exactly when z_j <= z_i and never exceeds 1.
+struct Recon {
+  float Hij, Hji, rij, rji;   // rij, rji: H*/h with the h <= 0 tests
+};
+__device__ __forceinline__ Recon recon(float hi, float hj, float dz, float invhi, float invhj) {
+  Recon R;
+  R.Hij = (dz <= 0.f) ? hi : fmaxf(0.f, hi - dz);
+  R.Hji = (dz >= 0.f) ? hj : fmaxf(0.f, hj + dz);
+  R.rij = (hi > 0.f) ? ((dz <= 0.f) ? 1.f : fminf(R.Hij * invhi, 1.f)) : 0.f;
+  R.rji = (hj > 0.f) ? ((dz >= 0.f) ? 1.f : fminf(R.Hji * invhj, 1.f)) : 0.f;
+  return R;
+}
 __device__ __forceinline__ float ovh_f(float h, float htiny) {
   float mh = fmaxf(h, htiny);
   return fdiv(2.0f * h, h * h + mh * mh);
@@ -47,22 +72,28 @@ __global__ void k_node_mix(Graph G, const InstConst* __restrict__ C, const InstS
   alpha_out[r] = alpha;
 }
 
-struct NodeF {   // FP32 view of one node used by the edge loops
+struct NodeF {   // FP32 view of one node used by the edge loop
   float h, q1, q2, z, ovh, v1, v2;
 };
 
-__device__ __forceinline__ NodeF load_node(const Graph& G, const StateMix& u, int64_t j, float htiny, bool sgn) {
+__device__ __forceinline__ NodeF load_node(const Graph& G, const StateMix& u, int64_t j, float htiny) {
   NodeF n;
   n.h = u.hf[j]; n.q1 = u.q1[j]; n.q2 = u.q2[j]; n.z = G.bathf[j];
   n.ovh = ovh_f(n.h, htiny);
   n.v1 = n.q1 * n.ovh;
-  n.v2 = sgn ? 0.0f : n.q2 * n.ovh;
+  n.v2 = n.q2 * n.ovh;
   return n;
 }
 
-// k_low_mix: d_ij, mu_ij, alpha limiting, low-order RHS, Galerkin RHS and
-// entropy residual of one row (SOURCES/update.f90:180-210, 291-364, 554-682,
-// 750-799, 825-878).
+// k_low_mix: one pass over the row's entries computing d_ij (lambda_max),
+// mu_ij, their alpha scaling, the low-order RHS (smb_2_roundoff), the
+// Galerkin RHS (smb_2) and the entropy stencil max/min, then the low-order
+// state and the entropy residual (SOURCES/update.f90:180-210, 291-364,
+// 554-682, 750-799, 825-878).  Each neighbour is loaded once, and c.v_j is
+// formed once and shared by mu_ij and the Galerkin flux, so the low-order
+// mass flux (mu_ij - c.v_j) h_j stays non-negative bit for bit.  The
+// diagonal entry only enters through terms that vanish identically
+// (u_i rat_ii - u_i rat_ii), so the diagonal's d, mu are written but not used.
 __global__ void __launch_bounds__(128) k_low_mix(Graph G, const InstConst* __restrict__ C,
                                                  const InstState* __restrict__ St, StateMix u,
                                                  const float* __restrict__ alpha, float* __restrict__ dL,
@@ -82,88 +113,90 @@ __global__ void __launch_bounds__(128) k_low_mix(Graph G, const InstConst* __res
   const float sqrt2 = 1.41421356237309515f;
   const int64_t base = entry_base(G, r);
   const int dp = G.dpos[r];
-  const NodeF ni = load_node(G, u, r, htiny, sgn);
+  const NodeF ni = load_node(G, u, r, htiny);
+  const float v2i_flux = sgn ? 0.f : ni.v2;          // flux() zeroes velocity(2) for type 13
   const float ai = alpha[r];
   const float m = (float)G.lumped[r];
   float ui3 = 0.f, ui4 = 0.f;
   if (S == 5) { ui3 = u.q3[r]; ui4 = u.q4[r]; }
+  const float invhi = (ni.h > 0.f) ? fdiv(1.0f, ni.h) : 0.f;
   bool delta_bad = false;
 
-  // pass 1: d_ij = |c_ij| lambda_max, mu_ij; MAX(d, mu); alpha scaling
   float sd = 0.f, sm_raw = 0.f, sm = 0.f;
+  float fix = 0.f, rk0 = 0.f, rk[5] = {0, 0, 0, 0, 0}, rk2[5] = {0, 0, 0, 0, 0};
+  const float Ei = 0.5f * (g * ni.h * ni.h + ni.v1 * ni.q1 + v2i_flux * ni.q2);
+  float emax = Ei, emin = Ei;
+  float ptx = 0.f, pty = 0.f;
+  const float ivi_x = ni.v1, ivi_y = ni.v2;
   for (int k = 0; k < L; k++) {
     const int64_t e = base + 32 * k;
-    float d = 0.f, mu = 0.f;
-    if (k != dp) {
-      const int j = G.col[e];
-      const NodeF nj = load_node(G, u, j, htiny, false);
-      const float cxe = G.cxf[e], cye = G.cyf[e];
-      const float norm = sqrtf(cxe * cxe + cye * cye);
-      const float inv = fdiv(1.0f, norm);
-      float lam;
-      if (!lambda_vacc<float>(ni.h, ni.q1, ni.q2, ni.ovh, nj.h, nj.q1, nj.q2, nj.ovh, cxe * inv, cye * inv, g, htiny,
-                              sqrt2, &lam))
-        delta_bad = true;
-      d = norm * lam;
-      const float vi1 = ni.q1 * ni.ovh, vi2 = ni.q2 * ni.ovh;
-      mu = fmaxf(fmaxf(-(cxe * vi1 + cye * vi2), 0.f), fmaxf(cxe * nj.v1 + cye * nj.v2, 0.f));
-      sm_raw += mu;
-      d = fmaxf(d, mu);
-      if (c.alpha_limit) {
-        const float s = fmaxf(ai, alpha[j]);
-        d *= s;
-        mu *= s;
+    const float cxe = G.cxf[e], cye = G.cyf[e];
+    if (k == dp) {
+      // diagonal: Galerkin boundary term -c_ii.v_i (fix_roundoff / smb_2), no viscosity
+      const float cvi = dotc(cxe, cye, ni.v1, v2i_flux);
+      fix += -cvi;
+      rk2[0] += -cvi * ni.h;
+      rk[1] += -cvi * ni.q1; rk[2] += -cvi * ni.q2;
+      rk2[1] += -cvi * ni.q1; rk2[2] += -cvi * ni.q2;
+      if (S == 5) { rk[3] += -cvi * ui3; rk[4] += -cvi * ui4; rk2[3] += -cvi * ui3; rk2[4] += -cvi * ui4; }
+      if (sgn) {
+        const float pc = fdiv((float)c.lambda_sgn * g, 3.0f * sqrtf(m));
+        const float x = fdiv(ui3, ni.h * ni.h);
+        const float pt = pc * ni.h * ni.h * ni.h * (2.f + 4.f * x * x * x - 6.f * x * x * x * x);
+        ptx -= pt * cxe;
+        pty -= pt * cye;
       }
+      continue;
+    }
+    const int j = G.col[e];
+    const NodeF nj = load_node(G, u, j, htiny);
+    float uj3 = 0.f, uj4 = 0.f;
+    if (S == 5) { uj3 = u.q3[j]; uj4 = u.q4[j]; }
+    // --- viscosities: compute_dij, compute_muij, MAX, alpha_limit
+    const float norm = sqrtf(cxe * cxe + cye * cye);
+    const float inv = fdiv(1.0f, norm);
+    float lam;
+    if (!lambda_vacc<float>(ni.h, ni.q1, ni.q2, ni.ovh, nj.h, nj.q1, nj.q2, nj.ovh, cxe * inv, cye * inv, g, htiny,
+                            sqrt2, &lam))
+      delta_bad = true;
+    const float cvj = dotc(cxe, cye, nj.v1, nj.v2);                   // c.v_j (compute_muij)
+    float mu = fmaxf(fmaxf(-dotc(cxe, cye, ivi_x, ivi_y), 0.f), fmaxf(cvj, 0.f));
+    sm_raw += mu;
+    float d = fmaxf(norm * lam, mu);
+    if (c.alpha_limit) {
+      const float s = fmaxf(ai, alpha[j]);
+      d *= s;
+      mu *= s;
     }
     sd += d;
     sm += mu;
     dL[e] = d;
     muL[e] = mu;
-  }
-  // diagonals: only used through terms that vanish; keep the reference values
-  dL[base + 32 * dp] = -sd;
-  muL[base + 32 * dp] = c.alpha_limit ? -(sm - sm_raw) : -sm_raw;
-
-  // pass 2: smb_2_roundoff (low order) and smb_2 (Galerkin) rows, maxmin(E)
-  float fix = 0.f, rk0 = 0.f, rk[5] = {0, 0, 0, 0, 0}, rk2[5] = {0, 0, 0, 0, 0};
-  const float Ei = 0.5f * (g * ni.h * ni.h + ni.v1 * ni.q1 + ni.v2 * ni.q2);
-  float emax = Ei, emin = Ei;
-  float ptx = 0.f, pty = 0.f;
-  for (int k = 0; k < L; k++) {
-    const int64_t e = base + 32 * k;
-    const int j = G.col[e];
-    const NodeF nj = (k == dp) ? ni : load_node(G, u, j, htiny, sgn);
-    float uj3 = 0.f, uj4 = 0.f;
-    if (S == 5) { uj3 = u.q3[j]; uj4 = u.q4[j]; }
-    const float d = dL[e], mu = muL[e];
-    const float cxe = G.cxf[e], cye = G.cyf[e];
-    const float Ej = 0.5f * (g * nj.h * nj.h + nj.v1 * nj.q1 + nj.v2 * nj.q2);
+    // --- entropy stencil
+    const float v2j_flux = sgn ? 0.f : nj.v2;
+    const float Ej = 0.5f * (g * nj.h * nj.h + nj.v1 * nj.q1 + v2j_flux * nj.q2);
     emax = fmaxf(emax, Ej);
     emin = fminf(emin, Ej);
-    const float zmax = fmaxf(ni.z, nj.z);
-    const float Hij = fmaxf(0.f, ni.h + ni.z - zmax);
-    const float Hji = fmaxf(0.f, nj.h + nj.z - zmax);
-    const float invhi = (ni.h > 0.f) ? fdiv(1.0f, ni.h) : 0.f;
+    // --- hydrostatic reconstruction
+    const float dz = nj.z - ni.z;
     const float invhj = (nj.h > 0.f) ? fdiv(1.0f, nj.h) : 0.f;
-    const float rij = Hij * invhi, rji = Hji * invhj;                 // h <= 0 tests (smb_2)
+    const Recon R = recon(ni.h, nj.h, dz, invhi, invhj);
+    const float rij = R.rij, rji = R.rji;                             // h <= 0 tests (smb_2)
     const float rijt = (ni.h <= htiny) ? 0.f : rij;                   // h <= htiny tests
     const float rjit = (nj.h <= htiny) ? 0.f : rji;
-    const float gal_h = -(cxe * nj.v1 + cye * nj.v2);                 // -c.v_j
-    const float topo = g * ni.h * ((nj.h + nj.z) - ni.h - ni.z);
-    if (k == dp) {
-      fix += gal_h;
-    } else {
-      fix += -mu - (d - mu) * rijt;
-      rk0 += (gal_h + mu) * nj.h + fmaxf((d - mu) * Hji, 0.f);
-    }
-    // mass row of smb_2
-    rk2[0] += gal_h * nj.h + d * (nj.h * rji - ni.h * rij) + mu * (nj.h * (1.f - rji) - ni.h * (1.f - rij));
-    float uq_i[5] = {ni.h, ni.q1, ni.q2, ui3, ui4};
-    float uq_j[5] = {nj.h, nj.q1, nj.q2, uj3, uj4};
+    const float cvj_flux = sgn ? dotc(cxe, cye, nj.v1, 0.f) : cvj;   // -c.velocity_j of flux()
+    const float topo = g * ni.h * ((nj.h - ni.h) + dz);               // g h_i (eta_j - eta_i)
+    // --- smb_2_roundoff mass row (fix_roundoff, rk_1)
+    fix += -mu - (d - mu) * rijt;
+    rk0 += (mu - cvj_flux) * nj.h + fmaxf((d - mu) * R.Hji, 0.f);
+    // --- smb_2 mass row
+    rk2[0] += -cvj_flux * nj.h + d * (nj.h * rji - ni.h * rij) + mu * (nj.h * (1.f - rji) - ni.h * (1.f - rij));
+    const float uq_i[5] = {ni.h, ni.q1, ni.q2, ui3, ui4};
+    const float uq_j[5] = {nj.h, nj.q1, nj.q2, uj3, uj4};
 #pragma unroll
     for (int q = 1; q < 5; q++) {
       if (q >= S) break;
-      const float gal = -(cxe * nj.v1 + cye * nj.v2) * uq_j[q];
+      const float gal = -cvj_flux * uq_j[q];
       rk[q] += gal + d * (uq_j[q] * rjit - uq_i[q] * rijt) + mu * (uq_j[q] * (1.f - rjit) - uq_i[q] * (1.f - rijt));
       rk2[q] += gal + d * (uq_j[q] * rji - uq_i[q] * rij) + mu * (uq_j[q] * (1.f - rji) - uq_i[q] * (1.f - rij));
     }
@@ -178,6 +211,9 @@ __global__ void __launch_bounds__(128) k_low_mix(Graph G, const InstConst* __res
       pty -= pt * cye;
     }
   }
+  // diagonals (-row sums, with the reference's mu re-summation under alpha)
+  dL[base + 32 * dp] = -sd;
+  muL[base + 32 * dp] = c.alpha_limit ? -(sm - sm_raw) : -sm_raw;
   // source terms
   if (c.type_test == 9 || c.type_test == 10) {
     const float fric = (float)(c.g * c.mannings * c.mannings);
@@ -185,8 +221,8 @@ __global__ void __launch_bounds__(128) k_low_mix(Graph G, const InstConst* __res
     const float vel = fric * sqrtf(ni.v1 * ni.v1 + ni.v2 * ni.v2);
     const float hloc = vel * dtf;
     const float coef = fdiv(m * vel * 2.f, hstar + fmaxf(hstar, hloc));
-    const float uq_i[3] = {ni.h, ni.q1, ni.q2};
-    for (int q = 1; q < 3; q++) { rk[q] -= coef * uq_i[q]; rk2[q] -= coef * uq_i[q]; }
+    rk[1] -= coef * ni.q1; rk[2] -= coef * ni.q2;
+    rk2[1] -= coef * ni.q1; rk2[2] -= coef * ni.q2;
   } else if (c.type_test == 11) {
     rk[1] -= m * 0.2f * ni.q1; rk[2] -= m * 0.2f * ni.q2;
     rk2[1] -= m * 0.2f * ni.q1; rk2[2] -= m * 0.2f * ni.q2;
@@ -211,7 +247,6 @@ __global__ void __launch_bounds__(128) k_low_mix(Graph G, const InstConst* __res
   else hL = fmax(u.h[r] + dtd * (double)rk2[0] * inv_m, 0.0);
   const float invm = (float)inv_m;
   uL.h[r] = hL;
-  uL.hf[r] = (float)hL;
   uL.q1[r] = ni.q1 + dtf * (rk[1] * invm);
   uL.q2[r] = ni.q2 + dtf * (rk[2] * invm);
   if (S == 5) { uL.q3[r] = ui3 + dtf * (rk[3] * invm); uL.q4[r] = ui4 + dtf * (rk[4] * invm); }
@@ -221,9 +256,9 @@ __global__ void __launch_bounds__(128) k_low_mix(Graph G, const InstConst* __res
   for (int q = 0; q < 3; q++) un_[q] = uq_i[q] + dtf * (rk2[q] * invm);
   const float on = ovh_f(un_[0], htiny);
   const float En = 0.5f * (g * un_[0] * un_[0] + (un_[1] * on) * un_[1] + (un_[2] * on) * un_[2]);
-  const float Ep0 = g * ni.h - 0.5f * (ni.v1 * ni.v1) - 0.5f * (ni.v2 * ni.v2);
+  const float Ep0 = g * ni.h - 0.5f * (ni.v1 * ni.v1) - 0.5f * (v2i_flux * v2i_flux);
   float rs = m * fdiv(En - Ei, dtf);
-  rs -= rk2[0] * Ep0 + rk2[1] * ni.v1 + rk2[2] * ni.v2;
+  rs -= rk2[0] * Ep0 + rk2[1] * ni.v1 + rk2[2] * v2i_flux;
   const float rescale = 0.5f * fabsf(emax - emin) + (float)c.rescale_floor;
   res[r] = fdiv(fabsf(rs), rescale);
   if (delta_bad) atomicOr(err, ERRB_DELTA);
@@ -232,11 +267,13 @@ __global__ void __launch_bounds__(128) k_low_mix(Graph G, const InstConst* __res
 // antidiffusive h-flux f_ij of compute_fct_matrix (update.f90:744-745)
 __device__ __forceinline__ float fct_flux(float d0, float m0, float rij, float hi, float zi, float hj, float zj) {
   const float dd = fminf(d0, rij) - d0, dm = fminf(m0, rij) - m0;
-  const float zmax = fmaxf(zi, zj);
-  const float Hij = fmaxf(0.f, hi + zi - zmax), Hji = fmaxf(0.f, hj + zj - zmax);
-  const float ratij = (hi <= 0.f) ? 0.f : fdiv(Hij, hi);
-  const float ratji = (hj <= 0.f) ? 0.f : fdiv(Hji, hj);
-  return dd * (hj * ratji - hi * ratij) + dm * (hj * (1.f - ratji) - hi * (1.f - ratij));
+  const float invhi = (hi > 0.f) ? fdiv(1.0f, hi) : 0.f;
+  const float invhj = (hj > 0.f) ? fdiv(1.0f, hj) : 0.f;
+  const Recon R = recon(hi, hj, zj - zi, invhi, invhj);
+  // explicit roundings: k_fct (P^-) and k_update (sum l f) must see the same f
+  const float a = __fsub_rn(__fmul_rn(hj, R.rji), __fmul_rn(hi, R.rij));
+  const float b = __fsub_rn(__fmul_rn(hj, __fsub_rn(1.f, R.rji)), __fmul_rn(hi, __fsub_rn(1.f, R.rij)));
+  return __fadd_rn(__fmul_rn(dd, a), __fmul_rn(dm, b));
 }
 
 // k_fct_mix: f_ij (FP32) and R^-_i (FP64 Q^-, P^-, R^-), fct.f90:15-30
@@ -263,7 +300,9 @@ __global__ void k_fct_mix(Graph G, const InstConst* __restrict__ C, const InstSt
   const double hL = uL.h[r];
   if (hL < 0.0) atomicOr(err, ERRB_NEG_H);
   const double scaled = G.lumped[r] * st.inv_dt * hL;
-  double R = fmin((0.0 - scaled) / P, 1.0);
+  // Q^-/P^- with Q^- shrunk by 4 ulp: the update multiplies by dt/m through
+  // reciprocals, and the limited sum must not overshoot -h^L by rounding
+  double R = fmin((0.0 - scaled) * (1.0 - 8.881784197001252e-16) / P, 1.0);
   if (scaled <= c.htiny) R = 0.0;
   rminus[r] = R;
 }
@@ -301,10 +340,10 @@ __global__ void k_update_mix(Graph G, const InstConst* __restrict__ C, const Ins
     sh += l * (double)f;
     const float lf = (float)l;
     const float dd = (fminf(d0, rij) - d0) * lf, dm = (fminf(m0, rij) - m0) * lf;
-    const float zmax = fmaxf(zi, zj);
-    const float Hij = fmaxf(0.f, hi + zi - zmax), Hji = fmaxf(0.f, hj + zj - zmax);
-    const float ratij = (hi <= 0.f) ? 0.f : fdiv(Hij, hi);
-    const float ratji = (hj <= 0.f) ? 0.f : fdiv(Hji, hj);
+    const float invhi = (hi > 0.f) ? fdiv(1.0f, hi) : 0.f;
+    const float invhj = (hj > 0.f) ? fdiv(1.0f, hj) : 0.f;
+    const Recon R = recon(hi, hj, zj - zi, invhi, invhj);
+    const float ratij = R.rij, ratji = R.rji;
     float uj[5] = {hj, u.q1[j], u.q2[j], 0.f, 0.f};
     if (S == 5) { uj[3] = u.q3[j]; uj[4] = u.q4[j]; }
 #pragma unroll
@@ -338,7 +377,7 @@ __global__ void k_update_mix(Graph G, const InstConst* __restrict__ C, const Ins
       if (msk & (1u << q)) qn[q] = (float)G.dir_val[(int64_t)q * G.n_rows + r];
   }
   out.h[r] = hn;
-  out.hf[r] = (float)hn;
+  out.hf[r] = shadow_depth(hn, c.htiny);
   out.q1[r] = qn[1];
   out.q2[r] = qn[2];
   if (S == 5) { out.q3[r] = qn[3]; out.q4[r] = qn[4]; }
@@ -389,15 +428,23 @@ __global__ void k_dt_mix(Graph G, const InstConst* __restrict__ C, InstState* __
 
 static inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
-void launch_stage_mix(const StageArgsMix& a, cudaStream_t s) {
+#define EV_BEGIN(k) if (kev) cudaEventRecord(kev->ev[2 * (k)], s)
+#define EV_END(k) if (kev) cudaEventRecord(kev->ev[2 * (k) + 1], s)
+
+void launch_stage_mix(const StageArgsMix& a, cudaStream_t s, const KernelEvents* kev) {
   const int bs = a.block;
   const unsigned nb = nblk(a.G.n_rows, bs);
+  EV_BEGIN(1);
   k_node_mix<<<nb, bs, 0, s>>>(a.G, a.C, a.St, a.u, a.w.alpha);
+  EV_END(1); EV_BEGIN(2);
   k_low_mix<<<nblk(a.G.n_rows, 128), 128, 0, s>>>(a.G, a.C, a.St, a.u, a.w.alpha, a.w.dL, a.w.muL, a.w.uL, a.w.res,
                                                    a.err);
+  EV_END(2); EV_BEGIN(3);
   k_fct_mix<<<nb, bs, 0, s>>>(a.G, a.C, a.St, a.u, a.w.dL, a.w.muL, a.w.uL, a.w.res, a.w.rminus, a.err);
+  EV_END(3); EV_BEGIN(4);
   k_update_mix<<<nb, bs, 0, s>>>(a.G, a.C, a.St, a.u, a.w.dL, a.w.muL, a.w.uL, a.w.res, a.w.rminus, a.u0, a.out,
                                  a.rk_stage, a.err);
+  EV_END(4);
 }
 
 void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, unsigned* err, int block,

@@ -30,11 +30,14 @@ class swe_params(ctypes.Structure):
 
 # every symbol include/swe_gpu.h declares
 EXPORTS = [
-    "swe_create", "swe_create_batch", "swe_destroy", "swe_last_error", "swe_set_params", "swe_set_dirichlet",
+    "swe_create", "swe_create_batch", "swe_destroy", "swe_last_error", "swe_set_params", "swe_set_bath",
+    "swe_set_dirichlet",
     "swe_sizes", "swe_get_matrices", "swe_compute_dij", "swe_euler", "swe_euler_intermediates",
     "swe_fct_positivity", "swe_upload", "swe_download", "swe_upload_device", "swe_download_device",
     "swe_set_time", "swe_rk3_steps", "swe_mass", "swe_last_launch_count", "swe_tuning",
+    "swe_last_device_ms", "swe_profile_kernels",
 ]
+KERNEL_KINDS = ("dt", "node", "low", "fct", "update")
 
 _lib = None
 
@@ -66,6 +69,7 @@ def load(build: bool = True):
         "swe_destroy": ([vp], None),
         "swe_last_error": ([vp], ctypes.c_char_p),
         "swe_set_params": ([vp, ctypes.c_int, pp], ctypes.c_int),
+        "swe_set_bath": ([vp, ctypes.c_int, dp], ctypes.c_int),
         "swe_set_dirichlet": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ip, dp], ctypes.c_int),
         "swe_sizes": ([vp, ctypes.c_int, ip, ip], ctypes.c_int),
         "swe_get_matrices": ([vp, ctypes.c_int, ip, ip, dp, dp, ip, dp, dp], ctypes.c_int),
@@ -82,6 +86,8 @@ def load(build: bool = True):
         "swe_mass": ([vp, dp], ctypes.c_int),
         "swe_last_launch_count": ([vp], ctypes.c_longlong),
         "swe_tuning": ([vp], ctypes.c_char_p),
+        "swe_last_device_ms": ([vp], ctypes.c_double),
+        "swe_profile_kernels": ([vp, ctypes.c_int, dp], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -198,20 +198,27 @@ def jittered_mesh(nx, ny, x0, x1, y0, y1, jitter=0.3, seed=0):
     rr = np.vstack([X.ravel(), Y.ravel()])
     tri = Delaunay(rr.T, qhull_options="Qbb Qc Qz Q12").simplices.T.astype(np.int64)
     jj = _ccw((tri + 1).astype(np.int32), rr)
-    # drop slivers of zero area that qhull may emit on the straight boundary
     x, y = rr[0], rr[1]
     a, b, c = jj[0] - 1, jj[1] - 1, jj[2] - 1
     area = 0.5 * ((x[b] - x[a]) * (y[c] - y[a]) - (y[b] - y[a]) * (x[c] - x[a]))
-    jj = jj[:, area > 1e-12 * dx * dy]
-    # element order: sort by centroid along y then x, so that element (and
-    # first-touch node) order follows the lattice
-    cy = (y[jj[0] - 1] + y[jj[1] - 1] + y[jj[2] - 1]) / 3
-    cx = (x[jj[0] - 1] + x[jj[1] - 1] + x[jj[2] - 1]) / 3
+    if jj.shape[1] != 2 * (nx - 1) * (ny - 1) or not (area > 1e-12 * dx * dy).all():
+        raise RuntimeError("degenerate Delaunay triangulation of the jittered lattice")
+    # element order: by centroid row then x, so that element (and first-touch
+    # node) order follows the lattice
+    cy = (y[a] + y[b] + y[c]) / 3
+    cx = (x[a] + x[b] + x[c]) / 3
     order = np.lexsort((cx, np.floor(cy / dy)))
     jj = np.ascontiguousarray(jj[:, order])
-    tol = 1e-9 * max(x1 - x0, y1 - y0)
-    jjs, sides = _rect_boundary(jj, rr, x0, x1, y0, y1, tol)
-    return dict(jj=np.asfortranarray(jj), rr=np.asfortranarray(rr), jjs=jjs, sides=sides)
+    # the hull is the rectangle and every lattice boundary point is a hull
+    # vertex (boundary points only move along their side), so the boundary
+    # edges join consecutive lattice boundary points: 1=x-min 2=y-min 3=x-max 4=y-max
+    i = np.arange(nx)
+    j = np.arange(ny)
+    segs = [(j * nx, 1, ny), (i, 2, nx), (j * nx + nx - 1, 3, ny), (i + nx * (ny - 1), 4, nx)]
+    jjs = np.hstack([np.vstack([n[:-1], n[1:]]) for n, _, _ in segs]) + 1
+    sides = np.concatenate([np.full(k - 1, sd) for _, sd, k in segs])
+    return dict(jj=np.asfortranarray(jj), rr=np.asfortranarray(rr), jjs=jjs.astype(np.int32),
+                sides=sides.astype(np.int32))
 
 
 def concat_meshes(meshes):

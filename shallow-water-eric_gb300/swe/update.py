@@ -99,6 +99,10 @@ class Update:
         cp = to_c_params(p)
         self._check(self._L.swe_set_params(self.h, inst, ctypes.byref(cp)))
 
+    def set_bath(self, bath, inst=0):
+        b = np.ascontiguousarray(bath, np.float64)
+        self._check(self._L.swe_set_bath(self.h, inst, _L.dp(b)))
+
     def set_dirichlet(self, comp, js, vals=None, inst=0):
         js = np.ascontiguousarray(js, np.int32)
         v = None if vals is None else np.ascontiguousarray(vals, np.float64)
@@ -152,6 +156,13 @@ class Update:
         u = self.download()
         return [u[:, self.node_off[b]:self.node_off[b + 1]] for b in range(self.n_inst)]
 
+    def upload_ptr(self, host_ptr: int):
+        """Upload from a raw host pointer (e.g. pinned memory) in the reference layout."""
+        self._check(self._L.swe_upload(self.h, ctypes.cast(host_ptr, ctypes.POINTER(ctypes.c_double))))
+
+    def download_ptr(self, host_ptr: int):
+        self._check(self._L.swe_download(self.h, ctypes.cast(host_ptr, ctypes.POINTER(ctypes.c_double))))
+
     def upload_device(self, ptr: int):
         self._check(self._L.swe_upload_device(self.h, ctypes.c_void_p(ptr)))
 
@@ -176,6 +187,17 @@ class Update:
     @property
     def last_launch_count(self):
         return int(self._L.swe_last_launch_count(self.h))
+
+    @property
+    def last_device_ms(self):
+        return float(self._L.swe_last_device_ms(self.h))
+
+    def profile_kernels(self, nsteps):
+        """Average device ms per launch of each kernel kind (dt, node, low,
+        fct, update) over nsteps event-bracketed steps."""
+        out = np.zeros(len(_L.KERNEL_KINDS))
+        self._check(self._L.swe_profile_kernels(self.h, nsteps, _L.dp(out)))
+        return dict(zip(_L.KERNEL_KINDS, out.tolist()))
 
     @property
     def tuning(self):
