@@ -121,8 +121,8 @@ static int alloc_state_f64(swe_ctx* c, StateF64& s, cudaError_t& st) {
 
 static int alloc_state_mix(swe_ctx* c, StateMix& s, cudaError_t& st) {
   const size_t n = c->L.n_rows;
-  s.h = c->buf.alloc<double>(n, st); s.hf = c->buf.alloc<float>(n, st);
-  s.q1 = c->buf.alloc<float>(n, st); s.q2 = c->buf.alloc<float>(n, st);
+  s.h = c->buf.alloc<double>(n, st);
+  s.nq = c->buf.alloc<float4>(n, st);
   if (c->S == 5) { s.q3 = c->buf.alloc<float>(n, st); s.q4 = c->buf.alloc<float>(n, st); }
   return st == cudaSuccess ? SWE_OK : SWE_ERR_CUDA;
 }
@@ -207,7 +207,9 @@ static int build_device(swe_ctx* c, const std::vector<std::vector<double>>& bath
     w.alpha = c->buf.alloc<float>(n, st); w.res = c->buf.alloc<float>(n, st);
     w.rminus = c->buf.alloc<double>(n, st);
     w.dL = c->buf.alloc<float>(ne, st); w.muL = c->buf.alloc<float>(ne, st);
-    alloc_state_mix(c, w.uL, st);
+    w.hL = c->buf.alloc<double>(n, st);
+    w.qL = c->buf.alloc<float2>(n, st);
+    if (c->S == 5) { w.q3L = c->buf.alloc<float>(n, st); w.q4L = c->buf.alloc<float>(n, st); }
   }
   if (st != cudaSuccess) return fail(c, SWE_ERR_CUDA, std::string("device allocation: ") + cudaGetErrorString(st));
   return SWE_OK;
@@ -232,26 +234,35 @@ __global__ void k_gather_out(double* __restrict__ stage, const int* __restrict__
 }
 __global__ void k_scatter_in_mix(const double* __restrict__ stage, const int* __restrict__ row_of_node,
                                  int64_t n_nodes, int S, StateMix a, const int* __restrict__ slice_inst,
-                                 const InstConst* __restrict__ C) {
+                                 const InstConst* __restrict__ C, const float* __restrict__ bathf) {
   int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (n >= n_nodes) return;
   const int64_t r = row_of_node[n];
   const double h = stage[n * S];
   a.h[r] = h;
-  a.hf[r] = shadow_depth(h, C[slice_inst[r >> 5]].htiny);
-  a.q1[r] = (float)stage[n * S + 1];
-  a.q2[r] = (float)stage[n * S + 2];
+  a.nq[r] = make_float4(shadow_depth(h, C[slice_inst[r >> 5]].htiny), (float)stage[n * S + 1],
+                        (float)stage[n * S + 2], bathf[r]);
   if (S == 5) { a.q3[r] = (float)stage[n * S + 3]; a.q4[r] = (float)stage[n * S + 4]; }
 }
+// mixed state (sm) or the mixed low-order state (w) back to the reference layout
 __global__ void k_gather_out_mix(double* __restrict__ stage, const int* __restrict__ row_of_node, int64_t n_nodes,
-                                 int S, StateMix a) {
+                                 int S, StateMix a, WorkMix w, int low) {
   int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (n >= n_nodes) return;
   const int64_t r = row_of_node[n];
-  stage[n * S] = a.h[r];
-  stage[n * S + 1] = a.q1[r];
-  stage[n * S + 2] = a.q2[r];
-  if (S == 5) { stage[n * S + 3] = a.q3[r]; stage[n * S + 4] = a.q4[r]; }
+  if (!low) {
+    const float4 v = a.nq[r];
+    stage[n * S] = a.h[r];
+    stage[n * S + 1] = v.y;
+    stage[n * S + 2] = v.z;
+    if (S == 5) { stage[n * S + 3] = a.q3[r]; stage[n * S + 4] = a.q4[r]; }
+  } else {
+    const float2 v = w.qL[r];
+    stage[n * S] = w.hL[r];
+    stage[n * S + 1] = v.x;
+    stage[n * S + 2] = v.y;
+    if (S == 5) { stage[n * S + 3] = w.q3L[r]; stage[n * S + 4] = w.q4L[r]; }
+  }
 }
 
 static int to_device(swe_ctx* c, const double* un, bool device_src, int64_t node_begin, int64_t node_end) {
@@ -267,19 +278,20 @@ static int to_device(swe_ctx* c, const double* un, bool device_src, int64_t node
   else
     k_scatter_in_mix<<<nb, 256, 0, c->stream>>>(c->d_stage + (size_t)c->S * node_begin,
                                                  c->d_row_of_node + node_begin, nn, c->S, c->mA, c->G.slice_inst,
-                                                 c->d_C);
+                                                 c->d_C, c->G.bathf);
   CK(cudaGetLastError());
   return SWE_OK;
 }
 
 static int from_device_state(swe_ctx* c, double* un, bool device_dst, int64_t node_begin, int64_t node_end,
-                             const StateF64* sf, const StateMix* sm) {
+                             const StateF64* sf, const StateMix* sm, bool low_mix = false) {
   const int64_t nn = node_end - node_begin;
   if (nn <= 0) return SWE_OK;
   const unsigned nb = (unsigned)((nn + 255) / 256);
   double* stg = c->d_stage + (size_t)c->S * node_begin;
   if (sf) k_gather_out<<<nb, 256, 0, c->stream>>>(stg, c->d_row_of_node + node_begin, nn, c->S, *sf);
-  else k_gather_out_mix<<<nb, 256, 0, c->stream>>>(stg, c->d_row_of_node + node_begin, nn, c->S, *sm);
+  else k_gather_out_mix<<<nb, 256, 0, c->stream>>>(stg, c->d_row_of_node + node_begin, nn, c->S,
+                                                    sm ? *sm : c->mA, c->wm, low_mix ? 1 : 0);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(un, stg, (size_t)c->S * nn * sizeof(double),
                      device_dst ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream));
@@ -473,6 +485,8 @@ SWE_API int swe_set_bath(swe_ctx* c, int inst, const double* bath) {
     CK(cudaMemcpyAsync((double*)c->G.bath + r0, L.bath.data() + r0, nr * sizeof(double), cudaMemcpyHostToDevice,
                        c->stream));
     CK(cudaMemcpyAsync((float*)c->G.bathf + r0, bf.data(), nr * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    launch_refresh_z(c->G, c->mA, c->stream);
+    CK(cudaGetLastError());
   }
   CK(cudaStreamSynchronize(c->stream));
   return SWE_OK;
@@ -620,7 +634,8 @@ SWE_API int swe_euler_intermediates(swe_ctx* c, int inst, double* dij_low, doubl
     if (alpha && (rc = rows_to_nodes(c, inst, c->wm.alpha, alpha))) return rc;
     if (res && (rc = rows_to_nodes(c, inst, c->wm.res, res))) return rc;
     if (rminus && (rc = rows_to_nodes(c, inst, c->wm.rminus, rminus))) return rc;
-    if (u_low && (rc = from_device_state(c, u_low, false, c->node_off[inst], c->node_off[inst + 1], nullptr, &c->wm.uL)))
+    if (u_low && (rc = from_device_state(c, u_low, false, c->node_off[inst], c->node_off[inst + 1], nullptr, nullptr,
+                                         true)))
       return rc;
   }
   CK(cudaStreamSynchronize(c->stream));

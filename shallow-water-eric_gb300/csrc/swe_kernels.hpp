@@ -13,14 +13,12 @@ struct StateF64 {
   double* q4;
 };
 
-// Mixed-precision state: h in FP64 (positivity and mass), the other
-// components and a shadow copy of h in FP32 (flux arithmetic, neighbour
-// gathers).
+// Mixed-precision state: h in FP64 (positivity and mass) plus a packed FP32
+// node record {h shadow, qx, qy, z} that neighbours gather with one 16-byte
+// load; type 13's h*eta and h*w in FP32.
 struct StateMix {
   double* h;
-  float* hf;
-  float* q1;
-  float* q2;
+  float4* nq;
   float* q3;
   float* q4;
 };
@@ -37,7 +35,9 @@ struct WorkMix {
   float *alpha, *res;                    // per row
   double* rminus;                        // per row (FP64 limiter)
   float *dL, *muL;                       // per entry
-  StateMix uL;                           // low-order state (h FP64)
+  double* hL;                            // low-order depth (FP64)
+  float2* qL;                            // low-order momenta
+  float *q3L, *q4L;                      // low-order h*eta, h*w (type 13)
 };
 
 struct StageArgs {
@@ -81,6 +81,7 @@ void launch_mass_f64(const Graph& G, const double* h, double* acc, cudaStream_t 
 void launch_stage_mix(const StageArgsMix& a, cudaStream_t s, const KernelEvents* kev = nullptr);
 void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, unsigned* err, int block,
                    cudaStream_t s);
+void launch_refresh_z(const Graph& G, StateMix u, cudaStream_t s);
 
 // kernels launched per stage / per step (for launch accounting)
 constexpr int kLaunchesPerStage = 4;

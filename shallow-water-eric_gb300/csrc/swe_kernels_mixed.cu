@@ -8,8 +8,11 @@
 //   * the low-order depth h^L = h (1 + dt fix/m) + dt rk_1/m,
 //   * the limiter's Q^-, P^-, R^- and the h-row sum  sum_j l_ij f_ij,
 //   * the new depth h = h^L + dt/m sum_j l_ij f_ij and its RK combination.
-// FP64 throughput on GB300 is ~1/70 of FP32, so FP64 is never used per edge
-// except for the P^- and l_ij f_ij accumulations.
+// FP64 throughput on GB300 is ~1/70 of FP32, so FP64 is used per edge only in
+// the P^- and l_ij f_ij accumulations.
+//
+// Node data that neighbours gather is packed per node as float4
+// {h shadow, qx, qy, z}: one 16-byte load (one L2 sector) per neighbour.
 #include "swe_kernels.hpp"
 
 namespace swe {
@@ -17,10 +20,15 @@ namespace swe {
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
 
 // c . v with an explicit rounding sequence.  The low-order mass flux
-// (-c.v_j + mu_ij) h_j is non-negative only if mu_ij >= c.v_j holds bit for
-// bit; FMA contraction chosen independently at two sites would break that.
+// (mu_ij - c.v_j) h_j is non-negative only if mu_ij >= c.v_j holds bit for
+// bit, so c.v_j is formed once per entry with a fixed rounding.
 __device__ __forceinline__ float dotc(float cx, float cy, float vx, float vy) {
   return __fmaf_rn(cx, vx, __fmul_rn(cy, vy));
+}
+
+__device__ __forceinline__ float ovh_f(float h, float htiny) {
+  float mh = fmaxf(h, htiny);
+  return fdiv(2.0f * h, __fmaf_rn(h, h, __fmul_rn(mh, mh)));
 }
 
 // Hydrostatic reconstruction H*_ij = max(0, h_i + z_i - max(z_i, z_j))
@@ -36,13 +44,18 @@ __device__ __forceinline__ Recon recon(float hi, float hj, float dz, float invhi
   Recon R;
   R.Hij = (dz <= 0.f) ? hi : fmaxf(0.f, hi - dz);
   R.Hji = (dz >= 0.f) ? hj : fmaxf(0.f, hj + dz);
-  R.rij = (hi > 0.f) ? ((dz <= 0.f) ? 1.f : fminf(R.Hij * invhi, 1.f)) : 0.f;
-  R.rji = (hj > 0.f) ? ((dz >= 0.f) ? 1.f : fminf(R.Hji * invhj, 1.f)) : 0.f;
+  R.rij = (hi > 0.f) ? ((dz <= 0.f) ? 1.f : fminf(__fmul_rn(R.Hij, invhi), 1.f)) : 0.f;
+  R.rji = (hj > 0.f) ? ((dz >= 0.f) ? 1.f : fminf(__fmul_rn(R.Hji, invhj), 1.f)) : 0.f;
   return R;
 }
-__device__ __forceinline__ float ovh_f(float h, float htiny) {
-  float mh = fmaxf(h, htiny);
-  return fdiv(2.0f * h, h * h + mh * mh);
+__device__ __forceinline__ float inv_pos(float h) { return (h > 0.f) ? fdiv(1.0f, h) : 0.f; }
+
+// antidiffusive h-flux f_ij of compute_fct_matrix (update.f90:744-745) with
+// explicit roundings: k_fct (P^-) and k_update (sum l f) must see the same f.
+__device__ __forceinline__ float fct_from(float dd, float dm, float hi, float hj, const Recon& R) {
+  const float a = __fsub_rn(__fmul_rn(hj, R.rji), __fmul_rn(hi, R.rij));
+  const float b = __fsub_rn(__fmul_rn(hj, __fsub_rn(1.f, R.rji)), __fmul_rn(hi, __fsub_rn(1.f, R.rij)));
+  return __fadd_rn(__fmul_rn(dd, a), __fmul_rn(dm, b));
 }
 
 // k_node_mix: alpha_i (SOURCES/update.f90:758-781) from the FP32 depth.
@@ -55,13 +68,14 @@ __global__ void k_node_mix(Graph G, const InstConst* __restrict__ C, const InstS
   const int b = G.slice_inst[r >> 5];
   if (St[b].done) return;
   const InstConst& c = C[b];
-  const float h = u.hf[r];
+  const float* hs = reinterpret_cast<const float*>(u.nq);
+  const float h = hs[4 * r];
   float alpha = 1.0f;
   if (c.alpha_limit && !(h <= (float)c.htiny)) {
     const int64_t base = entry_base(G, r);
     float num = 0.0f, denom = 0.0f;
     for (int k = 0; k < L; k++) {
-      const float hj = u.hf[G.col[base + 32 * k]];
+      const float hj = hs[4 * (int64_t)G.col[base + 32 * k]];
       num += hj - h;
       denom += fabsf(hj - h);
     }
@@ -76,13 +90,20 @@ struct NodeF {   // FP32 view of one node used by the edge loop
   float h, q1, q2, z, ovh, v1, v2;
 };
 
-__device__ __forceinline__ NodeF load_node(const Graph& G, const StateMix& u, int64_t j, float htiny) {
+__device__ __forceinline__ NodeF load_node(const StateMix& u, int64_t j, float htiny) {
+  const float4 a = u.nq[j];
   NodeF n;
-  n.h = u.hf[j]; n.q1 = u.q1[j]; n.q2 = u.q2[j]; n.z = G.bathf[j];
+  n.h = a.x; n.q1 = a.y; n.q2 = a.z; n.z = a.w;
   n.ovh = ovh_f(n.h, htiny);
   n.v1 = n.q1 * n.ovh;
   n.v2 = n.q2 * n.ovh;
   return n;
+}
+
+__device__ __forceinline__ float sgn_pressure(float lambda_sgn, float g, float m, float h, float heta) {
+  const float pc = fdiv(lambda_sgn * g, 3.0f * sqrtf(m));
+  const float x = fdiv(heta, h * h);
+  return pc * h * h * h * (2.f + 4.f * x * x * x - 6.f * x * x * x * x);   // mSGN_RHS pTilde (update.f90:522)
 }
 
 // k_low_mix: one pass over the row's entries computing d_ij (lambda_max),
@@ -90,14 +111,13 @@ __device__ __forceinline__ NodeF load_node(const Graph& G, const StateMix& u, in
 // Galerkin RHS (smb_2) and the entropy stencil max/min, then the low-order
 // state and the entropy residual (SOURCES/update.f90:180-210, 291-364,
 // 554-682, 750-799, 825-878).  Each neighbour is loaded once, and c.v_j is
-// formed once and shared by mu_ij and the Galerkin flux, so the low-order
-// mass flux (mu_ij - c.v_j) h_j stays non-negative bit for bit.  The
-// diagonal entry only enters through terms that vanish identically
-// (u_i rat_ii - u_i rat_ii), so the diagonal's d, mu are written but not used.
+// formed once and shared by mu_ij and the Galerkin flux.  The diagonal entry
+// only enters through terms that vanish identically (u_i rat_ii - u_i rat_ii)
+// and the Galerkin boundary term -c_ii.v_i.
 __global__ void __launch_bounds__(128) k_low_mix(Graph G, const InstConst* __restrict__ C,
                                                  const InstState* __restrict__ St, StateMix u,
                                                  const float* __restrict__ alpha, float* __restrict__ dL,
-                                                 float* __restrict__ muL, StateMix uL, float* __restrict__ res,
+                                                 float* __restrict__ muL, WorkMix w, float* __restrict__ res,
                                                  unsigned* __restrict__ err) {
   int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= G.n_rows) return;
@@ -113,45 +133,42 @@ __global__ void __launch_bounds__(128) k_low_mix(Graph G, const InstConst* __res
   const float sqrt2 = 1.41421356237309515f;
   const int64_t base = entry_base(G, r);
   const int dp = G.dpos[r];
-  const NodeF ni = load_node(G, u, r, htiny);
+  const NodeF ni = load_node(u, r, htiny);
   const float v2i_flux = sgn ? 0.f : ni.v2;          // flux() zeroes velocity(2) for type 13
   const float ai = alpha[r];
   const float m = (float)G.lumped[r];
   float ui3 = 0.f, ui4 = 0.f;
   if (S == 5) { ui3 = u.q3[r]; ui4 = u.q4[r]; }
-  const float invhi = (ni.h > 0.f) ? fdiv(1.0f, ni.h) : 0.f;
+  const float invhi = inv_pos(ni.h);
   bool delta_bad = false;
 
   float sd = 0.f, sm_raw = 0.f, sm = 0.f;
-  float fix = 0.f, rk0 = 0.f, rk[5] = {0, 0, 0, 0, 0}, rk2[5] = {0, 0, 0, 0, 0};
+  float fix = 0.f, rk0 = 0.f;
+  float rk1 = 0.f, rk2_ = 0.f, rk3 = 0.f, rk4 = 0.f;               // smb_2_roundoff momenta
+  float g0 = 0.f, g1 = 0.f, g2 = 0.f, g3 = 0.f, g4 = 0.f;          // smb_2
   const float Ei = 0.5f * (g * ni.h * ni.h + ni.v1 * ni.q1 + v2i_flux * ni.q2);
   float emax = Ei, emin = Ei;
   float ptx = 0.f, pty = 0.f;
-  const float ivi_x = ni.v1, ivi_y = ni.v2;
   for (int k = 0; k < L; k++) {
     const int64_t e = base + 32 * k;
     const float cxe = G.cxf[e], cye = G.cyf[e];
     if (k == dp) {
-      // diagonal: Galerkin boundary term -c_ii.v_i (fix_roundoff / smb_2), no viscosity
+      // diagonal: Galerkin boundary term -c_ii.v_i (fix_roundoff / smb_2)
       const float cvi = dotc(cxe, cye, ni.v1, v2i_flux);
-      fix += -cvi;
-      rk2[0] += -cvi * ni.h;
-      rk[1] += -cvi * ni.q1; rk[2] += -cvi * ni.q2;
-      rk2[1] += -cvi * ni.q1; rk2[2] += -cvi * ni.q2;
-      if (S == 5) { rk[3] += -cvi * ui3; rk[4] += -cvi * ui4; rk2[3] += -cvi * ui3; rk2[4] += -cvi * ui4; }
+      fix -= cvi;
+      g0 -= cvi * ni.h;
+      rk1 -= cvi * ni.q1; rk2_ -= cvi * ni.q2;
+      g1 -= cvi * ni.q1; g2 -= cvi * ni.q2;
+      if (S == 5) { rk3 -= cvi * ui3; rk4 -= cvi * ui4; g3 -= cvi * ui3; g4 -= cvi * ui4; }
       if (sgn) {
-        const float pc = fdiv((float)c.lambda_sgn * g, 3.0f * sqrtf(m));
-        const float x = fdiv(ui3, ni.h * ni.h);
-        const float pt = pc * ni.h * ni.h * ni.h * (2.f + 4.f * x * x * x - 6.f * x * x * x * x);
+        const float pt = sgn_pressure((float)c.lambda_sgn, g, m, ni.h, ui3);
         ptx -= pt * cxe;
         pty -= pt * cye;
       }
       continue;
     }
     const int j = G.col[e];
-    const NodeF nj = load_node(G, u, j, htiny);
-    float uj3 = 0.f, uj4 = 0.f;
-    if (S == 5) { uj3 = u.q3[j]; uj4 = u.q4[j]; }
+    const NodeF nj = load_node(u, j, htiny);
     // --- viscosities: compute_dij, compute_muij, MAX, alpha_limit
     const float norm = sqrtf(cxe * cxe + cye * cye);
     const float inv = fdiv(1.0f, norm);
@@ -160,7 +177,7 @@ __global__ void __launch_bounds__(128) k_low_mix(Graph G, const InstConst* __res
                             sqrt2, &lam))
       delta_bad = true;
     const float cvj = dotc(cxe, cye, nj.v1, nj.v2);                   // c.v_j (compute_muij)
-    float mu = fmaxf(fmaxf(-dotc(cxe, cye, ivi_x, ivi_y), 0.f), fmaxf(cvj, 0.f));
+    float mu = fmaxf(fmaxf(-dotc(cxe, cye, ni.v1, ni.v2), 0.f), fmaxf(cvj, 0.f));
     sm_raw += mu;
     float d = fmaxf(norm * lam, mu);
     if (c.alpha_limit) {
@@ -179,106 +196,91 @@ __global__ void __launch_bounds__(128) k_low_mix(Graph G, const InstConst* __res
     emin = fminf(emin, Ej);
     // --- hydrostatic reconstruction
     const float dz = nj.z - ni.z;
-    const float invhj = (nj.h > 0.f) ? fdiv(1.0f, nj.h) : 0.f;
-    const Recon R = recon(ni.h, nj.h, dz, invhi, invhj);
+    const Recon R = recon(ni.h, nj.h, dz, invhi, inv_pos(nj.h));
     const float rij = R.rij, rji = R.rji;                             // h <= 0 tests (smb_2)
     const float rijt = (ni.h <= htiny) ? 0.f : rij;                   // h <= htiny tests
     const float rjit = (nj.h <= htiny) ? 0.f : rji;
-    const float cvj_flux = sgn ? dotc(cxe, cye, nj.v1, 0.f) : cvj;   // -c.velocity_j of flux()
+    const float cvj_flux = sgn ? dotc(cxe, cye, nj.v1, 0.f) : cvj;   // c.velocity_j of flux()
     const float topo = g * ni.h * ((nj.h - ni.h) + dz);               // g h_i (eta_j - eta_i)
     // --- smb_2_roundoff mass row (fix_roundoff, rk_1)
     fix += -mu - (d - mu) * rijt;
     rk0 += (mu - cvj_flux) * nj.h + fmaxf((d - mu) * R.Hji, 0.f);
     // --- smb_2 mass row
-    rk2[0] += -cvj_flux * nj.h + d * (nj.h * rji - ni.h * rij) + mu * (nj.h * (1.f - rji) - ni.h * (1.f - rij));
-    const float uq_i[5] = {ni.h, ni.q1, ni.q2, ui3, ui4};
-    const float uq_j[5] = {nj.h, nj.q1, nj.q2, uj3, uj4};
-#pragma unroll
-    for (int q = 1; q < 5; q++) {
-      if (q >= S) break;
-      const float gal = -cvj_flux * uq_j[q];
-      rk[q] += gal + d * (uq_j[q] * rjit - uq_i[q] * rijt) + mu * (uq_j[q] * (1.f - rjit) - uq_i[q] * (1.f - rijt));
-      rk2[q] += gal + d * (uq_j[q] * rji - uq_i[q] * rij) + mu * (uq_j[q] * (1.f - rji) - uq_i[q] * (1.f - rij));
-    }
-    rk[1] -= topo * cxe;  rk[2] -= topo * cye;
-    rk2[1] -= topo * cxe; rk2[2] -= topo * cye;
-    if (sgn) {
-      const float mj = (float)G.lumped[j];
-      const float pc = fdiv((float)c.lambda_sgn * g, 3.0f * sqrtf(mj));
-      const float x = fdiv(uj3, nj.h * nj.h);
-      const float pt = pc * nj.h * nj.h * nj.h * (2.f + 4.f * x * x * x - 6.f * x * x * x * x);
-      ptx -= pt * cxe;
-      pty -= pt * cye;
+    g0 += -cvj_flux * nj.h + d * (nj.h * rji - ni.h * rij) + mu * (nj.h * (1.f - rji) - ni.h * (1.f - rij));
+    // --- momenta (both RHS) and topography
+    rk1 += -cvj_flux * nj.q1 + d * (nj.q1 * rjit - ni.q1 * rijt) + mu * (nj.q1 * (1.f - rjit) - ni.q1 * (1.f - rijt));
+    rk2_ += -cvj_flux * nj.q2 + d * (nj.q2 * rjit - ni.q2 * rijt) + mu * (nj.q2 * (1.f - rjit) - ni.q2 * (1.f - rijt));
+    g1 += -cvj_flux * nj.q1 + d * (nj.q1 * rji - ni.q1 * rij) + mu * (nj.q1 * (1.f - rji) - ni.q1 * (1.f - rij));
+    g2 += -cvj_flux * nj.q2 + d * (nj.q2 * rji - ni.q2 * rij) + mu * (nj.q2 * (1.f - rji) - ni.q2 * (1.f - rij));
+    rk1 -= topo * cxe; rk2_ -= topo * cye;
+    g1 -= topo * cxe; g2 -= topo * cye;
+    if (S == 5) {
+      const float uj3 = u.q3[j], uj4 = u.q4[j];
+      rk3 += -cvj_flux * uj3 + d * (uj3 * rjit - ui3 * rijt) + mu * (uj3 * (1.f - rjit) - ui3 * (1.f - rijt));
+      rk4 += -cvj_flux * uj4 + d * (uj4 * rjit - ui4 * rijt) + mu * (uj4 * (1.f - rjit) - ui4 * (1.f - rijt));
+      g3 += -cvj_flux * uj3 + d * (uj3 * rji - ui3 * rij) + mu * (uj3 * (1.f - rji) - ui3 * (1.f - rij));
+      g4 += -cvj_flux * uj4 + d * (uj4 * rji - ui4 * rij) + mu * (uj4 * (1.f - rji) - ui4 * (1.f - rij));
+      if (sgn) {
+        const float pt = sgn_pressure((float)c.lambda_sgn, g, (float)G.lumped[j], nj.h, uj3);
+        ptx -= pt * cxe;
+        pty -= pt * cye;
+      }
     }
   }
   // diagonals (-row sums, with the reference's mu re-summation under alpha)
   dL[base + 32 * dp] = -sd;
   muL[base + 32 * dp] = c.alpha_limit ? -(sm - sm_raw) : -sm_raw;
-  // source terms
+  // source terms (update.f90:425-551)
   if (c.type_test == 9 || c.type_test == 10) {
     const float fric = (float)(c.g * c.mannings * c.mannings);
     const float hstar = __powf(fmaxf(ni.h, htiny), 4.0f / 3.0f);
     const float vel = fric * sqrtf(ni.v1 * ni.v1 + ni.v2 * ni.v2);
     const float hloc = vel * dtf;
     const float coef = fdiv(m * vel * 2.f, hstar + fmaxf(hstar, hloc));
-    rk[1] -= coef * ni.q1; rk[2] -= coef * ni.q2;
-    rk2[1] -= coef * ni.q1; rk2[2] -= coef * ni.q2;
+    rk1 -= coef * ni.q1; rk2_ -= coef * ni.q2;
+    g1 -= coef * ni.q1; g2 -= coef * ni.q2;
   } else if (c.type_test == 11) {
-    rk[1] -= m * 0.2f * ni.q1; rk[2] -= m * 0.2f * ni.q2;
-    rk2[1] -= m * 0.2f * ni.q1; rk2[2] -= m * 0.2f * ni.q2;
+    rk1 -= m * 0.2f * ni.q1; rk2_ -= m * 0.2f * ni.q2;
+    g1 -= m * 0.2f * ni.q1; g2 -= m * 0.2f * ni.q2;
   } else if (c.type_test == 12) {
-    const float f = 2.0f;
-    const float a1 = m * f * ni.q2, a2 = m * f * ni.q1;
-    rk[1] += a1; rk[2] -= a2; rk2[1] += a1; rk2[2] -= a2;
+    const float a1 = m * 2.0f * ni.q2, a2 = m * 2.0f * ni.q1;
+    rk1 += a1; rk2_ -= a2; g1 += a1; g2 -= a2;
   } else if (sgn) {
     const float pc = fdiv((float)c.lambda_sgn * g, 3.0f * sqrtf(m));
     const float t = fdiv(ui3, ni.h);
     const float x = fdiv(ui3, ni.h * ni.h);
     const float s_i = 3.f * pc * t * t * 12.f * (x - 1.f);
-    rk[1] += ptx; rk[2] += pty; rk2[1] += ptx; rk2[2] += pty;
-    rk[3] += m * ui4; rk[4] -= m * s_i;
-    rk2[3] += m * ui4; rk2[4] -= m * s_i;
+    rk1 += ptx; rk2_ += pty; g1 += ptx; g2 += pty;
+    rk3 += m * ui4; rk4 -= m * s_i;
+    g3 += m * ui4; g4 -= m * s_i;
   }
   // low-order state: FP64 depth update, FP32 momenta
   const double inv_m = G.inv_lumped[r];
   const double dtd = st.dt;
   double hL;
   if (c.roundoff_fix) hL = u.h[r] * (1.0 + dtd * (double)fix * inv_m) + dtd * (double)rk0 * inv_m;
-  else hL = fmax(u.h[r] + dtd * (double)rk2[0] * inv_m, 0.0);
+  else hL = fmax(u.h[r] + dtd * (double)g0 * inv_m, 0.0);
   const float invm = (float)inv_m;
-  uL.h[r] = hL;
-  uL.q1[r] = ni.q1 + dtf * (rk[1] * invm);
-  uL.q2[r] = ni.q2 + dtf * (rk[2] * invm);
-  if (S == 5) { uL.q3[r] = ui3 + dtf * (rk[3] * invm); uL.q4[r] = ui4 + dtf * (rk[4] * invm); }
-  // entropy residual
-  float un_[3];
-  const float uq_i[3] = {ni.h, ni.q1, ni.q2};
-  for (int q = 0; q < 3; q++) un_[q] = uq_i[q] + dtf * (rk2[q] * invm);
-  const float on = ovh_f(un_[0], htiny);
-  const float En = 0.5f * (g * un_[0] * un_[0] + (un_[1] * on) * un_[1] + (un_[2] * on) * un_[2]);
+  w.hL[r] = hL;
+  w.qL[r] = make_float2(ni.q1 + dtf * (rk1 * invm), ni.q2 + dtf * (rk2_ * invm));
+  if (S == 5) { w.q3L[r] = ui3 + dtf * (rk3 * invm); w.q4L[r] = ui4 + dtf * (rk4 * invm); }
+  // entropy residual (update.f90:838-868), rescale once per node
+  const float un0 = ni.h + dtf * (g0 * invm);
+  const float un1 = ni.q1 + dtf * (g1 * invm);
+  const float un2 = ni.q2 + dtf * (g2 * invm);
+  const float on = ovh_f(un0, htiny);
+  const float En = 0.5f * (g * un0 * un0 + (un1 * on) * un1 + (un2 * on) * un2);
   const float Ep0 = g * ni.h - 0.5f * (ni.v1 * ni.v1) - 0.5f * (v2i_flux * v2i_flux);
   float rs = m * fdiv(En - Ei, dtf);
-  rs -= rk2[0] * Ep0 + rk2[1] * ni.v1 + rk2[2] * v2i_flux;
+  rs -= g0 * Ep0 + g1 * ni.v1 + g2 * v2i_flux;
   const float rescale = 0.5f * fabsf(emax - emin) + (float)c.rescale_floor;
   res[r] = fdiv(fabsf(rs), rescale);
   if (delta_bad) atomicOr(err, ERRB_DELTA);
 }
 
-// antidiffusive h-flux f_ij of compute_fct_matrix (update.f90:744-745)
-__device__ __forceinline__ float fct_flux(float d0, float m0, float rij, float hi, float zi, float hj, float zj) {
-  const float dd = fminf(d0, rij) - d0, dm = fminf(m0, rij) - m0;
-  const float invhi = (hi > 0.f) ? fdiv(1.0f, hi) : 0.f;
-  const float invhj = (hj > 0.f) ? fdiv(1.0f, hj) : 0.f;
-  const Recon R = recon(hi, hj, zj - zi, invhi, invhj);
-  // explicit roundings: k_fct (P^-) and k_update (sum l f) must see the same f
-  const float a = __fsub_rn(__fmul_rn(hj, R.rji), __fmul_rn(hi, R.rij));
-  const float b = __fsub_rn(__fmul_rn(hj, __fsub_rn(1.f, R.rji)), __fmul_rn(hi, __fsub_rn(1.f, R.rij)));
-  return __fadd_rn(__fmul_rn(dd, a), __fmul_rn(dm, b));
-}
-
 // k_fct_mix: f_ij (FP32) and R^-_i (FP64 Q^-, P^-, R^-), fct.f90:15-30
 __global__ void k_fct_mix(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St, StateMix u,
-                          const float* __restrict__ dL, const float* __restrict__ muL, StateMix uL,
+                          const float* __restrict__ dL, const float* __restrict__ muL, WorkMix w,
                           const float* __restrict__ res, double* __restrict__ rminus, unsigned* __restrict__ err) {
   int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= G.n_rows) return;
@@ -289,15 +291,22 @@ __global__ void k_fct_mix(Graph G, const InstConst* __restrict__ C, const InstSt
   if (st.done) return;
   const InstConst& c = C[b];
   const int64_t base = entry_base(G, r);
-  const float hi = u.hf[r], zi = G.bathf[r], resi = res[r];
+  const int dp = G.dpos[r];
+  const float4 ni = u.nq[r];
+  const float hi = ni.x, zi = ni.w, resi = res[r];
+  const float invhi = inv_pos(hi);
   double P = -1.e-15;
   for (int k = 0; k < L; k++) {
+    if (k == dp) continue;   // f_ii = 0
     const int64_t e = base + 32 * k;
     const int j = G.col[e];
-    const float f = fct_flux(dL[e], muL[e], fmaxf(resi, res[j]), hi, zi, u.hf[j], G.bathf[j]);
+    const float4 nj = u.nq[j];
+    const float d0 = dL[e], m0 = muL[e], rij = fmaxf(resi, res[j]);
+    const Recon R = recon(hi, nj.x, nj.w - zi, invhi, inv_pos(nj.x));
+    const float f = fct_from(fminf(d0, rij) - d0, fminf(m0, rij) - m0, hi, nj.x, R);
     if (f < 0.f) P += (double)f;
   }
-  const double hL = uL.h[r];
+  const double hL = w.hL[r];
   if (hL < 0.0) atomicOr(err, ERRB_NEG_H);
   const double scaled = G.lumped[r] * st.inv_dt * hL;
   // Q^-/P^- with Q^- shrunk by 4 ulp: the update multiplies by dt/m through
@@ -310,7 +319,7 @@ __global__ void k_fct_mix(Graph G, const InstConst* __restrict__ C, const InstSt
 // k_update_mix: limited antidiffusion (update.f90:276-282, apply_viscosity
 // :684-718), RK combination and Dirichlet data (main.f90:77-90).
 __global__ void k_update_mix(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St,
-                             StateMix u, const float* __restrict__ dL, const float* __restrict__ muL, StateMix uL,
+                             StateMix u, const float* __restrict__ dL, const float* __restrict__ muL, WorkMix w,
                              const float* __restrict__ res, const double* __restrict__ rminus, StateMix u0,
                              StateMix out, int rk_stage, unsigned* __restrict__ err) {
   int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -323,64 +332,75 @@ __global__ void k_update_mix(Graph G, const InstConst* __restrict__ C, const Ins
   const InstConst& c = C[b];
   const int S = c.S;
   const int64_t base = entry_base(G, r);
-  const float hi = u.hf[r], zi = G.bathf[r], resi = res[r];
+  const int dp = G.dpos[r];
+  const float4 ni = u.nq[r];
+  const float hi = ni.x, zi = ni.w, resi = res[r];
+  const float invhi = inv_pos(hi);
   const double Ri = rminus[r];
-  float ui[5] = {hi, u.q1[r], u.q2[r], 0.f, 0.f};
-  if (S == 5) { ui[3] = u.q3[r]; ui[4] = u.q4[r]; }
+  float ui3 = 0.f, ui4 = 0.f;
+  if (S == 5) { ui3 = u.q3[r]; ui4 = u.q4[r]; }
   double sh = 0.0;                       // sum_j l_ij f_ij (FP64)
-  float xx[5] = {0, 0, 0, 0, 0};
+  float x1 = 0.f, x2 = 0.f, x3 = 0.f, x4 = 0.f;
   for (int k = 0; k < L; k++) {
+    if (k == dp) continue;               // (u_i rat_ii - u_i rat_ii) = 0
     const int64_t e = base + 32 * k;
     const int j = G.col[e];
+    const float4 nj = u.nq[j];
     const float d0 = dL[e], m0 = muL[e];
     const float rij = fmaxf(resi, res[j]);
-    const float hj = u.hf[j], zj = G.bathf[j];
-    const float f = fct_flux(d0, m0, rij, hi, zi, hj, zj);
+    const float ddr = fminf(d0, rij) - d0, dmr = fminf(m0, rij) - m0;
+    const Recon R = recon(hi, nj.x, nj.w - zi, invhi, inv_pos(nj.x));
+    const float f = fct_from(ddr, dmr, hi, nj.x, R);
     const double l = (f >= 0.f) ? rminus[j] : Ri;
     sh += l * (double)f;
     const float lf = (float)l;
-    const float dd = (fminf(d0, rij) - d0) * lf, dm = (fminf(m0, rij) - m0) * lf;
-    const float invhi = (hi > 0.f) ? fdiv(1.0f, hi) : 0.f;
-    const float invhj = (hj > 0.f) ? fdiv(1.0f, hj) : 0.f;
-    const Recon R = recon(hi, hj, zj - zi, invhi, invhj);
-    const float ratij = R.rij, ratji = R.rji;
-    float uj[5] = {hj, u.q1[j], u.q2[j], 0.f, 0.f};
-    if (S == 5) { uj[3] = u.q3[j]; uj[4] = u.q4[j]; }
-#pragma unroll
-    for (int q = 1; q < 5; q++) {
-      if (q >= S) break;
-      xx[q] += dd * (uj[q] * ratji - ui[q] * ratij) + dm * (uj[q] * (1.f - ratji) - ui[q] * (1.f - ratij));
+    const float dd = ddr * lf, dm = dmr * lf;
+    x1 += dd * (nj.y * R.rji - ni.y * R.rij) + dm * (nj.y * (1.f - R.rji) - ni.y * (1.f - R.rij));
+    x2 += dd * (nj.z * R.rji - ni.z * R.rij) + dm * (nj.z * (1.f - R.rji) - ni.z * (1.f - R.rij));
+    if (S == 5) {
+      const float uj3 = u.q3[j], uj4 = u.q4[j];
+      x3 += dd * (uj3 * R.rji - ui3 * R.rij) + dm * (uj3 * (1.f - R.rji) - ui3 * (1.f - R.rij));
+      x4 += dd * (uj4 * R.rji - ui4 * R.rij) + dm * (uj4 * (1.f - R.rji) - ui4 * (1.f - R.rij));
     }
   }
   const double inv_m = G.inv_lumped[r];
   const float invm = (float)inv_m, dtf = (float)st.dt;
-  double hn = uL.h[r] + st.dt * (sh * inv_m);
-  float qn[5];
-  const float* ulq[5] = {nullptr, uL.q1, uL.q2, uL.q3, uL.q4};
-  for (int q = 1; q < S; q++) qn[q] = ulq[q][r] + dtf * (xx[q] * invm);
+  double hn = w.hL[r] + st.dt * (sh * inv_m);
+  const float2 qL = w.qL[r];
+  float q1 = qL.x + dtf * (x1 * invm);
+  float q2 = qL.y + dtf * (x2 * invm);
+  float q3 = 0.f, q4 = 0.f;
+  if (S == 5) { q3 = w.q3L[r] + dtf * (x3 * invm); q4 = w.q4L[r] + dtf * (x4 * invm); }
   if (hn < 0.0) atomicOr(err, ERRB_NEG_H);
-  if (!(hn == hn) || !(qn[1] == qn[1]) || !(qn[2] == qn[2])) atomicOr(err, ERRB_NAN);
+  if (!(hn == hn) || !(q1 == q1) || !(q2 == q2)) atomicOr(err, ERRB_NAN);
   if (rk_stage >= 2) {
-    const float* u0q[5] = {nullptr, u0.q1, u0.q2, u0.q3, u0.q4};
+    const float4 a0 = u0.nq[r];
+    const double h0 = u0.h[r];
     if (rk_stage == 2) {
-      hn = (3.0 * u0.h[r] + hn) * 0.25;
-      for (int q = 1; q < S; q++) qn[q] = (3.f * u0q[q][r] + qn[q]) * 0.25f;
+      hn = (3.0 * h0 + hn) * 0.25;
+      q1 = (3.f * a0.y + q1) * 0.25f;
+      q2 = (3.f * a0.z + q2) * 0.25f;
+      if (S == 5) { q3 = (3.f * u0.q3[r] + q3) * 0.25f; q4 = (3.f * u0.q4[r] + q4) * 0.25f; }
     } else {
-      hn = (u0.h[r] + 2.0 * hn) * (1.0 / 3.0);
-      for (int q = 1; q < S; q++) qn[q] = (u0q[q][r] + 2.f * qn[q]) * (1.f / 3.f);
+      hn = (h0 + 2.0 * hn) * (1.0 / 3.0);
+      q1 = (a0.y + 2.f * q1) * (1.f / 3.f);
+      q2 = (a0.z + 2.f * q2) * (1.f / 3.f);
+      if (S == 5) { q3 = (u0.q3[r] + 2.f * q3) * (1.f / 3.f); q4 = (u0.q4[r] + 2.f * q4) * (1.f / 3.f); }
     }
   }
   if (rk_stage >= 1 && G.dir_mask) {
     const unsigned msk = G.dir_mask[r];
-    if (msk & 1u) hn = G.dir_val[r];
-    for (int q = 1; q < S; q++)
-      if (msk & (1u << q)) qn[q] = (float)G.dir_val[(int64_t)q * G.n_rows + r];
+    if (msk) {
+      if (msk & 1u) hn = G.dir_val[r];
+      if (msk & 2u) q1 = (float)G.dir_val[G.n_rows + r];
+      if (msk & 4u) q2 = (float)G.dir_val[2 * G.n_rows + r];
+      if (S == 5 && (msk & 8u)) q3 = (float)G.dir_val[3 * G.n_rows + r];
+      if (S == 5 && (msk & 16u)) q4 = (float)G.dir_val[4 * G.n_rows + r];
+    }
   }
   out.h[r] = hn;
-  out.hf[r] = shadow_depth(hn, c.htiny);
-  out.q1[r] = qn[1];
-  out.q2[r] = qn[2];
-  if (S == 5) { out.q3[r] = qn[3]; out.q4[r] = qn[4]; }
+  out.nq[r] = make_float4(shadow_depth(hn, c.htiny), q1, q2, zi);
+  if (S == 5) { out.q3[r] = q3; out.q4[r] = q4; }
 }
 
 // k_dt_mix: FP32 lambda_max, max |d_ii|/m_i per instance (main.f90:166-174)
@@ -395,20 +415,19 @@ __global__ void k_dt_mix(Graph G, const InstConst* __restrict__ C, InstState* __
       const float g = (float)c.g, htiny = (float)c.htiny;
       const int L = G.len[r], dp = G.dpos[r];
       const int64_t base = entry_base(G, r);
-      const float hi = u.hf[r], q1 = u.q1[r], q2 = u.q2[r];
-      const float oi = ovh_f(hi, htiny);
+      const float4 ni = u.nq[r];
+      const float oi = ovh_f(ni.x, htiny);
       float s = 0.f;
       bool bad = false;
       for (int k = 0; k < L; k++) {
         if (k == dp) continue;
         const int64_t e = base + 32 * k;
-        const int j = G.col[e];
+        const float4 nj = u.nq[G.col[e]];
         const float cxe = G.cxf[e], cye = G.cyf[e];
         const float norm = sqrtf(cxe * cxe + cye * cye);
         const float inv = fdiv(1.0f, norm);
-        const float hj = u.hf[j];
         float lam;
-        if (!lambda_vacc<float>(hi, q1, q2, oi, hj, u.q1[j], u.q2[j], ovh_f(hj, htiny), cxe * inv, cye * inv, g,
+        if (!lambda_vacc<float>(ni.x, ni.y, ni.z, oi, nj.x, nj.y, nj.z, ovh_f(nj.x, htiny), cxe * inv, cye * inv, g,
                                 htiny, 1.41421356237309515f, &lam))
           bad = true;
         s += norm * lam;
@@ -426,6 +445,13 @@ __global__ void k_dt_mix(Graph G, const InstConst* __restrict__ C, InstState* __
   }
 }
 
+// Copy the bathymetry into the packed node records after a bathymetry change
+__global__ void k_refresh_z(Graph G, StateMix u) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= G.n_rows) return;
+  u.nq[r].w = G.bathf[r];
+}
+
 static inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 #define EV_BEGIN(k) if (kev) cudaEventRecord(kev->ev[2 * (k)], s)
@@ -437,12 +463,12 @@ void launch_stage_mix(const StageArgsMix& a, cudaStream_t s, const KernelEvents*
   EV_BEGIN(1);
   k_node_mix<<<nb, bs, 0, s>>>(a.G, a.C, a.St, a.u, a.w.alpha);
   EV_END(1); EV_BEGIN(2);
-  k_low_mix<<<nblk(a.G.n_rows, 128), 128, 0, s>>>(a.G, a.C, a.St, a.u, a.w.alpha, a.w.dL, a.w.muL, a.w.uL, a.w.res,
+  k_low_mix<<<nblk(a.G.n_rows, 128), 128, 0, s>>>(a.G, a.C, a.St, a.u, a.w.alpha, a.w.dL, a.w.muL, a.w, a.w.res,
                                                    a.err);
   EV_END(2); EV_BEGIN(3);
-  k_fct_mix<<<nb, bs, 0, s>>>(a.G, a.C, a.St, a.u, a.w.dL, a.w.muL, a.w.uL, a.w.res, a.w.rminus, a.err);
+  k_fct_mix<<<nb, bs, 0, s>>>(a.G, a.C, a.St, a.u, a.w.dL, a.w.muL, a.w, a.w.res, a.w.rminus, a.err);
   EV_END(3); EV_BEGIN(4);
-  k_update_mix<<<nb, bs, 0, s>>>(a.G, a.C, a.St, a.u, a.w.dL, a.w.muL, a.w.uL, a.w.res, a.w.rminus, a.u0, a.out,
+  k_update_mix<<<nb, bs, 0, s>>>(a.G, a.C, a.St, a.u, a.w.dL, a.w.muL, a.w, a.w.res, a.w.rminus, a.u0, a.out,
                                  a.rk_stage, a.err);
   EV_END(4);
 }
@@ -450,6 +476,10 @@ void launch_stage_mix(const StageArgsMix& a, cudaStream_t s, const KernelEvents*
 void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, unsigned* err, int block,
                    cudaStream_t s) {
   k_dt_mix<<<nblk(G.n_rows, block), block, 0, s>>>(G, C, St, u, err);
+}
+
+void launch_refresh_z(const Graph& G, StateMix u, cudaStream_t s) {
+  k_refresh_z<<<nblk(G.n_rows, 256), 256, 0, s>>>(G, u);
 }
 
 }  // namespace swe
