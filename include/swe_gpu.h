@@ -173,6 +173,32 @@ int swe_profile_kernels(swe_ctx* ctx, int nsteps, double* ms_out);
 /* Name of the kernel configuration chosen by the autotuner. */
 const char* swe_tuning(const swe_ctx* ctx);
 
+/* FCT_positivity for callers that cannot allocate device memory.
+ *
+ * No counterpart in the reference: its FCT_positivity (SOURCES/fct.f90:5-42)
+ * works on host arrays.  This entry point serves callers that manage device
+ * memory themselves (their own pool or arena, or a driver that forbids
+ * further cudaMalloc calls): every input and output is a device pointer the
+ * caller owns, and the only scratch (R^- per node) lives in a fixed device
+ * array compiled into the library.  Nothing is allocated or freed.
+ *   np        rows (1..SWE_NOALLOC_MAX_NODES; larger values -> SWE_ERR_ARG)
+ *   d_ia      row pointers, np+1 ints, 1-based like mass%ia
+ *   d_ja      column indices, 1-based
+ *   d_unext   (lumped/dt)*h^L per row
+ *   d_mat     f_ij per CSR entry
+ *   htiny     inputs%htiny
+ *   d_lij     l_ij per CSR entry (output)
+ *   stream    cudaStream_t to launch on (NULL = default stream); the call
+ *             synchronises that stream before returning.
+ * The scratch array (SWE_NOALLOC_MAX_NODES doubles, 8 MiB) is held by every
+ * GPU that loads the library until the process exits and is shared by all
+ * calls: calls that overlap on the GPU race, so serialise them.  The first
+ * call on a device looks up the array's address for that device (with it
+ * current); make that first call before any stream capture. */
+#define SWE_NOALLOC_MAX_NODES (1 << 20)
+int swe_fct_positivity_noalloc(int np, const int* d_ia, const int* d_ja, const double* d_unext,
+                               const double* d_mat, double htiny, double* d_lij, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

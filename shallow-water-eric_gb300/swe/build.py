@@ -28,6 +28,7 @@ UNITS = {
     "swe_kernels_f64.cu": ["-fmad=false"],
     "swe_kernels_mixed.cu": ["--use_fast_math", "-Xptxas", "-warn-spills"],
     "swe_api.cu": [],
+    "swe_noalloc.cu": ["-fmad=false"],
     "swe_setup.cpp": None,   # host C++
 }
 
