@@ -57,6 +57,10 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--profile-steps", type=int, default=3)
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--workload", choices=["wetdry", "thacker", "batch", "dam", "sgn"], default="wetdry",
+                    help="wetdry (default line) or one of the other workloads, printed as extra JSON lines")
+    ap.add_argument("--batch-count", type=int, default=512)
+    ap.add_argument("--sgn-nx", type=int, default=10001)
     return ap.parse_args()
 
 
@@ -224,6 +228,7 @@ def run_ours(args, rank, world, dist):
     u_mix = upd.download()
     mass_mix = float(upd.total_mass()[0])
     value = world * N * 3 * r["steps"] / (r["dev_ms"] / 1e3)
+    tuning = upd.tuning
     prof = upd.profile_kernels(args.profile_steps)
     stage_ms = prof["node"] + prof["low"] + prof["fct"] + prof["update"]
     step_kernel_ms = prof["dt"] + 3 * stage_ms
@@ -314,8 +319,130 @@ def run_ours(args, rank, world, dist):
         "mass_rel_drift_mixed": (mass_mix - mass0) / mass0,
         "min_h_mixed": float(u_mix[0].min()),
         "kernel_time_share_of_step": step_kernel_ms / (r["dev_ms"] / r["steps"]),
+        "tuning": tuning,
     }
     print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------- other workloads
+def _run_case(case, precision, steps=None):
+    """Advance a case on the GPU; returns (state, node-stage/s, steps run, upd)."""
+    from swe.update import from_case
+    upd = from_case(case, precision=precision)
+    upd.upload(case.u0)
+    tf = case.tfinal if steps is None else 1e30
+    upd.set_time(0.0, tf)
+    n = steps if steps is not None else 10 ** 9
+    _, _, k = upd.rk3_steps(min(n, 3))          # warm-up (graph build, autotune)
+    upd.upload(case.u0)
+    upd.set_time(0.0, tf)
+    total_ms, done = 0.0, 0
+    while done < n:
+        chunk = min(n - done, 400)
+        t, dt, k = upd.rk3_steps(chunk)
+        total_ms += upd.last_device_ms
+        done += k
+        if k < chunk:
+            break
+    N = case.mesh["rr"].shape[1]
+    return upd.download(), N * 3 * done / (total_ms / 1e3), done, upd
+
+
+def run_thacker(args):
+    """Thacker paraboloid, one period, FP64 and mixed per mesh spacing: analytic
+    L1 error of h (quadrature at Gauss points, like compute_errors), rates, and
+    the mixed-vs-FP64 difference.  film_htiny=True is the current reference
+    initial state (+htiny everywhere, condlim.f90:440); False is the revision
+    that produced the recorded runs."""
+    import oracle
+    from swe import cases as C
+    rows = []
+    for film in (True, False):
+        prev = None
+        for hsp in (0.2, 0.1, 0.05, 0.025, 0.0125):
+            mesh = C.thacker_mesh(hsp)
+            case = C.thacker_case(mesh, periods=1.0, cfl=0.3, film=film)
+            o = oracle.Oracle(mesh["jj"], mesh["rr"])
+            rj, rg = o.gauss()
+            lump = o.matrices()["lumped"]
+            out = {}
+            for prec in (0, 1):
+                u, v, n, upd = _run_case(case, prec)
+                tfin = float(upd.rk3_steps(0)[0][0])
+                upd.close()
+                ex = case.exact(1, rg, tfin)
+                err = o.norms(u[0], ex)[0] / o.norms(np.zeros(o.np), ex)[0]
+                out[prec] = (u, v, n, err)
+            u64, v64, n64, e64 = out[0]
+            umx, vmx, nmx, emx = out[1]
+            dmx = float(np.sum(lump * np.abs(umx[0] - u64[0])) / np.sum(lump * np.abs(u64[0])))
+            rate = None if prev is None else math.log(prev / e64) / math.log(2.0)
+            prev = e64
+            rows.append({"spacing": hsp, "film_htiny": film, "nodes": o.np, "steps": n64, "l1_fp64": e64,
+                         "l1_mixed": emx, "rate_fp64": rate, "mixed_vs_fp64_l1": dmx,
+                         "fp64_node_stage_per_s": v64, "mixed_node_stage_per_s": vmx})
+            log(f"thacker h={hsp} film={film}: N={o.np} L1 fp64={e64:.4e} mixed={emx:.4e} diff={dmx:.2e}")
+    print(json.dumps({"workload": "thacker_paraboloid_one_period", "rows": rows}), flush=True)
+
+
+def run_batch(args):
+    """Batched ensemble of dam breaks: one batched context (one launch per
+    kernel for all instances, per-instance dt) versus looping single-instance
+    contexts over the same meshes."""
+    from swe import cases as C
+    from swe.update import Update, from_case
+    cases = C.batch_instances(n_inst=args.batch_count, precision=1)
+    NT = sum(c.mesh["rr"].shape[1] for c in cases)
+    log(f"batch meshes ready: {len(cases)} instances, {NT} nodes")
+    items = [(c.mesh, c.bath, c.params) for c in cases]
+    upd = Update(batch=items)
+    for b, c in enumerate(cases):
+        for comp, js, vals in c.dirichlet:
+            upd.set_dirichlet(comp, js, vals, inst=b)
+    u0 = [c.u0 for c in cases]
+    upd.upload(u0); upd.set_time(0.0, 1e30); upd.rk3_steps(args.warmup)
+    upd.upload(u0); upd.set_time(0.0, 1e30)
+    upd.rk3_steps(args.steps)
+    batched_ms = upd.last_device_ms
+    vb = NT * 3 * args.steps / (batched_ms / 1e3)
+    tuning = upd.tuning
+    upd.close()
+    loop_ms = 0.0
+    for c in cases:
+        s = from_case(c, precision=1)
+        s.upload(c.u0); s.set_time(0.0, 1e30); s.rk3_steps(args.warmup)
+        s.upload(c.u0); s.set_time(0.0, 1e30)
+        s.rk3_steps(args.steps)
+        loop_ms += s.last_device_ms
+        s.close()
+    vl = NT * 3 * args.steps / (loop_ms / 1e3)
+    print(json.dumps({"workload": f"batched_dam_breaks_{len(cases)}", "nodes": NT, "steps": args.steps,
+                      "batched_node_stage_per_s": vb, "looped_single_instance_node_stage_per_s": vl,
+                      "batched_over_looped": vb / vl, "tuning": tuning}), flush=True)
+
+
+def run_single(args, which):
+    from swe import cases as C
+    if which == "dam":
+        case = C.dam_break_case(n=101, tfinal=0.2)
+        steps = None
+    else:
+        case = C.sgn_case(nx=args.sgn_nx, ny=max(3, int(round(2.0 / (100.0 / (args.sgn_nx - 1)))) + 1),
+                          nsteps=1000)
+        steps = args.steps
+    log(f"{which}: {case.mesh['rr'].shape[1]} nodes")
+    out = {"workload": case.name, "nodes": case.mesh["rr"].shape[1]}
+    res = {}
+    for prec in (0, 1):
+        u, v, n, upd = _run_case(case, prec, steps)
+        res[prec] = u
+        out[("fp64" if prec == 0 else "mixed") + "_node_stage_per_s"] = v
+        out["steps"] = n
+        lump = upd.lumped
+        upd.close()
+    out["mixed_vs_fp64_l1_h"] = float(np.sum(lump * np.abs(res[1][0] - res[0][0])) / np.sum(lump * np.abs(res[0][0])))
+    out["min_h_mixed"] = float(res[1][0].min())
+    print(json.dumps(out), flush=True)
 
 
 def main():
@@ -333,7 +460,10 @@ def main():
     else:
         torch.cuda.set_device(0)
     try:
-        run_ours(args, rank, world, dist)
+        if args.workload == "wetdry":
+            run_ours(args, rank, world, dist)
+        elif rank == 0:
+            {"thacker": run_thacker, "batch": run_batch}.get(args.workload, lambda a: run_single(a, args.workload))(args)
     finally:
         if dist:
             dist.destroy_process_group()

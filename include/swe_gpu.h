@@ -170,7 +170,12 @@ double swe_last_device_ms(const swe_ctx* ctx);
 enum { SWE_NKERNELS = 5 };
 int swe_profile_kernels(swe_ctx* ctx, int nsteps, double* ms_out);
 
-/* Name of the kernel configuration chosen by the autotuner. */
+/* Autotuner: times every block-size / entry-batch variant of the mixed
+ * kernels on the current state and keeps the fastest per kernel (all variants
+ * give the same results).  swe_rk3_steps runs it on its first call unless the
+ * environment sets SWE_AUTOTUNE=0.  swe_tuning names the chosen
+ * configuration. */
+int swe_autotune(swe_ctx* ctx);
 const char* swe_tuning(const swe_ctx* ctx);
 
 /* FCT_positivity for callers that cannot allocate device memory.

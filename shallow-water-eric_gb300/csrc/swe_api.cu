@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -65,6 +66,8 @@ struct swe_ctx {
   cudaGraphExec_t gexec = nullptr;
   int graph_steps = 0;
   int block = 128;
+  KernelTune tune;
+  bool tuned = false;
   long long last_launches = 0;
   double last_ms = 0.0;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
@@ -153,12 +156,19 @@ static int build_device(swe_ctx* c, const std::vector<std::vector<double>>& bath
   if (c->precision == SWE_PREC_FP64) {
     G.cx = upload_vec(c, L.cx, st);
     G.cy = upload_vec(c, L.cy, st);
+    G.cxii = upload_vec(c, L.cxii, st);
+    G.cyii = upload_vec(c, L.cyii, st);
   } else {
     std::vector<float> f(L.n_entries);
     for (int64_t e = 0; e < L.n_entries; e++) f[e] = (float)L.cx[e];
     G.cxf = upload_vec(c, f, st);
     for (int64_t e = 0; e < L.n_entries; e++) f[e] = (float)L.cy[e];
     G.cyf = upload_vec(c, f, st);
+    std::vector<float> fr(L.n_rows);
+    for (int64_t r = 0; r < L.n_rows; r++) fr[r] = (float)L.cxii[r];
+    G.cxiif = upload_vec(c, fr, st);
+    for (int64_t r = 0; r < L.n_rows; r++) fr[r] = (float)L.cyii[r];
+    G.cyiif = upload_vec(c, fr, st);
     std::vector<float> bf(L.n_rows);
     for (int64_t r = 0; r < L.n_rows; r++) bf[r] = (float)L.bath[r];
     G.bathf = upload_vec(c, bf, st);
@@ -198,6 +208,7 @@ static int build_device(swe_ctx* c, const std::vector<std::vector<double>>& bath
     w.ovh = c->buf.alloc<double>(n, st); w.v1 = c->buf.alloc<double>(n, st); w.v2 = c->buf.alloc<double>(n, st);
     w.ent = c->buf.alloc<double>(n, st); w.alpha = c->buf.alloc<double>(n, st);
     w.dL = c->buf.alloc<double>(ne, st); w.muL = c->buf.alloc<double>(ne, st); w.fct = c->buf.alloc<double>(ne, st);
+    w.dLii = c->buf.alloc<double>(n, st); w.muLii = c->buf.alloc<double>(n, st);
     w.res = c->buf.alloc<double>(n, st); w.rminus = c->buf.alloc<double>(n, st);
     alloc_state_f64(c, w.uL, st);
     c->d_lij = c->buf.alloc<double>(ne, st);
@@ -348,8 +359,9 @@ static void enqueue_step(swe_ctx* c, const KernelEvents* kev = nullptr, double* 
     }
   };
   if (kev) cudaEventRecord(kev->ev[0], s);
-  if (c->precision == SWE_PREC_FP64) launch_dt_f64(c->G, c->d_C, c->d_St, c->A, nullptr, c->d_err, c->block, s);
-  else launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->d_err, c->block, s);
+  if (c->precision == SWE_PREC_FP64)
+    launch_dt_f64(c->G, c->d_C, c->d_St, c->A, nullptr, nullptr, c->d_err, c->block, s);
+  else launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->d_err, c->tune, s);
   if (kev) cudaEventRecord(kev->ev[1], s);
   harvest(0, 0);
   launch_step_begin(c->d_C, c->d_St, c->n_inst, s);
@@ -363,7 +375,7 @@ static void enqueue_step(swe_ctx* c, const KernelEvents* kev = nullptr, double* 
       StageArgsMix a{c->G, c->d_C, c->d_St, c->mA, c->mA, c->mB, c->wm, stage, c->d_err, c->block};
       if (stage == 2) { a.u = c->mB; a.out = c->mC; }
       if (stage == 3) { a.u = c->mC; a.out = c->mA; }
-      launch_stage_mix(a, s, kev);
+      launch_stage_mix(a, s, kev, c->tune);
     }
     harvest(1, 4);
   }
@@ -536,17 +548,24 @@ SWE_API int swe_get_matrices(swe_ctx* c, int inst, int* ia, int* ja, double* mas
   return SWE_OK;
 }
 
-// copy a per-entry device array of one instance back into CSR order
-template <typename T>
-static int entries_to_csr(swe_ctx* c, int inst, const T* d_arr, double* out) {
+// copy a per-entry device array of one instance back into CSR order; the
+// diagonal positions come from a per-row device array (or are 0 if null)
+template <typename T, typename U = T>
+static int entries_to_csr(swe_ctx* c, int inst, const T* d_arr, double* out, const U* d_diag_rows = nullptr) {
   const Layout& L = c->L;
   const int64_t s0 = L.row_off[inst] / 32, s1 = L.row_off[inst + 1] / 32;
   const int64_t e0 = L.slice_ptr[s0], e1 = L.slice_ptr[s1];
   std::vector<T> h(e1 - e0);
   CK(cudaMemcpyAsync(h.data(), d_arr + e0, (e1 - e0) * sizeof(T), cudaMemcpyDeviceToHost, c->stream));
+  const int64_t r0 = L.row_off[inst], r1 = L.row_off[inst + 1];
+  std::vector<U> hd(r1 - r0, U(0));
+  if (d_diag_rows)
+    CK(cudaMemcpyAsync(hd.data(), d_diag_rows + r0, (r1 - r0) * sizeof(U), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   for (int64_t e = e0; e < e1; e++)
     if (L.ref_pos[e] >= 0) out[L.ref_pos[e]] = (double)h[e - e0];
+  for (int64_t r = r0; r < r1; r++)
+    if (L.ref_pos_diag[r] >= 0) out[L.ref_pos_diag[r]] = (double)hd[r - r0];
   return SWE_OK;
 }
 
@@ -569,11 +588,11 @@ SWE_API int swe_compute_dij(swe_ctx* c, int inst, const double* un, double* dij,
   std::vector<InstState> saved;
   if ((rc = save_state(c, saved))) return rc;
   if ((rc = set_inst_state_dt(c, inst, c->params[inst].dt > 0 ? c->params[inst].dt : 1.0, 1))) return rc;
-  launch_dt_f64(c->G, c->d_C, c->d_St, c->A, c->w.dL, c->d_err, c->block, c->stream);
+  launch_dt_f64(c->G, c->d_C, c->d_St, c->A, c->w.dL, c->w.dLii, c->d_err, c->block, c->stream);
   CK(cudaGetLastError());
   if ((rc = read_errors(c))) { restore_done(c, saved); return rc; }
   std::vector<double> d(c->meshes[inst].ja.size());
-  if ((rc = entries_to_csr(c, inst, c->w.dL, d.data()))) return rc;
+  if ((rc = entries_to_csr(c, inst, c->w.dL, d.data(), c->w.dLii))) return rc;
   if ((rc = restore_done(c, saved))) return rc;
   if (dij) std::copy(d.begin(), d.end(), dij);
   if (dt_out) {
@@ -598,7 +617,7 @@ SWE_API int swe_euler(swe_ctx* c, int inst, const double* un, double* unext) {
     launch_stage_f64(a, c->stream);
   } else {
     StageArgsMix a{c->G, c->d_C, c->d_St, c->mA, c->mA, c->mB, c->wm, 0, c->d_err, c->block};
-    launch_stage_mix(a, c->stream);
+    launch_stage_mix(a, c->stream, nullptr, c->tune);
   }
   CK(cudaGetLastError());
   int erc = read_errors(c);
@@ -619,10 +638,10 @@ SWE_API int swe_euler_intermediates(swe_ctx* c, int inst, double* dij_low, doubl
   if (!c->euler_done || c->euler_inst != inst) return fail(c, SWE_ERR_ARG, "call swe_euler on this instance first");
   int rc;
   if (c->precision == SWE_PREC_FP64) {
-    if (dij_low && (rc = entries_to_csr(c, inst, c->w.dL, dij_low))) return rc;
-    if (muij_low && (rc = entries_to_csr(c, inst, c->w.muL, muij_low))) return rc;
-    if (fctmat && (rc = entries_to_csr(c, inst, c->w.fct, fctmat))) return rc;
-    if (lij && (rc = entries_to_csr(c, inst, c->d_lij, lij))) return rc;
+    if (dij_low && (rc = entries_to_csr(c, inst, c->w.dL, dij_low, c->w.dLii))) return rc;
+    if (muij_low && (rc = entries_to_csr(c, inst, c->w.muL, muij_low, c->w.muLii))) return rc;
+    if (fctmat && (rc = entries_to_csr(c, inst, c->w.fct, fctmat))) return rc;          // f_ii = 0
+    if (lij && (rc = entries_to_csr(c, inst, c->d_lij, lij, c->w.rminus))) return rc;   // l_ii = R_i
     if (alpha && (rc = rows_to_nodes(c, inst, c->w.alpha, alpha))) return rc;
     if (res && (rc = rows_to_nodes(c, inst, c->w.res, res))) return rc;
     if (rminus && (rc = rows_to_nodes(c, inst, c->w.rminus, rminus))) return rc;
@@ -647,17 +666,22 @@ SWE_API int swe_fct_positivity(swe_ctx* c, int inst, const double* unext, const 
   if (c->precision != SWE_PREC_FP64) return fail(c, SWE_ERR_ARG, "swe_fct_positivity is an FP64 operator");
   const Layout& L = c->L;
   const HostMesh& m = c->meshes[inst];
-  std::vector<double> hrow(L.n_rows, 0.0), hent(L.n_entries, 0.0);
-  for (int i = 0; i < m.np; i++) hrow[L.new_of_old[inst][i]] = unext[i];
+  std::vector<double> hrow(L.n_rows, 0.0), hdiag(L.n_rows, 0.0), hent(L.n_entries, 0.0);
+  for (int i = 0; i < m.np; i++) {
+    const int64_t r = L.new_of_old[inst][i];
+    hrow[r] = unext[i];
+    hdiag[r] = mat[m.diag[i]];
+  }
   const int64_t s0 = L.row_off[inst] / 32, s1 = L.row_off[inst + 1] / 32;
   for (int64_t e = L.slice_ptr[s0]; e < L.slice_ptr[s1]; e++)
     if (L.ref_pos[e] >= 0) hent[e] = mat[L.ref_pos[e]];
   CK(cudaMemcpyAsync(c->w.uL.h, hrow.data(), L.n_rows * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->w.dLii, hdiag.data(), L.n_rows * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(c->w.fct, hent.data(), L.n_entries * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  launch_fct_positivity_f64(c->G, c->d_C, c->w.uL.h, c->w.fct, c->w.rminus, c->d_lij, c->stream);
+  launch_fct_positivity_f64(c->G, c->d_C, c->w.uL.h, c->w.fct, c->w.dLii, c->w.rminus, c->d_lij, c->stream);
   CK(cudaGetLastError());
   c->euler_done = false;
-  return entries_to_csr(c, inst, c->d_lij, lij);
+  return entries_to_csr(c, inst, c->d_lij, lij, c->w.rminus);   // l_ii = R_i
 }
 
 SWE_API int swe_upload(swe_ctx* c, const double* un) {
@@ -709,9 +733,83 @@ SWE_API int swe_set_time(swe_ctx* c, const double* time, const double* t_final) 
   return restore_done(c, hs);
 }
 
+// Autotuner of the mixed kernels: for every kernel kind, time each (block
+// size, entry batch) variant on the current state and keep the fastest.  The
+// variants compute identical results and every timed kernel is idempotent on
+// its inputs (it only rewrites its own outputs), so the state is unchanged.
+static int autotune(swe_ctx* c) {
+  if (c->precision != SWE_PREC_MIXED) { c->tuned = true; return SWE_OK; }
+  int rc;
+  std::vector<InstState> saved;
+  if ((rc = save_state(c, saved))) return rc;
+  std::vector<InstState> run = saved;
+  for (auto& st : run) { st.done = 0; if (!(st.dt > 0)) { st.dt = 1e-6; st.inv_dt = 1e6; } }
+  if ((rc = restore_done(c, run))) return rc;
+  const cudaStream_t s = c->stream;
+  StageArgsMix a{c->G, c->d_C, c->d_St, c->mA, c->mA, c->mB, c->wm, 1, c->d_err, c->block};
+  KernelTune t = c->tune;
+  launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->d_err, t, s);   // populate every work array once
+  launch_stage_mix(a, s, nullptr, t);
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const int blocks[3] = {64, 128, 256};
+  const int batches[3] = {1, 2, 4};
+  std::string desc;
+  const char* names[5] = {"dt", "node", "low", "fct", "update"};
+  for (int kind = 0; kind < 5; kind++) {
+    float best = 1e30f;
+    int bb = t.block[kind], bt = t.batch[kind];
+    for (int ib = 0; ib < 3; ib++)
+      for (int it = 0; it < 3; it++) {
+        if (kind == 2 && batches[it] > 2) continue;
+        KernelTune v = t;
+        v.block[kind] = blocks[ib];
+        v.batch[kind] = batches[it];
+        float tmin = 1e30f;
+        for (int rep = 0; rep < 3; rep++) {
+          cudaEventRecord(e0, s);
+          if (kind == 0) launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->d_err, v, s);
+          else launch_kernel_mix(kind, a, v, s);
+          cudaEventRecord(e1, s);
+          CK(cudaEventSynchronize(e1));
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, e0, e1);
+          tmin = std::min(tmin, ms);
+        }
+        if (tmin < best) { best = tmin; bb = blocks[ib]; bt = batches[it]; }
+      }
+    t.block[kind] = bb;
+    t.batch[kind] = bt;
+    char buf[64];
+    snprintf(buf, sizeof buf, "%s%s:block%d/batch%d", kind ? " " : "", names[kind], bb, bt);
+    desc += buf;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CK(cudaGetLastError());
+  CK(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned), s));
+  if ((rc = restore_done(c, saved))) return rc;
+  c->tune = t;
+  c->tuned = true;
+  c->tuning = "thread-per-row SELL-32; autotuned " + desc;
+  if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; c->graph_steps = 0; }
+  return SWE_OK;
+}
+
+SWE_API int swe_autotune(swe_ctx* c) {
+  if (!c) return SWE_ERR_ARG;
+  return autotune(c);
+}
+
 SWE_API int swe_rk3_steps(swe_ctx* c, int nsteps, double* time_out, double* dt_out, int* steps_done) {
   if (!c || nsteps < 0) return fail(c, SWE_ERR_ARG, "bad arguments");
   int rc;
+  if (!c->tuned) {
+    const char* env = getenv("SWE_AUTOTUNE");
+    if (env && env[0] == '0') c->tuned = true;
+    else if ((rc = autotune(c))) return rc;
+  }
   std::vector<InstState> hs;
   if ((rc = save_state(c, hs))) return rc;
   for (auto& s : hs) { s.steps = 0; s.maxd_bits = 0ull; }

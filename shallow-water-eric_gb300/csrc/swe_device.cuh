@@ -24,18 +24,24 @@ struct InstState {
 };
 
 // The SELL-32 edge graph (see swe_setup.hpp).  Entry k of row r is at
-// slice_ptr[r>>5] + 32*k + (r&31).
+// slice_ptr[r>>5] + 32*k + (r&31); entries are the off-diagonal CSR entries
+// in reference order, the diagonal (c_ii) is stored per row and belongs
+// between entries dpos-1 and dpos of the reference row.
 struct Graph {
   int64_t n_rows;
   const int64_t* __restrict__ slice_ptr;
   const int* __restrict__ slice_inst;
   const int* __restrict__ col;
-  const uint8_t* __restrict__ len;
+  const uint8_t* __restrict__ len;       // off-diagonal entries (0: padding row)
   const uint8_t* __restrict__ dpos;
   const double* __restrict__ cx;
   const double* __restrict__ cy;
+  const double* __restrict__ cxii;
+  const double* __restrict__ cyii;
   const float* __restrict__ cxf;
   const float* __restrict__ cyf;
+  const float* __restrict__ cxiif;
+  const float* __restrict__ cyiif;
   const double* __restrict__ lumped;
   const double* __restrict__ inv_lumped;
   const double* __restrict__ bath;

@@ -26,7 +26,8 @@ struct StateMix {
 // Work arrays of one stage
 struct WorkF64 {
   double *ovh, *v1, *v2, *ent, *alpha;   // per row
-  double *dL, *muL, *fct;                // per entry
+  double *dL, *muL, *fct;                // per off-diagonal entry
+  double *dLii, *muLii;                  // per row: the diagonal of dL, muL
   double *res, *rminus;                  // per row
   StateF64 uL;                           // low-order state
 };
@@ -71,16 +72,26 @@ struct KernelEvents {
 
 void launch_stage_f64(const StageArgs& a, cudaStream_t s, const KernelEvents* kev = nullptr);
 void launch_dt_f64(const Graph& G, const InstConst* C, InstState* St, const StateF64& u, double* d_out,
-                   unsigned* err, int block, cudaStream_t s);
+                   double* dii_out, unsigned* err, int block, cudaStream_t s);
 void launch_step_begin(const InstConst* C, InstState* St, int n_inst, cudaStream_t s);
 void launch_step_end(InstState* St, int n_inst, cudaStream_t s);
 void launch_fct_positivity_f64(const Graph& G, const InstConst* C, const double* unext, const double* mat,
-                               double* rtmp, double* lij, cudaStream_t s);
+                               const double* matii, double* rtmp, double* lij, cudaStream_t s);
 void launch_mass_f64(const Graph& G, const double* h, double* acc, cudaStream_t s);
 
-void launch_stage_mix(const StageArgsMix& a, cudaStream_t s, const KernelEvents* kev = nullptr);
-void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, unsigned* err, int block,
-                   cudaStream_t s);
+// Launch configuration of the mixed kernels, per kernel kind (0 dt, 1 node,
+// 2 low, 3 fct, 4 update): block size and entry batch (1, 2 or 4; 1 or 2 for
+// low).  Chosen by the autotuner in swe_api.cu; every choice gives the same
+// results.
+struct KernelTune {
+  int block[5] = {128, 128, 128, 128, 128};
+  int batch[5] = {1, 1, 1, 1, 1};
+};
+
+void launch_stage_mix(const StageArgsMix& a, cudaStream_t s, const KernelEvents* kev, const KernelTune& t);
+void launch_kernel_mix(int kind, const StageArgsMix& a, const KernelTune& t, cudaStream_t s);
+void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, unsigned* err,
+                   const KernelTune& t, cudaStream_t s);
 void launch_refresh_z(const Graph& G, StateMix u, cudaStream_t s);
 
 // kernels launched per stage / per step (for launch accounting)

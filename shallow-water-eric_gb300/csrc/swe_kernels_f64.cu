@@ -53,10 +53,12 @@ __global__ void k_node_f64(Graph G, const InstConst* __restrict__ C, const InstS
   nd.ent[r] = 0.5 * E;
   double alpha = 1.0;
   if (c.alpha_limit && !(h <= c.htiny)) {
-    int64_t base = entry_base(G, r);
+    const int64_t base = entry_base(G, r);
+    const int dp = G.dpos[r];
     double num = 0.0, denom = 0.0;
-    for (int k = 0; k < L; k++) {
-      double hj = u.h[G.col[base + 32 * k]];
+    for (int kk = 0; kk <= L; kk++) {          // reference order, diagonal at dp
+      const int k = kk - (kk > dp ? 1 : 0);
+      const double hj = (kk == dp) ? h : u.h[G.col[base + 32 * k]];
       num = num + hj - h;
       denom = denom + tabs(hj - h);
     }
@@ -118,7 +120,8 @@ __device__ __forceinline__ void sgn_node_f64(const InstConst& c, double m, doubl
 // ---------------------------------------------------------------------------
 __global__ void k_low_f64(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St,
                           StateF64 u, NodeF64 nd, double* __restrict__ dL, double* __restrict__ muL,
-                          StateF64 uL, double* __restrict__ res, unsigned* __restrict__ err) {
+                          double* __restrict__ dLii, double* __restrict__ muLii, StateF64 uL,
+                          double* __restrict__ res, unsigned* __restrict__ err) {
   int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= G.n_rows) return;
   const int L = G.len[r];
@@ -139,13 +142,14 @@ __global__ void k_low_f64(Graph G, const InstConst* __restrict__ C, const InstSt
   const double zi = G.bath[r], m = G.lumped[r];
   bool delta_bad = false;
 
-  // pass 1: raw d_ij (lambda_max) and mu_ij, diagonals = -row sums
+  // pass 1: raw d_ij (lambda_max) and mu_ij, diagonals = -row sums (the
+  // diagonal's own value, 0, adds nothing to the sums)
   double sd = 0.0, sm = 0.0;
   for (int k = 0; k < L; k++) {
     const int64_t e = base + 32 * k;
     const int j = G.col[e];
     double d = 0.0, mu = 0.0;
-    if (k != dp) {
+    {
       const double cxe = G.cx[e], cye = G.cy[e];
       const double norm = sqrt(cxe * cxe + cye * cye);
       const double nx = cxe / norm, ny = cye / norm;
@@ -177,23 +181,24 @@ __global__ void k_low_f64(Graph G, const InstConst* __restrict__ C, const InstSt
   }
   const double dii_raw = -sd, muii_raw = -sm;
   // pass 2: dij = MAX(dij, muij) on every entry, then alpha limiting with the
-  // reference's diagonal re-summation
+  // reference's diagonal re-summation (the mu sum includes the old mu_ii at
+  // its place in the row)
   sd = 0.0; sm = 0.0;
-  for (int k = 0; k < L; k++) {
-    const int64_t e = base + 32 * k;
-    double d, mu;
-    if (k == dp) {
-      d = tmax(dii_raw, muii_raw);
-      mu = muii_raw;
-      if (c.alpha_limit) d = 0.0;
-    } else {
-      mu = muL[e];
-      d = tmax(dL[e], mu);
-      if (c.alpha_limit) {
-        const double s = tmax(ai, nd.alpha[G.col[e]]);
-        d = d * s;
-        mu = mu * s;
-      }
+  double dii = tmax(dii_raw, muii_raw), muii = muii_raw;
+  if (c.alpha_limit) dii = 0.0;
+  for (int kk = 0; kk <= L; kk++) {
+    if (kk == dp) {
+      sd = sd + dii;
+      sm = sm + muii;
+      continue;
+    }
+    const int64_t e = base + 32 * (kk - (kk > dp ? 1 : 0));
+    double mu = muL[e];
+    double d = tmax(dL[e], mu);
+    if (c.alpha_limit) {
+      const double s = tmax(ai, nd.alpha[G.col[e]]);
+      d = d * s;
+      mu = mu * s;
     }
     sd = sd + d;
     sm = sm + mu;
@@ -201,24 +206,28 @@ __global__ void k_low_f64(Graph G, const InstConst* __restrict__ C, const InstSt
     muL[e] = mu;
   }
   if (c.alpha_limit) {
-    dL[base + 32 * dp] = -sd;
-    muL[base + 32 * dp] = -sm;
+    dii = -sd;
+    muii = -sm;
   }
+  dLii[r] = dii;
+  muLii[r] = muii;
 
-  // pass 3: smb_2_roundoff and smb_2 rows, maxmin of the entropy
+  // pass 3: smb_2_roundoff and smb_2 rows, maxmin of the entropy, in
+  // reference order with the diagonal at dp
   double rk[5] = {0, 0, 0, 0, 0}, rk2[5] = {0, 0, 0, 0, 0};
   double fix = 0.0;
-  double emax = nd.ent[G.col[base]], emin = emax;
-  for (int k = 0; k < L; k++) {
-    const int64_t e = base + 32 * k;
-    const int j = G.col[e];
+  double emax = nd.ent[r], emin = emax;
+  for (int kk = 0; kk <= L; kk++) {
+    const bool isd = (kk == dp);
+    const int64_t e = base + 32 * (kk - (kk > dp ? 1 : 0));
+    const int j = isd ? (int)r : G.col[e];
     double uj[5];
     uj[0] = u.h[j]; uj[1] = u.q1[j]; uj[2] = u.q2[j];
     if (S == 5) { uj[3] = u.q3[j]; uj[4] = u.q4[j]; }
     const double zj = G.bath[j];
     const double v1j = nd.v1[j], v2j = nd.v2[j];
-    const double d = dL[e], mu = muL[e];
-    const double cxe = G.cx[e], cye = G.cy[e];
+    const double d = isd ? dii : dL[e], mu = isd ? muii : muL[e];
+    const double cxe = isd ? G.cxii[r] : G.cx[e], cye = isd ? G.cyii[r] : G.cy[e];
     const double ej = nd.ent[j];
     emax = tmax(emax, ej);
     emin = tmin(emin, ej);
@@ -232,7 +241,7 @@ __global__ void k_low_f64(Graph G, const InstConst* __restrict__ C, const InstSt
       double xx = 0.0;
       xx = xx - cxe * (v1j);
       xx = xx - cye * (v2j);
-      if (k == dp) {
+      if (isd) {
         fix = fix + xx;
       } else {
         fix = fix - mu + (d - mu) * (-ratij);
@@ -268,13 +277,15 @@ __global__ void k_low_f64(Graph G, const InstConst* __restrict__ C, const InstSt
     double s_i, p_i;
     sgn_node_f64(c, m, ui[0], ui[3], &p_i, &s_i);
     double ax = rk[1], ay = rk[2], bx = rk2[1], by = rk2[2];
-    for (int k = 0; k < L; k++) {
-      const int64_t e = base + 32 * k;
-      const int j = G.col[e];
+    for (int kk = 0; kk <= L; kk++) {
+      const bool isd = (kk == dp);
+      const int64_t e = base + 32 * (kk - (kk > dp ? 1 : 0));
+      const int j = isd ? (int)r : G.col[e];
+      const double cxe = isd ? G.cxii[r] : G.cx[e], cye = isd ? G.cyii[r] : G.cy[e];
       double pj, sj;
       sgn_node_f64(c, G.lumped[j], u.h[j], u.q3[j], &pj, &sj);
-      ax = ax - pj * G.cx[e]; ay = ay - pj * G.cy[e];
-      bx = bx - pj * G.cx[e]; by = by - pj * G.cy[e];
+      ax = ax - pj * cxe; ay = ay - pj * cye;
+      bx = bx - pj * cxe; by = by - pj * cye;
     }
     source_f64(c, st, m, ui, v1i, v2i, rk, ax, ay, s_i);
     source_f64(c, st, m, ui, v1i, v2i, rk2, bx, by, s_i);
@@ -436,7 +447,8 @@ __global__ void k_update_f64(Graph G, const InstConst* __restrict__ C, const Ins
 // receives every d_ij.
 // ---------------------------------------------------------------------------
 __global__ void k_dt_f64(Graph G, const InstConst* __restrict__ C, InstState* __restrict__ St, StateF64 u,
-                         const double* __restrict__ ovh, double* __restrict__ d_out, unsigned* __restrict__ err) {
+                         const double* __restrict__ ovh, double* __restrict__ d_out, double* __restrict__ dii_out,
+                         unsigned* __restrict__ err) {
   int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   double val = 0.0;
   int b = -1;
@@ -444,7 +456,7 @@ __global__ void k_dt_f64(Graph G, const InstConst* __restrict__ C, InstState* __
     b = G.slice_inst[r >> 5];
     if (!St[b].done) {
       const InstConst& c = C[b];
-      const int L = G.len[r], dp = G.dpos[r];
+      const int L = G.len[r];
       const int64_t base = entry_base(G, r);
       const double sqrt2 = sqrt(2.0);
       const double hi = u.h[r], q1 = u.q1[r], q2 = u.q2[r];
@@ -454,7 +466,7 @@ __global__ void k_dt_f64(Graph G, const InstConst* __restrict__ C, InstState* __
       for (int k = 0; k < L; k++) {
         const int64_t e = base + 32 * k;
         double d = 0.0;
-        if (k != dp) {
+        {
           const int j = G.col[e];
           const double cxe = G.cx[e], cye = G.cy[e];
           const double norm = sqrt(cxe * cxe + cye * cye);
@@ -469,7 +481,7 @@ __global__ void k_dt_f64(Graph G, const InstConst* __restrict__ C, InstState* __
         if (d_out) d_out[e] = d;
         s = s + d;
       }
-      if (d_out) d_out[base + 32 * dp] = -s;
+      if (dii_out) dii_out[r] = -s;
       val = tabs(-s) / G.lumped[r];
       if (bad) atomicOr(err, ERRB_DELTA);
     } else {
@@ -513,8 +525,8 @@ __global__ void k_step_end(InstState* __restrict__ St, int n_inst) {
 
 // FCT_positivity as a stand-alone operator on one instance (fct.f90:5-42)
 __global__ void k_fct_positivity_f64(Graph G, const InstConst* __restrict__ C, const double* __restrict__ unext,
-                                     const double* __restrict__ mat, double* __restrict__ rtmp,
-                                     double* __restrict__ lij, int pass) {
+                                     const double* __restrict__ mat, const double* __restrict__ matii,
+                                     double* __restrict__ rtmp, double* __restrict__ lij, int pass) {
   int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= G.n_rows) return;
   const int L = G.len[r];
@@ -522,9 +534,10 @@ __global__ void k_fct_positivity_f64(Graph G, const InstConst* __restrict__ C, c
   const int b = G.slice_inst[r >> 5];
   const int64_t base = entry_base(G, r);
   if (pass == 0) {
+    const int dp = G.dpos[r];
     double P = -1.e-15;
-    for (int k = 0; k < L; k++) {
-      const double f = mat[base + 32 * k];
+    for (int kk = 0; kk <= L; kk++) {         // reference order, diagonal at dp
+      const double f = (kk == dp) ? matii[r] : mat[base + 32 * (kk - (kk > dp ? 1 : 0))];
       if (f < 0.0) P = P + f;
     }
     double R = tmin((0.0 - unext[r]) / P, 1.0);
@@ -574,7 +587,8 @@ void launch_stage_f64(const StageArgs& a, cudaStream_t s, const KernelEvents* ke
   EV_BEGIN(1);
   k_node_f64<<<nblk(a.G.n_rows, bs), bs, 0, s>>>(a.G, a.C, a.St, a.u, nd);
   EV_END(1); EV_BEGIN(2);
-  k_low_f64<<<nblk(a.G.n_rows, bs), bs, 0, s>>>(a.G, a.C, a.St, a.u, nd, a.w.dL, a.w.muL, a.w.uL, a.w.res, a.err);
+  k_low_f64<<<nblk(a.G.n_rows, bs), bs, 0, s>>>(a.G, a.C, a.St, a.u, nd, a.w.dL, a.w.muL, a.w.dLii, a.w.muLii,
+                                                a.w.uL, a.w.res, a.err);
   EV_END(2); EV_BEGIN(3);
   k_fct_f64<<<nblk(a.G.n_rows, bs), bs, 0, s>>>(a.G, a.C, a.St, a.u, a.w.dL, a.w.muL, a.w.uL, a.w.res, a.w.fct,
                                                 a.w.rminus, a.err);
@@ -585,8 +599,8 @@ void launch_stage_f64(const StageArgs& a, cudaStream_t s, const KernelEvents* ke
 }
 
 void launch_dt_f64(const Graph& G, const InstConst* C, InstState* St, const StateF64& u, double* d_out,
-                   unsigned* err, int block, cudaStream_t s) {
-  k_dt_f64<<<nblk(G.n_rows, block), block, 0, s>>>(G, C, St, u, nullptr, d_out, err);
+                   double* dii_out, unsigned* err, int block, cudaStream_t s) {
+  k_dt_f64<<<nblk(G.n_rows, block), block, 0, s>>>(G, C, St, u, nullptr, d_out, dii_out, err);
 }
 
 void launch_step_begin(const InstConst* C, InstState* St, int n_inst, cudaStream_t s) {
@@ -598,9 +612,9 @@ void launch_step_end(InstState* St, int n_inst, cudaStream_t s) {
 }
 
 void launch_fct_positivity_f64(const Graph& G, const InstConst* C, const double* unext, const double* mat,
-                               double* rtmp, double* lij, cudaStream_t s) {
-  k_fct_positivity_f64<<<nblk(G.n_rows, 128), 128, 0, s>>>(G, C, unext, mat, rtmp, lij, 0);
-  k_fct_positivity_f64<<<nblk(G.n_rows, 128), 128, 0, s>>>(G, C, unext, mat, rtmp, lij, 1);
+                               const double* matii, double* rtmp, double* lij, cudaStream_t s) {
+  k_fct_positivity_f64<<<nblk(G.n_rows, 128), 128, 0, s>>>(G, C, unext, mat, matii, rtmp, lij, 0);
+  k_fct_positivity_f64<<<nblk(G.n_rows, 128), 128, 0, s>>>(G, C, unext, mat, matii, rtmp, lij, 1);
 }
 
 void launch_mass_f64(const Graph& G, const double* h, double* acc, cudaStream_t s) {

@@ -58,9 +58,16 @@ __device__ __forceinline__ float fct_from(float dd, float dm, float hi, float hj
   return __fadd_rn(__fmul_rn(dd, a), __fmul_rn(dm, b));
 }
 
+// Entry loops are processed in batches of B entries: every load of a batch is
+// issued before any of them is used, so a thread keeps B gathers in flight
+// (the kernels are latency-bound otherwise).  Sums keep the entry order, so
+// every batch size gives the same result; the autotuner picks B per kernel.
+
 // k_node_mix: alpha_i (SOURCES/update.f90:758-781) from the FP32 depth.
-__global__ void k_node_mix(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St, StateMix u,
-                           float* __restrict__ alpha_out) {
+template <int B>
+__global__ void __launch_bounds__(256) k_node_mix(Graph G, const InstConst* __restrict__ C,
+                                                  const InstState* __restrict__ St, StateMix u,
+                                                  float* __restrict__ alpha_out) {
   int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= G.n_rows) return;
   const int L = G.len[r];
@@ -74,10 +81,19 @@ __global__ void k_node_mix(Graph G, const InstConst* __restrict__ C, const InstS
   if (c.alpha_limit && !(h <= (float)c.htiny)) {
     const int64_t base = entry_base(G, r);
     float num = 0.0f, denom = 0.0f;
-    for (int k = 0; k < L; k++) {
-      const float hj = hs[4 * (int64_t)G.col[base + 32 * k]];
-      num += hj - h;
-      denom += fabsf(hj - h);
+    for (int k0 = 0; k0 < L; k0 += B) {
+      int j[B];
+#pragma unroll
+      for (int q = 0; q < B; q++) j[q] = (k0 + q < L) ? G.col[base + 32 * (k0 + q)] : (int)r;
+      float hj[B];
+#pragma unroll
+      for (int q = 0; q < B; q++) hj[q] = hs[4 * (int64_t)j[q]];
+#pragma unroll
+      for (int q = 0; q < B; q++)
+        if (k0 + q < L) {
+          num += hj[q] - h;
+          denom += fabsf(hj[q] - h);
+        }
     }
     const float a = (denom <= fabsf(num)) ? 1.0f : fdiv(fabsf(num), denom);
     const float a2 = a * a, a4 = a2 * a2;
@@ -114,7 +130,8 @@ __device__ __forceinline__ float sgn_pressure(float lambda_sgn, float g, float m
 // formed once and shared by mu_ij and the Galerkin flux.  The diagonal entry
 // only enters through terms that vanish identically (u_i rat_ii - u_i rat_ii)
 // and the Galerkin boundary term -c_ii.v_i.
-__global__ void __launch_bounds__(128) k_low_mix(Graph G, const InstConst* __restrict__ C,
+template <int B>
+__global__ void __launch_bounds__(256) k_low_mix(Graph G, const InstConst* __restrict__ C,
                                                  const InstState* __restrict__ St, StateMix u,
                                                  const float* __restrict__ alpha, float* __restrict__ dL,
                                                  float* __restrict__ muL, WorkMix w, float* __restrict__ res,
@@ -132,7 +149,6 @@ __global__ void __launch_bounds__(128) k_low_mix(Graph G, const InstConst* __res
   const float g = (float)c.g, htiny = (float)c.htiny, dtf = (float)st.dt;
   const float sqrt2 = 1.41421356237309515f;
   const int64_t base = entry_base(G, r);
-  const int dp = G.dpos[r];
   const NodeF ni = load_node(u, r, htiny);
   const float v2i_flux = sgn ? 0.f : ni.v2;          // flux() zeroes velocity(2) for type 13
   const float ai = alpha[r];
@@ -142,33 +158,55 @@ __global__ void __launch_bounds__(128) k_low_mix(Graph G, const InstConst* __res
   const float invhi = inv_pos(ni.h);
   bool delta_bad = false;
 
-  float sd = 0.f, sm_raw = 0.f, sm = 0.f;
   float fix = 0.f, rk0 = 0.f;
   float rk1 = 0.f, rk2_ = 0.f, rk3 = 0.f, rk4 = 0.f;               // smb_2_roundoff momenta
   float g0 = 0.f, g1 = 0.f, g2 = 0.f, g3 = 0.f, g4 = 0.f;          // smb_2
   const float Ei = 0.5f * (g * ni.h * ni.h + ni.v1 * ni.q1 + v2i_flux * ni.q2);
   float emax = Ei, emin = Ei;
   float ptx = 0.f, pty = 0.f;
-  for (int k = 0; k < L; k++) {
-    const int64_t e = base + 32 * k;
-    const float cxe = G.cxf[e], cye = G.cyf[e];
-    if (k == dp) {
-      // diagonal: Galerkin boundary term -c_ii.v_i (fix_roundoff / smb_2)
-      const float cvi = dotc(cxe, cye, ni.v1, v2i_flux);
-      fix -= cvi;
-      g0 -= cvi * ni.h;
-      rk1 -= cvi * ni.q1; rk2_ -= cvi * ni.q2;
-      g1 -= cvi * ni.q1; g2 -= cvi * ni.q2;
-      if (S == 5) { rk3 -= cvi * ui3; rk4 -= cvi * ui4; g3 -= cvi * ui3; g4 -= cvi * ui4; }
-      if (sgn) {
-        const float pt = sgn_pressure((float)c.lambda_sgn, g, m, ni.h, ui3);
-        ptx -= pt * cxe;
-        pty -= pt * cye;
-      }
-      continue;
+  {
+    // diagonal: Galerkin boundary term -c_ii.v_i (fix_roundoff / smb_2);
+    // its viscous and topography terms vanish
+    const float cxe = G.cxiif[r], cye = G.cyiif[r];
+    const float cvi = dotc(cxe, cye, ni.v1, v2i_flux);
+    fix -= cvi;
+    g0 -= cvi * ni.h;
+    rk1 -= cvi * ni.q1; rk2_ -= cvi * ni.q2;
+    g1 -= cvi * ni.q1; g2 -= cvi * ni.q2;
+    if (S == 5) { rk3 -= cvi * ui3; rk4 -= cvi * ui4; g3 -= cvi * ui3; g4 -= cvi * ui4; }
+    if (sgn) {
+      const float pt = sgn_pressure((float)c.lambda_sgn, g, m, ni.h, ui3);
+      ptx -= pt * cxe;
+      pty -= pt * cye;
     }
-    const int j = G.col[e];
-    const NodeF nj = load_node(u, j, htiny);
+  }
+  for (int k0 = 0; k0 < L; k0 += B) {
+   int jb[B];
+   float cxb[B], cyb[B];
+#pragma unroll
+   for (int q = 0; q < B; q++) {
+     if (k0 + q < L) {
+       const int64_t e = base + 32 * (k0 + q);
+       jb[q] = G.col[e]; cxb[q] = G.cxf[e]; cyb[q] = G.cyf[e];
+     } else {
+       jb[q] = (int)r; cxb[q] = 0.f; cyb[q] = 0.f;
+     }
+   }
+   float4 nqb[B];
+   float alb[B];
+#pragma unroll
+   for (int q = 0; q < B; q++) { nqb[q] = u.nq[jb[q]]; alb[q] = alpha[jb[q]]; }
+#pragma unroll
+   for (int q = 0; q < B; q++) {
+    if (k0 + q >= L) break;
+    const int64_t e = base + 32 * (k0 + q);
+    const float cxe = cxb[q], cye = cyb[q];
+    const int j = jb[q];
+    NodeF nj;
+    nj.h = nqb[q].x; nj.q1 = nqb[q].y; nj.q2 = nqb[q].z; nj.z = nqb[q].w;
+    nj.ovh = ovh_f(nj.h, htiny);
+    nj.v1 = nj.q1 * nj.ovh;
+    nj.v2 = nj.q2 * nj.ovh;
     // --- viscosities: compute_dij, compute_muij, MAX, alpha_limit
     const float norm = sqrtf(cxe * cxe + cye * cye);
     const float inv = fdiv(1.0f, norm);
@@ -178,15 +216,12 @@ __global__ void __launch_bounds__(128) k_low_mix(Graph G, const InstConst* __res
       delta_bad = true;
     const float cvj = dotc(cxe, cye, nj.v1, nj.v2);                   // c.v_j (compute_muij)
     float mu = fmaxf(fmaxf(-dotc(cxe, cye, ni.v1, ni.v2), 0.f), fmaxf(cvj, 0.f));
-    sm_raw += mu;
     float d = fmaxf(norm * lam, mu);
     if (c.alpha_limit) {
-      const float s = fmaxf(ai, alpha[j]);
+      const float s = fmaxf(ai, alb[q]);
       d *= s;
       mu *= s;
     }
-    sd += d;
-    sm += mu;
     dL[e] = d;
     muL[e] = mu;
     // --- entropy stencil
@@ -226,10 +261,8 @@ __global__ void __launch_bounds__(128) k_low_mix(Graph G, const InstConst* __res
         pty -= pt * cye;
       }
     }
+   }
   }
-  // diagonals (-row sums, with the reference's mu re-summation under alpha)
-  dL[base + 32 * dp] = -sd;
-  muL[base + 32 * dp] = c.alpha_limit ? -(sm - sm_raw) : -sm_raw;
   // source terms (update.f90:425-551)
   if (c.type_test == 9 || c.type_test == 10) {
     const float fric = (float)(c.g * c.mannings * c.mannings);
@@ -279,7 +312,8 @@ __global__ void __launch_bounds__(128) k_low_mix(Graph G, const InstConst* __res
 }
 
 // k_fct_mix: f_ij (FP32) and R^-_i (FP64 Q^-, P^-, R^-), fct.f90:15-30
-__global__ void k_fct_mix(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St, StateMix u,
+template <int B>
+__global__ void __launch_bounds__(256) k_fct_mix(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St, StateMix u,
                           const float* __restrict__ dL, const float* __restrict__ muL, WorkMix w,
                           const float* __restrict__ res, double* __restrict__ rminus, unsigned* __restrict__ err) {
   int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -291,20 +325,35 @@ __global__ void k_fct_mix(Graph G, const InstConst* __restrict__ C, const InstSt
   if (st.done) return;
   const InstConst& c = C[b];
   const int64_t base = entry_base(G, r);
-  const int dp = G.dpos[r];
   const float4 ni = u.nq[r];
   const float hi = ni.x, zi = ni.w, resi = res[r];
   const float invhi = inv_pos(hi);
-  double P = -1.e-15;
-  for (int k = 0; k < L; k++) {
-    if (k == dp) continue;   // f_ii = 0
-    const int64_t e = base + 32 * k;
-    const int j = G.col[e];
-    const float4 nj = u.nq[j];
-    const float d0 = dL[e], m0 = muL[e], rij = fmaxf(resi, res[j]);
-    const Recon R = recon(hi, nj.x, nj.w - zi, invhi, inv_pos(nj.x));
-    const float f = fct_from(fminf(d0, rij) - d0, fminf(m0, rij) - m0, hi, nj.x, R);
-    if (f < 0.f) P += (double)f;
+  double P = -1.e-15;                    // f_ii = 0 adds nothing
+  for (int k0 = 0; k0 < L; k0 += B) {
+    int jb[B];
+    float d0b[B], m0b[B];
+#pragma unroll
+    for (int q = 0; q < B; q++) {
+      if (k0 + q < L) {
+        const int64_t e = base + 32 * (k0 + q);
+        jb[q] = G.col[e]; d0b[q] = dL[e]; m0b[q] = muL[e];
+      } else {
+        jb[q] = (int)r; d0b[q] = 0.f; m0b[q] = 0.f;
+      }
+    }
+    float4 njb[B];
+    float rsb[B];
+#pragma unroll
+    for (int q = 0; q < B; q++) { njb[q] = u.nq[jb[q]]; rsb[q] = res[jb[q]]; }
+#pragma unroll
+    for (int q = 0; q < B; q++) {
+      if (k0 + q >= L) break;
+      const float d0 = d0b[q], m0 = m0b[q], rij = fmaxf(resi, rsb[q]);
+      const float4 nj = njb[q];
+      const Recon R = recon(hi, nj.x, nj.w - zi, invhi, inv_pos(nj.x));
+      const float f = fct_from(fminf(d0, rij) - d0, fminf(m0, rij) - m0, hi, nj.x, R);
+      if (f < 0.f) P += (double)f;
+    }
   }
   const double hL = w.hL[r];
   if (hL < 0.0) atomicOr(err, ERRB_NEG_H);
@@ -318,7 +367,8 @@ __global__ void k_fct_mix(Graph G, const InstConst* __restrict__ C, const InstSt
 
 // k_update_mix: limited antidiffusion (update.f90:276-282, apply_viscosity
 // :684-718), RK combination and Dirichlet data (main.f90:77-90).
-__global__ void k_update_mix(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St,
+template <int B>
+__global__ void __launch_bounds__(256) k_update_mix(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St,
                              StateMix u, const float* __restrict__ dL, const float* __restrict__ muL, WorkMix w,
                              const float* __restrict__ res, const double* __restrict__ rminus, StateMix u0,
                              StateMix out, int rk_stage, unsigned* __restrict__ err) {
@@ -332,7 +382,6 @@ __global__ void k_update_mix(Graph G, const InstConst* __restrict__ C, const Ins
   const InstConst& c = C[b];
   const int S = c.S;
   const int64_t base = entry_base(G, r);
-  const int dp = G.dpos[r];
   const float4 ni = u.nq[r];
   const float hi = ni.x, zi = ni.w, resi = res[r];
   const float invhi = inv_pos(hi);
@@ -341,17 +390,34 @@ __global__ void k_update_mix(Graph G, const InstConst* __restrict__ C, const Ins
   if (S == 5) { ui3 = u.q3[r]; ui4 = u.q4[r]; }
   double sh = 0.0;                       // sum_j l_ij f_ij (FP64)
   float x1 = 0.f, x2 = 0.f, x3 = 0.f, x4 = 0.f;
-  for (int k = 0; k < L; k++) {
-    if (k == dp) continue;               // (u_i rat_ii - u_i rat_ii) = 0
-    const int64_t e = base + 32 * k;
-    const int j = G.col[e];
-    const float4 nj = u.nq[j];
-    const float d0 = dL[e], m0 = muL[e];
-    const float rij = fmaxf(resi, res[j]);
+  for (int k0 = 0; k0 < L; k0 += B) {    // the diagonal's terms vanish: (u_i rat_ii - u_i rat_ii) = 0
+   int jb[B];
+   float d0b[B], m0b[B];
+#pragma unroll
+   for (int q = 0; q < B; q++) {
+     if (k0 + q < L) {
+       const int64_t e = base + 32 * (k0 + q);
+       jb[q] = G.col[e]; d0b[q] = dL[e]; m0b[q] = muL[e];
+     } else {
+       jb[q] = (int)r; d0b[q] = 0.f; m0b[q] = 0.f;
+     }
+   }
+   float4 njb[B];
+   float rsb[B];
+   double Rjb[B];
+#pragma unroll
+   for (int q = 0; q < B; q++) { njb[q] = u.nq[jb[q]]; rsb[q] = res[jb[q]]; Rjb[q] = rminus[jb[q]]; }
+#pragma unroll
+   for (int q = 0; q < B; q++) {
+    if (k0 + q >= L) break;
+    const int j = jb[q];
+    const float4 nj = njb[q];
+    const float d0 = d0b[q], m0 = m0b[q];
+    const float rij = fmaxf(resi, rsb[q]);
     const float ddr = fminf(d0, rij) - d0, dmr = fminf(m0, rij) - m0;
     const Recon R = recon(hi, nj.x, nj.w - zi, invhi, inv_pos(nj.x));
     const float f = fct_from(ddr, dmr, hi, nj.x, R);
-    const double l = (f >= 0.f) ? rminus[j] : Ri;
+    const double l = (f >= 0.f) ? Rjb[q] : Ri;
     sh += l * (double)f;
     const float lf = (float)l;
     const float dd = ddr * lf, dm = dmr * lf;
@@ -362,6 +428,7 @@ __global__ void k_update_mix(Graph G, const InstConst* __restrict__ C, const Ins
       x3 += dd * (uj3 * R.rji - ui3 * R.rij) + dm * (uj3 * (1.f - R.rji) - ui3 * (1.f - R.rij));
       x4 += dd * (uj4 * R.rji - ui4 * R.rij) + dm * (uj4 * (1.f - R.rji) - ui4 * (1.f - R.rij));
     }
+   }
   }
   const double inv_m = G.inv_lumped[r];
   const float invm = (float)inv_m, dtf = (float)st.dt;
@@ -404,7 +471,8 @@ __global__ void k_update_mix(Graph G, const InstConst* __restrict__ C, const Ins
 }
 
 // k_dt_mix: FP32 lambda_max, max |d_ii|/m_i per instance (main.f90:166-174)
-__global__ void k_dt_mix(Graph G, const InstConst* __restrict__ C, InstState* __restrict__ St, StateMix u,
+template <int B>
+__global__ void __launch_bounds__(256) k_dt_mix(Graph G, const InstConst* __restrict__ C, InstState* __restrict__ St, StateMix u,
                          unsigned* __restrict__ err) {
   int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   float val = 0.f;
@@ -413,17 +481,32 @@ __global__ void k_dt_mix(Graph G, const InstConst* __restrict__ C, InstState* __
     if (!St[b].done) {
       const InstConst& c = C[b];
       const float g = (float)c.g, htiny = (float)c.htiny;
-      const int L = G.len[r], dp = G.dpos[r];
+      const int L = G.len[r];
       const int64_t base = entry_base(G, r);
       const float4 ni = u.nq[r];
       const float oi = ovh_f(ni.x, htiny);
       float s = 0.f;
       bool bad = false;
-      for (int k = 0; k < L; k++) {
-        if (k == dp) continue;
-        const int64_t e = base + 32 * k;
-        const float4 nj = u.nq[G.col[e]];
-        const float cxe = G.cxf[e], cye = G.cyf[e];
+      for (int k0 = 0; k0 < L; k0 += B) {
+       int jb[B];
+       float cxb[B], cyb[B];
+#pragma unroll
+       for (int q = 0; q < B; q++) {
+         if (k0 + q < L) {
+           const int64_t e = base + 32 * (k0 + q);
+           jb[q] = G.col[e]; cxb[q] = G.cxf[e]; cyb[q] = G.cyf[e];
+         } else {
+           jb[q] = (int)r; cxb[q] = 1.f; cyb[q] = 0.f;
+         }
+       }
+       float4 njb[B];
+#pragma unroll
+       for (int q = 0; q < B; q++) njb[q] = u.nq[jb[q]];
+#pragma unroll
+       for (int q = 0; q < B; q++) {
+        if (k0 + q >= L) break;
+        const float4 nj = njb[q];
+        const float cxe = cxb[q], cye = cyb[q];
         const float norm = sqrtf(cxe * cxe + cye * cye);
         const float inv = fdiv(1.0f, norm);
         float lam;
@@ -431,6 +514,7 @@ __global__ void k_dt_mix(Graph G, const InstConst* __restrict__ C, InstState* __
                                 htiny, 1.41421356237309515f, &lam))
           bad = true;
         s += norm * lam;
+       }
       }
       val = s * (float)G.inv_lumped[r];
       if (bad) atomicOr(err, ERRB_DELTA);
@@ -457,25 +541,46 @@ static inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) 
 #define EV_BEGIN(k) if (kev) cudaEventRecord(kev->ev[2 * (k)], s)
 #define EV_END(k) if (kev) cudaEventRecord(kev->ev[2 * (k) + 1], s)
 
-void launch_stage_mix(const StageArgsMix& a, cudaStream_t s, const KernelEvents* kev) {
-  const int bs = a.block;
-  const unsigned nb = nblk(a.G.n_rows, bs);
-  EV_BEGIN(1);
-  k_node_mix<<<nb, bs, 0, s>>>(a.G, a.C, a.St, a.u, a.w.alpha);
-  EV_END(1); EV_BEGIN(2);
-  k_low_mix<<<nblk(a.G.n_rows, 128), 128, 0, s>>>(a.G, a.C, a.St, a.u, a.w.alpha, a.w.dL, a.w.muL, a.w, a.w.res,
-                                                   a.err);
-  EV_END(2); EV_BEGIN(3);
-  k_fct_mix<<<nb, bs, 0, s>>>(a.G, a.C, a.St, a.u, a.w.dL, a.w.muL, a.w, a.w.res, a.w.rminus, a.err);
-  EV_END(3); EV_BEGIN(4);
-  k_update_mix<<<nb, bs, 0, s>>>(a.G, a.C, a.St, a.u, a.w.dL, a.w.muL, a.w, a.w.res, a.w.rminus, a.u0, a.out,
-                                 a.rk_stage, a.err);
-  EV_END(4);
+#define SWE_DISPATCH_B(b, KERNEL, GRID, BS, ...)                         \
+  switch (b) {                                                           \
+    case 4: KERNEL<4><<<GRID, BS, 0, s>>>(__VA_ARGS__); break;           \
+    case 2: KERNEL<2><<<GRID, BS, 0, s>>>(__VA_ARGS__); break;           \
+    default: KERNEL<1><<<GRID, BS, 0, s>>>(__VA_ARGS__); break;          \
+  }
+
+void launch_kernel_mix(int kind, const StageArgsMix& a, const KernelTune& t, cudaStream_t s) {
+  const int64_t n = a.G.n_rows;
+  switch (kind) {
+    case 1: SWE_DISPATCH_B(t.batch[1], k_node_mix, nblk(n, t.block[1]), t.block[1], a.G, a.C, a.St, a.u, a.w.alpha)
+            break;
+    case 2: if (t.batch[2] >= 2)
+              k_low_mix<2><<<nblk(n, t.block[2]), t.block[2], 0, s>>>(a.G, a.C, a.St, a.u, a.w.alpha, a.w.dL, a.w.muL,
+                                                                       a.w, a.w.res, a.err);
+            else
+              k_low_mix<1><<<nblk(n, t.block[2]), t.block[2], 0, s>>>(a.G, a.C, a.St, a.u, a.w.alpha, a.w.dL, a.w.muL,
+                                                                       a.w, a.w.res, a.err);
+            break;
+    case 3: SWE_DISPATCH_B(t.batch[3], k_fct_mix, nblk(n, t.block[3]), t.block[3], a.G, a.C, a.St, a.u, a.w.dL,
+                           a.w.muL, a.w, a.w.res, a.w.rminus, a.err)
+            break;
+    case 4: SWE_DISPATCH_B(t.batch[4], k_update_mix, nblk(n, t.block[4]), t.block[4], a.G, a.C, a.St, a.u, a.w.dL,
+                           a.w.muL, a.w, a.w.res, a.w.rminus, a.u0, a.out, a.rk_stage, a.err)
+            break;
+    default: break;
+  }
 }
 
-void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, unsigned* err, int block,
-                   cudaStream_t s) {
-  k_dt_mix<<<nblk(G.n_rows, block), block, 0, s>>>(G, C, St, u, err);
+void launch_stage_mix(const StageArgsMix& a, cudaStream_t s, const KernelEvents* kev, const KernelTune& t) {
+  for (int kind = 1; kind <= 4; kind++) {
+    EV_BEGIN(kind);
+    launch_kernel_mix(kind, a, t, s);
+    EV_END(kind);
+  }
+}
+
+void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, unsigned* err,
+                   const KernelTune& t, cudaStream_t s) {
+  SWE_DISPATCH_B(t.batch[0], k_dt_mix, nblk(G.n_rows, t.block[0]), t.block[0], G, C, St, u, err)
 }
 
 void launch_refresh_z(const Graph& G, StateMix u, cudaStream_t s) {

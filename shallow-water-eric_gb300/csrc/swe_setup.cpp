@@ -201,6 +201,10 @@ Layout build_layout(const std::vector<HostMesh>& meshes, const std::vector<std::
   L.n_slices = L.n_rows / 32;
   L.len.assign(L.n_rows, 0);
   L.dpos.assign(L.n_rows, 0);
+  L.valid.assign(L.n_rows, 0);
+  L.cxii.assign(L.n_rows, 0.0);
+  L.cyii.assign(L.n_rows, 0.0);
+  L.ref_pos_diag.assign(L.n_rows, -1);
   L.lumped.assign(L.n_rows, 1.0);
   L.bath.assign(L.n_rows, 0.0);
   L.old_of_new.assign(L.n_rows, -1);
@@ -215,8 +219,12 @@ Layout build_layout(const std::vector<HostMesh>& meshes, const std::vector<std::
       int64_t r = L.row_off[b] + nof[i];
       L.new_of_old[b][i] = (int)r;
       L.old_of_new[r] = i;
-      L.len[r] = (uint8_t)(m.ia[i + 1] - m.ia[i]);
+      L.len[r] = (uint8_t)(m.ia[i + 1] - m.ia[i] - 1);
       L.dpos[r] = (uint8_t)(m.diag[i] - m.ia[i]);
+      L.valid[r] = 1;
+      L.cxii[r] = m.cx[m.diag[i]];
+      L.cyii[r] = m.cy[m.diag[i]];
+      L.ref_pos_diag[r] = m.diag[i];
       L.lumped[r] = m.lumped[i];
       L.bath[r] = baths[b][i];
     }
@@ -244,8 +252,10 @@ Layout build_layout(const std::vector<HostMesh>& meshes, const std::vector<std::
     for (int i = 0; i < m.np; i++) {
       int64_t r = L.new_of_old[b][i];
       int64_t base = L.slice_ptr[r / 32] + (r % 32);
+      int k = 0;
       for (int p = m.ia[i]; p < m.ia[i + 1]; p++) {
-        int64_t e = base + 32 * (int64_t)(p - m.ia[i]);
+        if (p == m.diag[i]) continue;
+        int64_t e = base + 32 * (int64_t)(k++);
         L.col[e] = L.new_of_old[b][m.ja[p]];
         L.cx[e] = m.cx[p];
         L.cy[e] = m.cy[p];

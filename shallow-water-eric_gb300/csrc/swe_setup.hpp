@@ -29,8 +29,12 @@ std::vector<int> rcm_order(const HostMesh& m);
 // Global SELL-32 layout of a batch of meshes.  Row r (new numbering) of
 // instance b lives in [row_off[b], row_off[b] + np_b); each instance's row
 // range is padded to a multiple of 32 so that no slice straddles two
-// instances.  Entry k of row r sits at slice_ptr[r/32] + 32*k + r%32, and a
-// row's entries keep the reference CSR order (ascending original column).
+// instances.  Entry k of row r sits at slice_ptr[r/32] + 32*k + r%32.  The
+// entries are the row's OFF-DIAGONAL CSR entries in reference order
+// (ascending original column); the diagonal entry (i,i) is kept per row
+// (cxii, cyii) together with dpos, the number of off-diagonal entries that
+// precede it in the reference row, so that reference-order sums can insert it
+// at its place.
 struct Layout {
   int n_inst = 0;
   int64_t n_rows = 0;                    // padded total
@@ -40,11 +44,14 @@ struct Layout {
   std::vector<int64_t> slice_ptr;        // n_slices + 1, entry offsets
   std::vector<int> slice_inst;           // n_slices
   std::vector<uint8_t> slice_w;          // n_slices, max row length in slice
-  std::vector<uint8_t> len;              // n_rows (0 for padding rows)
-  std::vector<uint8_t> dpos;             // n_rows, k of the diagonal entry
+  std::vector<uint8_t> len;              // n_rows: off-diagonal entries (0 for padding rows)
+  std::vector<uint8_t> dpos;             // n_rows: off-diagonal entries before the diagonal
+  std::vector<uint8_t> valid;            // n_rows: 1 for mesh rows, 0 for padding rows
   std::vector<int> col;                  // n_entries (padding -> own row)
   std::vector<double> cx, cy;            // n_entries (padding -> 0)
+  std::vector<double> cxii, cyii;        // n_rows: diagonal c_ii
   std::vector<int64_t> ref_pos;          // n_entries: instance-local CSR position or -1
+  std::vector<int64_t> ref_pos_diag;     // n_rows: CSR position of (i,i) or -1
   std::vector<double> lumped, bath;      // n_rows
   std::vector<int64_t> old_of_new;       // n_rows: instance-local old index or -1
   std::vector<std::vector<int>> new_of_old;   // per instance, global row index

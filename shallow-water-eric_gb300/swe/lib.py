@@ -35,7 +35,7 @@ EXPORTS = [
     "swe_sizes", "swe_get_matrices", "swe_compute_dij", "swe_euler", "swe_euler_intermediates",
     "swe_fct_positivity", "swe_upload", "swe_download", "swe_upload_device", "swe_download_device",
     "swe_set_time", "swe_rk3_steps", "swe_mass", "swe_last_launch_count", "swe_tuning",
-    "swe_last_device_ms", "swe_profile_kernels", "swe_fct_positivity_noalloc",
+    "swe_last_device_ms", "swe_profile_kernels", "swe_fct_positivity_noalloc", "swe_autotune",
 ]
 NOALLOC_MAX_NODES = 1 << 20   # SWE_NOALLOC_MAX_NODES
 KERNEL_KINDS = ("dt", "node", "low", "fct", "update")
@@ -88,6 +88,7 @@ def load(build: bool = True):
         "swe_last_launch_count": ([vp], ctypes.c_longlong),
         "swe_tuning": ([vp], ctypes.c_char_p),
         "swe_last_device_ms": ([vp], ctypes.c_double),
+        "swe_autotune": ([vp], ctypes.c_int),
         "swe_profile_kernels": ([vp, ctypes.c_int, dp], ctypes.c_int),
         "swe_fct_positivity_noalloc": ([ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p],

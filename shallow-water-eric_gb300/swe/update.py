@@ -199,6 +199,10 @@ class Update:
         self._check(self._L.swe_profile_kernels(self.h, nsteps, _L.dp(out)))
         return dict(zip(_L.KERNEL_KINDS, out.tolist()))
 
+    def autotune(self):
+        self._check(self._L.swe_autotune(self.h))
+        return self.tuning
+
     @property
     def tuning(self):
         return self._L.swe_tuning(self.h).decode()
