@@ -366,13 +366,21 @@ def run_thacker(args):
             rj, rg = o.gauss()
             lump = o.matrices()["lumped"]
             out = {}
-            for prec in (0, 1):
-                u, v, n, upd = _run_case(case, prec)
-                tfin = float(upd.rk3_steps(0)[0][0])
-                upd.close()
-                ex = case.exact(1, rg, tfin)
-                err = o.norms(u[0], ex)[0] / o.norms(np.zeros(o.np), ex)[0]
-                out[prec] = (u, v, n, err)
+            from swe.lib import SweError
+            try:
+                for prec in (0, 1):
+                    u, v, n, upd = _run_case(case, prec)
+                    tfin = float(upd.rk3_steps(0)[0][0])
+                    upd.close()
+                    ex = case.exact(1, rg, tfin)
+                    err = o.norms(u[0], ex)[0] / o.norms(np.zeros(o.np), ex)[0]
+                    out[prec] = (u, v, n, err)
+            except SweError as e:
+                # the reference STOPs as well (check_hmin) on such meshes
+                rows.append({"spacing": hsp, "film_htiny": film, "nodes": o.np,
+                             "stopped": f"{'FP64' if prec == 0 else 'mixed'} run: {e}"})
+                log(f"thacker h={hsp} film={film}: stopped ({e})")
+                continue
             u64, v64, n64, e64 = out[0]
             umx, vmx, nmx, emx = out[1]
             dmx = float(np.sum(lump * np.abs(umx[0] - u64[0])) / np.sum(lump * np.abs(u64[0])))

@@ -171,8 +171,8 @@ enum { SWE_NKERNELS = 5 };
 int swe_profile_kernels(swe_ctx* ctx, int nsteps, double* ms_out);
 
 /* Autotuner: times every block-size / entry-batch variant of the mixed
- * kernels on the current state and keeps the fastest per kernel (all variants
- * give the same results).  swe_rk3_steps runs it on its first call unless the
+ * kernels on the current state and keeps the fastest per kernel (variants
+ * agree to FP32 rounding).  swe_rk3_steps runs it on its first call unless the
  * environment sets SWE_AUTOTUNE=0.  swe_tuning names the chosen
  * configuration. */
 int swe_autotune(swe_ctx* ctx);

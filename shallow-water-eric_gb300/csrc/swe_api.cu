@@ -735,8 +735,8 @@ SWE_API int swe_set_time(swe_ctx* c, const double* time, const double* t_final) 
 
 // Autotuner of the mixed kernels: for every kernel kind, time each (block
 // size, entry batch) variant on the current state and keep the fastest.  The
-// variants compute identical results and every timed kernel is idempotent on
-// its inputs (it only rewrites its own outputs), so the state is unchanged.
+// variants agree to FP32 rounding, and every timed kernel is idempotent on its
+// inputs (it only rewrites its own outputs), so the state is unchanged.
 static int autotune(swe_ctx* c) {
   if (c->precision != SWE_PREC_MIXED) { c->tuned = true; return SWE_OK; }
   int rc;

@@ -81,8 +81,9 @@ void launch_mass_f64(const Graph& G, const double* h, double* acc, cudaStream_t 
 
 // Launch configuration of the mixed kernels, per kernel kind (0 dt, 1 node,
 // 2 low, 3 fct, 4 update): block size and entry batch (1, 2 or 4; 1 or 2 for
-// low).  Chosen by the autotuner in swe_api.cu; every choice gives the same
-// results.
+// low).  Chosen by the autotuner in swe_api.cu.  Every choice sums in the same
+// entry order; the batch variants are separate instantiations whose FMA
+// contraction may differ, so results agree to FP32 rounding.
 struct KernelTune {
   int block[5] = {128, 128, 128, 128, 128};
   int batch[5] = {1, 1, 1, 1, 1};

@@ -60,8 +60,9 @@ __device__ __forceinline__ float fct_from(float dd, float dm, float hi, float hj
 
 // Entry loops are processed in batches of B entries: every load of a batch is
 // issued before any of them is used, so a thread keeps B gathers in flight
-// (the kernels are latency-bound otherwise).  Sums keep the entry order, so
-// every batch size gives the same result; the autotuner picks B per kernel.
+// (the kernels are latency-bound otherwise).  Sums keep the entry order; the
+// instantiations may contract FMAs differently, so batch sizes agree to FP32
+// rounding.  The autotuner picks B per kernel.
 
 // k_node_mix: alpha_i (SOURCES/update.f90:758-781) from the FP32 depth.
 template <int B>

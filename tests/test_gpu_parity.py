@@ -316,5 +316,9 @@ def test_autotuned_variants_agree(monkeypatch):
         upd.rk3_steps(20)
         outs.append(upd.download())
         assert ("autotuned" in upd.tuning) == (env == "1")
+    # variants are separate template instantiations: FMA contraction may
+    # differ, so they agree to FP32 rounding rather than bit for bit
+    lump = upd.lumped
+    assert _rel_l1(outs[1][0], outs[0][0], lump) <= 1e-6
     scale = np.abs(outs[0]).max(axis=1, keepdims=True) + 1e-300
-    assert np.max(np.abs(outs[0] - outs[1]) / scale) <= 1e-6
+    assert np.max(np.abs(outs[0] - outs[1]) / scale) <= 1e-5
