@@ -100,6 +100,12 @@ static InstConst make_const(const swe_params& p) {
   k.rescale_floor = 1.e-10 * p.gravity * (p.max_water_h * p.max_water_h);   // update.f90:866
   k.type_test = p.type_test; k.S = p.syst_size; k.visc = p.viscosity_type; k.viscous_type = p.viscous_type;
   k.alpha_limit = p.if_alpha_limit; k.roundoff_fix = p.if_roundoff_fix;
+  k.gf = (float)k.g;
+  k.htinyf = (float)k.htiny;
+  k.htiny_lo = (float)(k.htiny - (double)k.htinyf);
+  k.fricf = (float)(k.g * k.mannings * k.mannings);
+  k.lambda_sgnf = (float)k.lambda_sgn;
+  k.rescale_floorf = (float)k.rescale_floor;
   return k;
 }
 
@@ -124,7 +130,7 @@ static int alloc_state_f64(swe_ctx* c, StateF64& s, cudaError_t& st) {
 
 static int alloc_state_mix(swe_ctx* c, StateMix& s, cudaError_t& st) {
   const size_t n = c->L.n_rows;
-  s.h = c->buf.alloc<double>(n, st);
+  s.h = c->buf.alloc<float2>(n, st);
   s.nq = c->buf.alloc<float4>(n, st);
   if (c->S == 5) { s.q3 = c->buf.alloc<float>(n, st); s.q4 = c->buf.alloc<float>(n, st); }
   return st == cudaSuccess ? SWE_OK : SWE_ERR_CUDA;
@@ -152,6 +158,12 @@ static int build_device(swe_ctx* c, const std::vector<std::vector<double>>& bath
   std::vector<double> inv(L.n_rows);
   for (int64_t r = 0; r < L.n_rows; r++) inv[r] = 1.0 / L.lumped[r];
   G.inv_lumped = upload_vec(c, inv, st);
+  if (c->precision == SWE_PREC_MIXED) {
+    std::vector<float> lf(L.n_rows), ilf(L.n_rows);
+    for (int64_t r = 0; r < L.n_rows; r++) { lf[r] = (float)L.lumped[r]; ilf[r] = (float)inv[r]; }
+    G.lumpedf = upload_vec(c, lf, st);
+    G.inv_lumpedf = upload_vec(c, ilf, st);
+  }
   G.bath = upload_vec(c, L.bath, st);
   if (c->precision == SWE_PREC_FP64) {
     G.cx = upload_vec(c, L.cx, st);
@@ -185,8 +197,7 @@ static int build_device(swe_ctx* c, const std::vector<std::vector<double>>& bath
   for (int b = 0; b < c->n_inst; b++) {
     hc[b] = make_const(c->params[b]);
     hs[b] = InstState{};
-    hs[b].dt = c->params[b].dt;
-    hs[b].inv_dt = c->params[b].dt > 0 ? 1.0 / c->params[b].dt : 0.0;
+    inst_set_dt(hs[b], c->params[b].dt);
     hs[b].t_final = 1e300;
   }
   c->d_C = upload_vec(c, hc, st);
@@ -216,9 +227,9 @@ static int build_device(swe_ctx* c, const std::vector<std::vector<double>>& bath
     alloc_state_mix(c, c->mA, st); alloc_state_mix(c, c->mB, st); alloc_state_mix(c, c->mC, st);
     WorkMix& w = c->wm;
     w.alpha = c->buf.alloc<float>(n, st); w.res = c->buf.alloc<float>(n, st);
-    w.rminus = c->buf.alloc<double>(n, st);
+    w.rminus = c->buf.alloc<float>(n, st); w.rneg = c->buf.alloc<float>(n, st);
     w.dL = c->buf.alloc<float>(ne, st); w.muL = c->buf.alloc<float>(ne, st);
-    w.hL = c->buf.alloc<double>(n, st);
+    w.hL = c->buf.alloc<float2>(n, st);
     w.qL = c->buf.alloc<float2>(n, st);
     if (c->S == 5) { w.q3L = c->buf.alloc<float>(n, st); w.q4L = c->buf.alloc<float>(n, st); }
   }
@@ -250,7 +261,7 @@ __global__ void k_scatter_in_mix(const double* __restrict__ stage, const int* __
   if (n >= n_nodes) return;
   const int64_t r = row_of_node[n];
   const double h = stage[n * S];
-  a.h[r] = h;
+  a.h[r] = df_from_double(h);
   a.nq[r] = make_float4(shadow_depth(h, C[slice_inst[r >> 5]].htiny), (float)stage[n * S + 1],
                         (float)stage[n * S + 2], bathf[r]);
   if (S == 5) { a.q3[r] = (float)stage[n * S + 3]; a.q4[r] = (float)stage[n * S + 4]; }
@@ -263,13 +274,13 @@ __global__ void k_gather_out_mix(double* __restrict__ stage, const int* __restri
   const int64_t r = row_of_node[n];
   if (!low) {
     const float4 v = a.nq[r];
-    stage[n * S] = a.h[r];
+    stage[n * S] = df_to_double(a.h[r]);
     stage[n * S + 1] = v.y;
     stage[n * S + 2] = v.z;
     if (S == 5) { stage[n * S + 3] = a.q3[r]; stage[n * S + 4] = a.q4[r]; }
   } else {
     const float2 v = w.qL[r];
-    stage[n * S] = w.hL[r];
+    stage[n * S] = df_to_double(w.hL[r]);
     stage[n * S + 1] = v.x;
     stage[n * S + 2] = v.y;
     if (S == 5) { stage[n * S + 3] = w.q3L[r]; stage[n * S + 4] = w.q4L[r]; }
@@ -325,7 +336,7 @@ static int set_inst_state_dt(swe_ctx* c, int inst, double dt, int done_others) {
   CK(cudaMemcpyAsync(hs.data(), c->d_St, sizeof(InstState) * c->n_inst, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   for (int b = 0; b < c->n_inst; b++) {
-    if (b == inst) { hs[b].dt = dt; hs[b].inv_dt = 1.0 / dt; hs[b].done = 0; }
+    if (b == inst) { inst_set_dt(hs[b], dt); hs[b].done = 0; }
     else if (done_others) hs[b].done = 1;
   }
   CK(cudaMemcpyAsync(c->d_St, hs.data(), sizeof(InstState) * c->n_inst, cudaMemcpyHostToDevice, c->stream));
@@ -478,8 +489,7 @@ SWE_API int swe_set_params(swe_ctx* c, int inst, const swe_params* p) {
   CK(cudaMemcpyAsync(c->d_C + inst, &k, sizeof(InstConst), cudaMemcpyHostToDevice, c->stream));
   std::vector<InstState> hs;
   if ((rc = save_state(c, hs))) return rc;
-  hs[inst].dt = p->dt;
-  hs[inst].inv_dt = p->dt > 0 ? 1.0 / p->dt : 0.0;
+  inst_set_dt(hs[inst], p->dt);
   return restore_done(c, hs);
 }
 
@@ -743,7 +753,7 @@ static int autotune(swe_ctx* c) {
   std::vector<InstState> saved;
   if ((rc = save_state(c, saved))) return rc;
   std::vector<InstState> run = saved;
-  for (auto& st : run) { st.done = 0; if (!(st.dt > 0)) { st.dt = 1e-6; st.inv_dt = 1e6; } }
+  for (auto& st : run) { st.done = 0; if (!(st.dt > 0)) inst_set_dt(st, 1e-6); }
   if ((rc = restore_done(c, run))) return rc;
   const cudaStream_t s = c->stream;
   StageArgsMix a{c->G, c->d_C, c->d_St, c->mA, c->mA, c->mB, c->wm, 1, c->d_err, c->block};
@@ -868,7 +878,8 @@ SWE_API int swe_profile_kernels(swe_ctx* c, int nsteps, double* ms_out) {
 SWE_API int swe_mass(swe_ctx* c, double* mass_out) {
   if (!c || !mass_out) return fail(c, SWE_ERR_ARG, "bad arguments");
   CK(cudaMemsetAsync(c->d_mass_acc, 0, 2 * sizeof(double) * c->n_inst, c->stream));
-  launch_mass_f64(c->G, c->precision == SWE_PREC_FP64 ? c->A.h : c->mA.h, c->d_mass_acc, c->stream);
+  if (c->precision == SWE_PREC_FP64) launch_mass_f64(c->G, c->A.h, c->d_mass_acc, c->stream);
+  else launch_mass_mix(c->G, c->mA.h, c->d_mass_acc, c->stream);
   CK(cudaGetLastError());
   std::vector<double> acc(2 * c->n_inst);
   CK(cudaMemcpyAsync(acc.data(), c->d_mass_acc, acc.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));

@@ -10,10 +10,15 @@ namespace swe {
 // SWE_ERR_* after each launch sequence.
 enum : unsigned { ERRB_NEG_H = 1u, ERRB_DELTA = 2u, ERRB_NAN = 4u };
 
-// Per-instance constants (one record per mesh of a batch).
+// Per-instance constants (one record per mesh of a batch).  The FP32 copies
+// are rounded once on the host: the mixed kernels never convert per row
+// (a float<->double conversion issues on GB300's narrow FP64 pipe).
 struct InstConst {
   double g, htiny, cfl, mannings, lambda_sgn, max_water_h, rescale_floor;
   int type_test, S, visc, viscous_type, alpha_limit, roundoff_fix;
+  float gf, htinyf, htiny_lo;      // htiny = htinyf + htiny_lo (double-float)
+  float fricf;                     // g n^2 (friction)
+  float lambda_sgnf, rescale_floorf;
 };
 
 // Per-instance time-loop state, device resident.
@@ -21,7 +26,15 @@ struct InstState {
   double dt, inv_dt, time, t_final;
   unsigned long long maxd_bits;   // max |d_ii|/m_i of the current step (double bits)
   int done, steps;
+  float dtf, inv_dtf;             // FP32 copies of dt and inv_dt
 };
+
+__host__ __device__ inline void inst_set_dt(InstState& s, double dt) {
+  s.dt = dt;
+  s.inv_dt = dt > 0.0 ? 1.0 / dt : 0.0;
+  s.dtf = (float)s.dt;
+  s.inv_dtf = (float)s.inv_dt;
+}
 
 // The SELL-32 edge graph (see swe_setup.hpp).  Entry k of row r is at
 // slice_ptr[r>>5] + 32*k + (r&31); entries are the off-diagonal CSR entries
@@ -44,6 +57,8 @@ struct Graph {
   const float* __restrict__ cyiif;
   const double* __restrict__ lumped;
   const double* __restrict__ inv_lumped;
+  const float* __restrict__ lumpedf;      // FP32 copies (mixed path)
+  const float* __restrict__ inv_lumpedf;
   const double* __restrict__ bath;
   const float* __restrict__ bathf;
   const uint8_t* __restrict__ dir_mask;   // bit k: component k is Dirichlet
@@ -64,6 +79,45 @@ __device__ __forceinline__ float shadow_depth(double h, double htiny) {
   if (h > 0.0 && !(f > 0.0f)) f = 1.17549435e-38f;   // smallest normal (FTZ-safe)
   return f;
 }
+
+// ---- double-float arithmetic (value = x + y, two FP32 words, |y| <= ulp(x)/2)
+// Knuth's two-sum and the FMA two-product, written with explicit roundings so
+// that no contraction changes them.  About 48 significant bits; every
+// operation issues on the FP32 pipes.
+__device__ __forceinline__ float2 two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return make_float2(s, e);
+}
+__device__ __forceinline__ float2 df_from_double(double v) {
+  const float hi = __double2float_rn(v);
+  return make_float2(hi, __double2float_rn(v - (double)hi));
+}
+__device__ __forceinline__ double df_to_double(float2 a) { return (double)a.x + (double)a.y; }
+__device__ __forceinline__ float2 df_add_f(float2 a, float b) {     // a + b
+  const float2 t = two_sum(a.x, b);
+  return two_sum(t.x, __fadd_rn(t.y, a.y));
+}
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {      // a + b
+  const float2 t = two_sum(a.x, b.x);
+  return two_sum(t.x, __fadd_rn(t.y, __fadd_rn(a.y, b.y)));
+}
+__device__ __forceinline__ float2 df_mul_f(float2 a, float b) {     // a * b
+  const float p = __fmul_rn(a.x, b);
+  const float e = __fmaf_rn(a.y, b, __fmaf_rn(a.x, b, -p));
+  return two_sum(p, e);
+}
+__device__ __forceinline__ float2 df_scale(float2 a, float pow2) {  // a * 2^k, exact
+  return make_float2(__fmul_rn(a.x, pow2), __fmul_rn(a.y, pow2));
+}
+__device__ __forceinline__ float2 df_div3(float2 a) {               // a / 3
+  const float q1 = __fdiv_rn(a.x, 3.0f);
+  const float r = __fadd_rn(__fmaf_rn(-3.0f, q1, a.x), a.y);      // a.x - 3 q1 is exact
+  return two_sum(q1, __fdiv_rn(r, 3.0f));
+}
+// a > (hi + lo) for normalised pairs
+__device__ __forceinline__ bool df_gt(float2 a, float hi, float lo) { return a.x > hi || (a.x == hi && a.y > lo); }
 
 template <typename T> __device__ __forceinline__ T tmax(T a, T b) { return a > b ? a : b; }
 template <typename T> __device__ __forceinline__ T tmin(T a, T b) { return a < b ? a : b; }

@@ -13,11 +13,12 @@ struct StateF64 {
   double* q4;
 };
 
-// Mixed-precision state: h in FP64 (positivity and mass) plus a packed FP32
-// node record {h shadow, qx, qy, z} that neighbours gather with one 16-byte
-// load; type 13's h*eta and h*w in FP32.
+// Mixed-precision state: h as a double-float pair (hi + lo, about 48
+// significant bits: positivity and mass) plus a packed FP32 node record
+// {h shadow, qx, qy, z} that neighbours gather with one 16-byte load; type
+// 13's h*eta and h*w in FP32.
 struct StateMix {
-  double* h;
+  float2* h;
   float4* nq;
   float* q3;
   float* q4;
@@ -34,9 +35,10 @@ struct WorkF64 {
 
 struct WorkMix {
   float *alpha, *res;                    // per row
-  double* rminus;                        // per row (FP64 limiter)
+  float* rminus;                         // per row: R^-_i
+  float* rneg;                           // per row: R^-_i * sum_{f_ij<0} f_ij
   float *dL, *muL;                       // per entry
-  double* hL;                            // low-order depth (FP64)
+  float2* hL;                            // low-order depth (double-float)
   float2* qL;                            // low-order momenta
   float *q3L, *q4L;                      // low-order h*eta, h*w (type 13)
 };
@@ -94,6 +96,7 @@ void launch_kernel_mix(int kind, const StageArgsMix& a, const KernelTune& t, cud
 void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, unsigned* err,
                    const KernelTune& t, cudaStream_t s);
 void launch_refresh_z(const Graph& G, StateMix u, cudaStream_t s);
+void launch_mass_mix(const Graph& G, const float2* h, double* acc, cudaStream_t s);
 
 // kernels launched per stage / per step (for launch accounting)
 constexpr int kLaunchesPerStage = 4;

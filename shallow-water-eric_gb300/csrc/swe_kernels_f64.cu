@@ -508,8 +508,7 @@ __global__ void k_step_begin(const InstConst* __restrict__ C, InstState* __restr
   if (s.done) return;
   if (!(s.time < s.t_final)) { s.done = 1; return; }
   double mx = __longlong_as_double((long long)s.maxd_bits);
-  s.dt = C[b].cfl * 1 / mx;
-  s.inv_dt = 1.0 / s.dt;
+  inst_set_dt(s, C[b].cfl * 1 / mx);
   s.maxd_bits = 0ull;
 }
 

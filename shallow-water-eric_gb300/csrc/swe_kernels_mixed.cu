@@ -1,15 +1,27 @@
-// Mixed FP32/FP64 stage kernels.
+// Mixed-precision stage kernels: every per-edge and per-row operation issues
+// on the FP32 pipes.
 //
-// Same sweep structure as the FP64 path (one thread per row, SELL-32 graph,
-// entries in reference order) but the bulk flux, lambda_max, viscosity,
-// entropy-residual and antidiffusion arithmetic runs in FP32 on FP32 data
-// (q, z, c_ij, d_ij, mu_ij, and an FP32 shadow of h).  FP64 is kept only
-// where positivity and mass need it, all per node:
-//   * the low-order depth h^L = h (1 + dt fix/m) + dt rk_1/m,
-//   * the limiter's Q^-, P^-, R^- and the h-row sum  sum_j l_ij f_ij,
-//   * the new depth h = h^L + dt/m sum_j l_ij f_ij and its RK combination.
-// FP64 throughput on GB300 is ~1/70 of FP32, so FP64 is used per edge only in
-// the P^- and l_ij f_ij accumulations.
+// Same sweep structure as the FP64 path (one thread per row, SELL-32 graph)
+// with the flux, lambda_max, viscosity, entropy-residual and antidiffusion
+// arithmetic in FP32 on FP32 data (q, z, c_ij, d_ij, mu_ij and an FP32 shadow
+// of h).  A warp-wide FP64 instruction, or a float<->double conversion, costs
+// GB300 tens of SM cycles (FP64 runs at ~1/64 of the FP32 rate), and a design
+// that kept the limiter sums and the per-row depth updates in FP64 measured
+// its FP64 pipe 73-79% busy in the limiter and update sweeps.  The precision
+// the scheme needs is kept without FP64:
+//   * the depth h (state, low-order h^L, new depth, RK combination) is a
+//     double-float pair hi + lo (about 48 significant bits), so the FP32
+//     increments of a stage are never lost to the rounding of h;
+//   * h^L = h + a (fix h + rk_1) with a = dt/m_i: non-negative in any
+//     rounding, because a |fix| <= CFL < 1 and rk_1 >= 0 (SOURCES/update.f90:
+//     202-215);
+//   * the limiter R^-_i = min(1, (1 - 2^-18) Q^-_i / P^-_i) (fct.f90:15-30) is
+//     FP32; the 2^-18 margin (64 units in the last place) bounds the at most
+//     ~12 roundings between the limiter and the depth update, so the limited
+//     update cannot take more than h^L out of a node (see k_fct_mix);
+//   * the reference's threshold tests (h <= htiny, h <= 0) use an FP32 shadow
+//     of h that keeps both decisions exact, and m h^L/dt <= htiny is decided in
+//     FP64 inside a 1e-5 band around htiny.
 //
 // Node data that neighbours gather is packed per node as float4
 // {h shadow, qx, qy, z}: one 16-byte load (one L2 sector) per neighbour.
@@ -29,6 +41,17 @@ __device__ __forceinline__ float dotc(float cx, float cy, float vx, float vy) {
 __device__ __forceinline__ float ovh_f(float h, float htiny) {
   float mh = fmaxf(h, htiny);
   return fdiv(2.0f * h, __fmaf_rn(h, h, __fmul_rn(mh, mh)));
+}
+
+// FP32 shadow of a double-float depth that keeps the sign of (h - htiny) and
+// of h (the mixed kernels branch on h <= htiny and h <= 0 with it).
+__device__ __forceinline__ float shadow_df(float2 h, const InstConst& c) {
+  float f = h.x;
+  const bool above = df_gt(h, c.htinyf, c.htiny_lo);
+  if (above && !(f > c.htinyf)) f = nextafterf(c.htinyf, 3.4e38f);
+  if (!above && f > c.htinyf) f = c.htinyf;
+  if (!(f > 0.0f) && (h.x > 0.0f || h.y > 0.0f)) f = 1.17549435e-38f;   // smallest normal (FTZ-safe)
+  return f;
 }
 
 // Hydrostatic reconstruction H*_ij = max(0, h_i + z_i - max(z_i, z_j))
@@ -51,11 +74,69 @@ __device__ __forceinline__ Recon recon(float hi, float hj, float dz, float invhi
 __device__ __forceinline__ float inv_pos(float h) { return (h > 0.f) ? fdiv(1.0f, h) : 0.f; }
 
 // antidiffusive h-flux f_ij of compute_fct_matrix (update.f90:744-745) with
-// explicit roundings: k_fct (P^-) and k_update (sum l f) must see the same f.
+// explicit roundings: k_fct and k_update must see the same f, bit for bit.
 __device__ __forceinline__ float fct_from(float dd, float dm, float hi, float hj, const Recon& R) {
   const float a = __fsub_rn(__fmul_rn(hj, R.rji), __fmul_rn(hi, R.rij));
   const float b = __fsub_rn(__fmul_rn(hj, __fsub_rn(1.f, R.rji)), __fmul_rn(hi, __fsub_rn(1.f, R.rij)));
   return __fadd_rn(__fmul_rn(dd, a), __fmul_rn(dm, b));
+}
+
+// ---- lambda_max of the two-rarefaction bound (condlim.f90:879-981) in FP32.
+// Per-node inputs are formed once and reused: the normal velocities come from
+// the c.v products that mu_ij needs anyway, sqrt(g h) of both states, and
+// sqrt(h) = sqrt(g h) / sqrt(g).
+struct LamK {
+  float g, htiny, rsg;   // rsg = 1/sqrt(g)
+};
+__device__ __forceinline__ LamK lam_k(float g, float htiny) { return LamK{g, htiny, rsqrtf(g)}; }
+
+// phi (condlim.f90:960-981); one_over_h(h) and sqrt(g h) are shared by the
+// two sides
+__device__ __forceinline__ float phi_f(float h, float vl, float hl, float vr, float hr, float ovhl, float ovhr,
+                                       float sql, float sqr, const LamK& k) {
+  const float ovh = ovh_f(h, k.htiny);
+  const float sgh = sqrtf(k.g * h);
+  const float fl = (h > hl) ? (h - hl) * sqrtf(0.5f * k.g * (ovh + ovhl)) : 2.f * (sgh - sql);
+  const float fr = (h > hr) ? (h - hr) * sqrtf(0.5f * k.g * (ovh + ovhr)) : 2.f * (sgh - sqr);
+  return fl + fr + vr - vl;
+}
+
+// compute_lambda_vacc (condlim.f90:879-957).  vl, vr: normal velocities;
+// ovh*: one_over_h of the states; sq*: sqrt(g |h|).  Returns false where the
+// reference STOPs (Delta < 0), with a relative band of 1e-5 h_min for FP32
+// rounding.
+__device__ __forceinline__ bool lambda_f(float hl, float hr, float vl, float vr, float ovhl, float ovhr, float sql,
+                                         float sqr, const LamK& k, float* lambda) {
+  const float x0 = 3.34314575f;   // (2 sqrt(2) - 1)^2
+  const bool lmin = hl <= hr;
+  const float hmin = lmin ? hl : hr, hmax = lmin ? hr : hl;
+  bool ok = true;
+  float ht;
+  float fh = phi_f(x0 * hmin, vl, hl, vr, hr, ovhl, ovhr, sql, sqr, k);
+  if (0.f <= fh) {
+    const float s = fmaxf(vl - vr + 2.f * sql + 2.f * sqr, 0.f);
+    ht = fminf(x0 * hmin, fdiv(s * s, 16.f * k.g));
+  } else {
+    fh = phi_f(x0 * hmax, vl, hl, vr, hr, ovhl, ovhr, sql, sqr, k);
+    const float sqrmin = (lmin ? sql : sqr) * k.rsg, sqrmax = (lmin ? sqr : sql) * k.rsg;
+    if (0.f <= fh) {
+      const float a = 0.353553391f;   // 1 / (2 sqrt(2))
+      const float cc = -(hmin * a) - sqrmin * sqrmax + sqrmin * (vr - vl) * (0.5f * k.rsg);
+      float Delta = hmin - 4.f * a * cc;
+      if (Delta < 0.f) {
+        if (Delta < -1e-5f * hmin) ok = false;
+        Delta = 0.f;
+      }
+      const float s = (sqrtf(Delta) - sqrmin) * 1.41421356f;   // / (2a)
+      ht = fminf(x0 * hmax, s * s);
+    } else {
+      ht = sqrmin * sqrmax * (1.f + 1.41421356f * k.rsg * fdiv(vl - vr, sqrmin + sqrmax));
+    }
+  }
+  const float lbdl = vl - sql * sqrtf((1.f + fmaxf((ht - hl) * ovhl * 0.5f, 0.f)) * (1.f + fmaxf((ht - hl) * ovhl, 0.f)));
+  const float lbdr = vr + sqr * sqrtf((1.f + fmaxf((ht - hr) * ovhr * 0.5f, 0.f)) * (1.f + fmaxf((ht - hr) * ovhr, 0.f)));
+  *lambda = fmaxf(fabsf(lbdl), fabsf(lbdr));
+  return ok;
 }
 
 // Entry loops are processed in batches of B entries: every load of a batch is
@@ -79,7 +160,7 @@ __global__ void __launch_bounds__(256) k_node_mix(Graph G, const InstConst* __re
   const float* hs = reinterpret_cast<const float*>(u.nq);
   const float h = hs[4 * r];
   float alpha = 1.0f;
-  if (c.alpha_limit && !(h <= (float)c.htiny)) {
+  if (c.alpha_limit && !(h <= c.htinyf)) {
     const int64_t base = entry_base(G, r);
     float num = 0.0f, denom = 0.0f;
     for (int k0 = 0; k0 < L; k0 += B) {
@@ -107,8 +188,7 @@ struct NodeF {   // FP32 view of one node used by the edge loop
   float h, q1, q2, z, ovh, v1, v2;
 };
 
-__device__ __forceinline__ NodeF load_node(const StateMix& u, int64_t j, float htiny) {
-  const float4 a = u.nq[j];
+__device__ __forceinline__ NodeF node_from(const float4 a, float htiny) {
   NodeF n;
   n.h = a.x; n.q1 = a.y; n.q2 = a.z; n.z = a.w;
   n.ovh = ovh_f(n.h, htiny);
@@ -128,9 +208,9 @@ __device__ __forceinline__ float sgn_pressure(float lambda_sgn, float g, float m
 // Galerkin RHS (smb_2) and the entropy stencil max/min, then the low-order
 // state and the entropy residual (SOURCES/update.f90:180-210, 291-364,
 // 554-682, 750-799, 825-878).  Each neighbour is loaded once, and c.v_j is
-// formed once and shared by mu_ij and the Galerkin flux.  The diagonal entry
-// only enters through terms that vanish identically (u_i rat_ii - u_i rat_ii)
-// and the Galerkin boundary term -c_ii.v_i.
+// formed once and shared by mu_ij, lambda_max and the Galerkin flux.  The
+// diagonal entry only enters through terms that vanish identically
+// (u_i rat_ii - u_i rat_ii) and the Galerkin boundary term -c_ii.v_i.
 template <int B>
 __global__ void __launch_bounds__(256) k_low_mix(Graph G, const InstConst* __restrict__ C,
                                                  const InstState* __restrict__ St, StateMix u,
@@ -142,18 +222,19 @@ __global__ void __launch_bounds__(256) k_low_mix(Graph G, const InstConst* __res
   const int L = G.len[r];
   if (L == 0) return;
   const int b = G.slice_inst[r >> 5];
-  const InstState st = St[b];
+  const InstState& st = St[b];
   if (st.done) return;
   const InstConst& c = C[b];
   const int S = c.S;
   const bool sgn = c.type_test == 13;
-  const float g = (float)c.g, htiny = (float)c.htiny, dtf = (float)st.dt;
-  const float sqrt2 = 1.41421356237309515f;
+  const float g = c.gf, htiny = c.htinyf, dtf = st.dtf;
+  const LamK lk = lam_k(g, htiny);
   const int64_t base = entry_base(G, r);
-  const NodeF ni = load_node(u, r, htiny);
+  const NodeF ni = node_from(u.nq[r], htiny);
+  const float sqi = sqrtf(g * fabsf(ni.h));
   const float v2i_flux = sgn ? 0.f : ni.v2;          // flux() zeroes velocity(2) for type 13
   const float ai = alpha[r];
-  const float m = (float)G.lumped[r];
+  const float m = G.lumpedf[r];
   float ui3 = 0.f, ui4 = 0.f;
   if (S == 5) { ui3 = u.q3[r]; ui4 = u.q4[r]; }
   const float invhi = inv_pos(ni.h);
@@ -176,7 +257,7 @@ __global__ void __launch_bounds__(256) k_low_mix(Graph G, const InstConst* __res
     g1 -= cvi * ni.q1; g2 -= cvi * ni.q2;
     if (S == 5) { rk3 -= cvi * ui3; rk4 -= cvi * ui4; g3 -= cvi * ui3; g4 -= cvi * ui4; }
     if (sgn) {
-      const float pt = sgn_pressure((float)c.lambda_sgn, g, m, ni.h, ui3);
+      const float pt = sgn_pressure(c.lambda_sgnf, g, m, ni.h, ui3);
       ptx -= pt * cxe;
       pty -= pt * cye;
     }
@@ -203,20 +284,17 @@ __global__ void __launch_bounds__(256) k_low_mix(Graph G, const InstConst* __res
     const int64_t e = base + 32 * (k0 + q);
     const float cxe = cxb[q], cye = cyb[q];
     const int j = jb[q];
-    NodeF nj;
-    nj.h = nqb[q].x; nj.q1 = nqb[q].y; nj.q2 = nqb[q].z; nj.z = nqb[q].w;
-    nj.ovh = ovh_f(nj.h, htiny);
-    nj.v1 = nj.q1 * nj.ovh;
-    nj.v2 = nj.q2 * nj.ovh;
+    const NodeF nj = node_from(nqb[q], htiny);
     // --- viscosities: compute_dij, compute_muij, MAX, alpha_limit
-    const float norm = sqrtf(cxe * cxe + cye * cye);
-    const float inv = fdiv(1.0f, norm);
+    const float n2 = cxe * cxe + cye * cye;
+    const float inv = rsqrtf(n2);
+    const float norm = n2 * inv;
+    const float cvi = dotc(cxe, cye, ni.v1, ni.v2);                   // c.v_i (compute_muij)
+    const float cvj = dotc(cxe, cye, nj.v1, nj.v2);                   // c.v_j
     float lam;
-    if (!lambda_vacc<float>(ni.h, ni.q1, ni.q2, ni.ovh, nj.h, nj.q1, nj.q2, nj.ovh, cxe * inv, cye * inv, g, htiny,
-                            sqrt2, &lam))
+    if (!lambda_f(ni.h, nj.h, cvi * inv, cvj * inv, ni.ovh, nj.ovh, sqi, sqrtf(g * fabsf(nj.h)), lk, &lam))
       delta_bad = true;
-    const float cvj = dotc(cxe, cye, nj.v1, nj.v2);                   // c.v_j (compute_muij)
-    float mu = fmaxf(fmaxf(-dotc(cxe, cye, ni.v1, ni.v2), 0.f), fmaxf(cvj, 0.f));
+    float mu = fmaxf(fmaxf(-cvi, 0.f), fmaxf(cvj, 0.f));
     float d = fmaxf(norm * lam, mu);
     if (c.alpha_limit) {
       const float s = fmaxf(ai, alb[q]);
@@ -257,7 +335,7 @@ __global__ void __launch_bounds__(256) k_low_mix(Graph G, const InstConst* __res
       g3 += -cvj_flux * uj3 + d * (uj3 * rji - ui3 * rij) + mu * (uj3 * (1.f - rji) - ui3 * (1.f - rij));
       g4 += -cvj_flux * uj4 + d * (uj4 * rji - ui4 * rij) + mu * (uj4 * (1.f - rji) - ui4 * (1.f - rij));
       if (sgn) {
-        const float pt = sgn_pressure((float)c.lambda_sgn, g, (float)G.lumped[j], nj.h, uj3);
+        const float pt = sgn_pressure(c.lambda_sgnf, g, G.lumpedf[j], nj.h, uj3);
         ptx -= pt * cxe;
         pty -= pt * cye;
       }
@@ -266,9 +344,8 @@ __global__ void __launch_bounds__(256) k_low_mix(Graph G, const InstConst* __res
   }
   // source terms (update.f90:425-551)
   if (c.type_test == 9 || c.type_test == 10) {
-    const float fric = (float)(c.g * c.mannings * c.mannings);
     const float hstar = __powf(fmaxf(ni.h, htiny), 4.0f / 3.0f);
-    const float vel = fric * sqrtf(ni.v1 * ni.v1 + ni.v2 * ni.v2);
+    const float vel = c.fricf * sqrtf(ni.v1 * ni.v1 + ni.v2 * ni.v2);
     const float hloc = vel * dtf;
     const float coef = fdiv(m * vel * 2.f, hstar + fmaxf(hstar, hloc));
     rk1 -= coef * ni.q1; rk2_ -= coef * ni.q2;
@@ -280,7 +357,7 @@ __global__ void __launch_bounds__(256) k_low_mix(Graph G, const InstConst* __res
     const float a1 = m * 2.0f * ni.q2, a2 = m * 2.0f * ni.q1;
     rk1 += a1; rk2_ -= a2; g1 += a1; g2 -= a2;
   } else if (sgn) {
-    const float pc = fdiv((float)c.lambda_sgn * g, 3.0f * sqrtf(m));
+    const float pc = fdiv(c.lambda_sgnf * g, 3.0f * sqrtf(m));
     const float t = fdiv(ui3, ni.h);
     const float x = fdiv(ui3, ni.h * ni.h);
     const float s_i = 3.f * pc * t * t * 12.f * (x - 1.f);
@@ -288,13 +365,17 @@ __global__ void __launch_bounds__(256) k_low_mix(Graph G, const InstConst* __res
     rk3 += m * ui4; rk4 -= m * s_i;
     g3 += m * ui4; g4 -= m * s_i;
   }
-  // low-order state: FP64 depth update, FP32 momenta
-  const double inv_m = G.inv_lumped[r];
-  const double dtd = st.dt;
-  double hL;
-  if (c.roundoff_fix) hL = u.h[r] * (1.0 + dtd * (double)fix * inv_m) + dtd * (double)rk0 * inv_m;
-  else hL = fmax(u.h[r] + dtd * (double)g0 * inv_m, 0.0);
-  const float invm = (float)inv_m;
+  // low-order state: double-float depth plus an FP32 increment
+  const float invm = G.inv_lumpedf[r];
+  const float a = dtf * invm;
+  const float2 h = u.h[r];
+  float2 hL;
+  if (c.roundoff_fix) {
+    hL = df_add_f(h, a * __fmaf_rn(fix, ni.h, rk0));   // h + a (fix h + rk_1), a |fix| <= CFL
+  } else {
+    hL = df_add_f(h, a * g0);
+    if (hL.x < 0.f) hL = make_float2(0.f, 0.f);
+  }
   w.hL[r] = hL;
   w.qL[r] = make_float2(ni.q1 + dtf * (rk1 * invm), ni.q2 + dtf * (rk2_ * invm));
   if (S == 5) { w.q3L[r] = ui3 + dtf * (rk3 * invm); w.q4L[r] = ui4 + dtf * (rk4 * invm); }
@@ -305,31 +386,42 @@ __global__ void __launch_bounds__(256) k_low_mix(Graph G, const InstConst* __res
   const float on = ovh_f(un0, htiny);
   const float En = 0.5f * (g * un0 * un0 + (un1 * on) * un1 + (un2 * on) * un2);
   const float Ep0 = g * ni.h - 0.5f * (ni.v1 * ni.v1) - 0.5f * (v2i_flux * v2i_flux);
-  float rs = m * fdiv(En - Ei, dtf);
+  float rs = m * (En - Ei) * st.inv_dtf;
   rs -= g0 * Ep0 + g1 * ni.v1 + g2 * v2i_flux;
-  const float rescale = 0.5f * fabsf(emax - emin) + (float)c.rescale_floor;
+  const float rescale = 0.5f * fabsf(emax - emin) + c.rescale_floorf;
   res[r] = fdiv(fabsf(rs), rescale);
   if (delta_bad) atomicOr(err, ERRB_DELTA);
 }
 
-// k_fct_mix: f_ij (FP32) and R^-_i (FP64 Q^-, P^-, R^-), fct.f90:15-30
+// Limiter margin: (1 - 2^-18) Q^-.  Between the limiter and the depth update
+// the negative part of sum_j l_ij f_ij passes through at most ~12 FP32
+// roundings (h^L to FP32, m and dt and their reciprocals, two products here,
+// the quotient, R P, the row sum and dt/m times it in k_update_mix), each at
+// most 2^-24 relative, so (1 - 2^-18)(1 + 2^-24)^12 < 1 and the update never
+// removes more than h^L from a node.
+constexpr float kLimiterShrink = 1.0f - 3.814697265625e-6f;
+
+// k_fct_mix: f_ij and the limiter R^-_i (fct.f90:15-30): P^- = sum f^- - 1e-15,
+// Q^- = -m h^L/dt, R^- = min(Q^-/P^-, 1), 0 where m h^L/dt <= htiny.  Also
+// stores R^-_i P_i (the limited negative part of the h-row, reused by the
+// update).
 template <int B>
 __global__ void __launch_bounds__(256) k_fct_mix(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St, StateMix u,
                           const float* __restrict__ dL, const float* __restrict__ muL, WorkMix w,
-                          const float* __restrict__ res, double* __restrict__ rminus, unsigned* __restrict__ err) {
+                          const float* __restrict__ res, unsigned* __restrict__ err) {
   int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= G.n_rows) return;
   const int L = G.len[r];
   if (L == 0) return;
   const int b = G.slice_inst[r >> 5];
-  const InstState st = St[b];
+  const InstState& st = St[b];
   if (st.done) return;
   const InstConst& c = C[b];
   const int64_t base = entry_base(G, r);
   const float4 ni = u.nq[r];
   const float hi = ni.x, zi = ni.w, resi = res[r];
   const float invhi = inv_pos(hi);
-  double P = -1.e-15;                    // f_ii = 0 adds nothing
+  float neg = 0.f;                       // f_ii = 0 adds nothing
   for (int k0 = 0; k0 < L; k0 += B) {
     int jb[B];
     float d0b[B], m0b[B];
@@ -353,32 +445,39 @@ __global__ void __launch_bounds__(256) k_fct_mix(Graph G, const InstConst* __res
       const float4 nj = njb[q];
       const Recon R = recon(hi, nj.x, nj.w - zi, invhi, inv_pos(nj.x));
       const float f = fct_from(fminf(d0, rij) - d0, fminf(m0, rij) - m0, hi, nj.x, R);
-      if (f < 0.f) P += (double)f;
+      if (f < 0.f) neg = __fadd_rn(neg, f);
     }
   }
-  const double hL = w.hL[r];
-  if (hL < 0.0) atomicOr(err, ERRB_NEG_H);
-  const double scaled = G.lumped[r] * st.inv_dt * hL;
-  // Q^-/P^- with Q^- shrunk by 4 ulp: the update multiplies by dt/m through
-  // reciprocals, and the limited sum must not overshoot -h^L by rounding
-  double R = fmin((0.0 - scaled) * (1.0 - 8.881784197001252e-16) / P, 1.0);
-  if (scaled <= c.htiny) R = 0.0;
-  rminus[r] = R;
+  const float2 hL = w.hL[r];
+  if (hL.x < 0.f) atomicOr(err, ERRB_NEG_H);
+  const float scaled = __fmul_rn(__fmul_rn(hL.x, G.lumpedf[r]), st.inv_dtf);   // m h^L / dt
+  bool dry = scaled <= c.htinyf;
+  if (fabsf(scaled - c.htinyf) <= 1e-5f * c.htinyf)                           // decide in FP64 near htiny
+    dry = G.lumped[r] * st.inv_dt * df_to_double(hL) <= c.htiny;
+  float R = 0.f;
+  if (!dry) {
+    const float mP = __fsub_rn(1.e-15f, neg);                                  // -P^- > 0
+    const float Q = __fmul_rn(scaled, kLimiterShrink);                         // -Q^- >= 0
+    R = (Q >= mP) ? 1.f : __fdiv_rn(Q, mP);
+  }
+  w.rminus[r] = R;
+  w.rneg[r] = __fmul_rn(R, neg);
 }
 
 // k_update_mix: limited antidiffusion (update.f90:276-282, apply_viscosity
-// :684-718), RK combination and Dirichlet data (main.f90:77-90).
+// :684-718), RK combination and Dirichlet data (main.f90:77-90).  The h-row
+// sum is R^-_i P_i (from k_fct_mix) plus sum_{f_ij >= 0} R^-_j f_ij.
 template <int B>
 __global__ void __launch_bounds__(256) k_update_mix(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St,
                              StateMix u, const float* __restrict__ dL, const float* __restrict__ muL, WorkMix w,
-                             const float* __restrict__ res, const double* __restrict__ rminus, StateMix u0,
-                             StateMix out, int rk_stage, unsigned* __restrict__ err) {
+                             const float* __restrict__ res, StateMix u0, StateMix out, int rk_stage,
+                             unsigned* __restrict__ err) {
   int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= G.n_rows) return;
   const int L = G.len[r];
   if (L == 0) return;
   const int b = G.slice_inst[r >> 5];
-  const InstState st = St[b];
+  const InstState& st = St[b];
   if (st.done) return;
   const InstConst& c = C[b];
   const int S = c.S;
@@ -386,10 +485,10 @@ __global__ void __launch_bounds__(256) k_update_mix(Graph G, const InstConst* __
   const float4 ni = u.nq[r];
   const float hi = ni.x, zi = ni.w, resi = res[r];
   const float invhi = inv_pos(hi);
-  const double Ri = rminus[r];
+  const float Ri = w.rminus[r];
   float ui3 = 0.f, ui4 = 0.f;
   if (S == 5) { ui3 = u.q3[r]; ui4 = u.q4[r]; }
-  double sh = 0.0;                       // sum_j l_ij f_ij (FP64)
+  float pos = 0.f;                       // sum_{f >= 0} R_j f_ij
   float x1 = 0.f, x2 = 0.f, x3 = 0.f, x4 = 0.f;
   for (int k0 = 0; k0 < L; k0 += B) {    // the diagonal's terms vanish: (u_i rat_ii - u_i rat_ii) = 0
    int jb[B];
@@ -404,10 +503,9 @@ __global__ void __launch_bounds__(256) k_update_mix(Graph G, const InstConst* __
      }
    }
    float4 njb[B];
-   float rsb[B];
-   double Rjb[B];
+   float rsb[B], Rjb[B];
 #pragma unroll
-   for (int q = 0; q < B; q++) { njb[q] = u.nq[jb[q]]; rsb[q] = res[jb[q]]; Rjb[q] = rminus[jb[q]]; }
+   for (int q = 0; q < B; q++) { njb[q] = u.nq[jb[q]]; rsb[q] = res[jb[q]]; Rjb[q] = w.rminus[jb[q]]; }
 #pragma unroll
    for (int q = 0; q < B; q++) {
     if (k0 + q >= L) break;
@@ -418,9 +516,8 @@ __global__ void __launch_bounds__(256) k_update_mix(Graph G, const InstConst* __
     const float ddr = fminf(d0, rij) - d0, dmr = fminf(m0, rij) - m0;
     const Recon R = recon(hi, nj.x, nj.w - zi, invhi, inv_pos(nj.x));
     const float f = fct_from(ddr, dmr, hi, nj.x, R);
-    const double l = (f >= 0.f) ? Rjb[q] : Ri;
-    sh += l * (double)f;
-    const float lf = (float)l;
+    float lf = Ri;
+    if (f >= 0.f) { lf = Rjb[q]; pos = __fmaf_rn(lf, f, pos); }
     const float dd = ddr * lf, dm = dmr * lf;
     x1 += dd * (nj.y * R.rji - ni.y * R.rij) + dm * (nj.y * (1.f - R.rji) - ni.y * (1.f - R.rij));
     x2 += dd * (nj.z * R.rji - ni.z * R.rij) + dm * (nj.z * (1.f - R.rji) - ni.z * (1.f - R.rij));
@@ -431,26 +528,26 @@ __global__ void __launch_bounds__(256) k_update_mix(Graph G, const InstConst* __
     }
    }
   }
-  const double inv_m = G.inv_lumped[r];
-  const float invm = (float)inv_m, dtf = (float)st.dt;
-  double hn = w.hL[r] + st.dt * (sh * inv_m);
+  const float invm = G.inv_lumpedf[r], dtf = st.dtf;
+  const float sh = __fadd_rn(w.rneg[r], pos);
+  float2 hn = df_add_f(w.hL[r], __fmul_rn(__fmul_rn(dtf, invm), sh));
   const float2 qL = w.qL[r];
   float q1 = qL.x + dtf * (x1 * invm);
   float q2 = qL.y + dtf * (x2 * invm);
   float q3 = 0.f, q4 = 0.f;
   if (S == 5) { q3 = w.q3L[r] + dtf * (x3 * invm); q4 = w.q4L[r] + dtf * (x4 * invm); }
-  if (hn < 0.0) atomicOr(err, ERRB_NEG_H);
-  if (!(hn == hn) || !(q1 == q1) || !(q2 == q2)) atomicOr(err, ERRB_NAN);
+  if (hn.x < 0.f) atomicOr(err, ERRB_NEG_H);
+  if (!(hn.x == hn.x) || !(q1 == q1) || !(q2 == q2)) atomicOr(err, ERRB_NAN);
   if (rk_stage >= 2) {
     const float4 a0 = u0.nq[r];
-    const double h0 = u0.h[r];
+    const float2 h0 = u0.h[r];
     if (rk_stage == 2) {
-      hn = (3.0 * h0 + hn) * 0.25;
+      hn = df_scale(df_add(df_mul_f(h0, 3.f), hn), 0.25f);
       q1 = (3.f * a0.y + q1) * 0.25f;
       q2 = (3.f * a0.z + q2) * 0.25f;
       if (S == 5) { q3 = (3.f * u0.q3[r] + q3) * 0.25f; q4 = (3.f * u0.q4[r] + q4) * 0.25f; }
     } else {
-      hn = (h0 + 2.0 * hn) * (1.0 / 3.0);
+      hn = df_div3(df_add(h0, df_scale(hn, 2.f)));
       q1 = (a0.y + 2.f * q1) * (1.f / 3.f);
       q2 = (a0.z + 2.f * q2) * (1.f / 3.f);
       if (S == 5) { q3 = (u0.q3[r] + 2.f * q3) * (1.f / 3.f); q4 = (u0.q4[r] + 2.f * q4) * (1.f / 3.f); }
@@ -459,7 +556,7 @@ __global__ void __launch_bounds__(256) k_update_mix(Graph G, const InstConst* __
   if (rk_stage >= 1 && G.dir_mask) {
     const unsigned msk = G.dir_mask[r];
     if (msk) {
-      if (msk & 1u) hn = G.dir_val[r];
+      if (msk & 1u) hn = df_from_double(G.dir_val[r]);
       if (msk & 2u) q1 = (float)G.dir_val[G.n_rows + r];
       if (msk & 4u) q2 = (float)G.dir_val[2 * G.n_rows + r];
       if (S == 5 && (msk & 8u)) q3 = (float)G.dir_val[3 * G.n_rows + r];
@@ -467,7 +564,7 @@ __global__ void __launch_bounds__(256) k_update_mix(Graph G, const InstConst* __
     }
   }
   out.h[r] = hn;
-  out.nq[r] = make_float4(shadow_depth(hn, c.htiny), q1, q2, zi);
+  out.nq[r] = make_float4(shadow_df(hn, c), q1, q2, zi);
   if (S == 5) { out.q3[r] = q3; out.q4[r] = q4; }
 }
 
@@ -481,11 +578,12 @@ __global__ void __launch_bounds__(256) k_dt_mix(Graph G, const InstConst* __rest
     const int b = G.slice_inst[r >> 5];
     if (!St[b].done) {
       const InstConst& c = C[b];
-      const float g = (float)c.g, htiny = (float)c.htiny;
+      const float g = c.gf, htiny = c.htinyf;
+      const LamK lk = lam_k(g, htiny);
       const int L = G.len[r];
       const int64_t base = entry_base(G, r);
-      const float4 ni = u.nq[r];
-      const float oi = ovh_f(ni.x, htiny);
+      const NodeF ni = node_from(u.nq[r], htiny);
+      const float sqi = sqrtf(g * fabsf(ni.h));
       float s = 0.f;
       bool bad = false;
       for (int k0 = 0; k0 < L; k0 += B) {
@@ -506,18 +604,18 @@ __global__ void __launch_bounds__(256) k_dt_mix(Graph G, const InstConst* __rest
 #pragma unroll
        for (int q = 0; q < B; q++) {
         if (k0 + q >= L) break;
-        const float4 nj = njb[q];
+        const NodeF nj = node_from(njb[q], htiny);
         const float cxe = cxb[q], cye = cyb[q];
-        const float norm = sqrtf(cxe * cxe + cye * cye);
-        const float inv = fdiv(1.0f, norm);
+        const float n2 = cxe * cxe + cye * cye;
+        const float inv = rsqrtf(n2);
         float lam;
-        if (!lambda_vacc<float>(ni.x, ni.y, ni.z, oi, nj.x, nj.y, nj.z, ovh_f(nj.x, htiny), cxe * inv, cye * inv, g,
-                                htiny, 1.41421356237309515f, &lam))
+        if (!lambda_f(ni.h, nj.h, dotc(cxe, cye, ni.v1, ni.v2) * inv, dotc(cxe, cye, nj.v1, nj.v2) * inv, ni.ovh,
+                      nj.ovh, sqi, sqrtf(g * fabsf(nj.h)), lk, &lam))
           bad = true;
-        s += norm * lam;
+        s += (n2 * inv) * lam;
        }
       }
-      val = s * (float)G.inv_lumped[r];
+      val = s * G.inv_lumpedf[r];
       if (bad) atomicOr(err, ERRB_DELTA);
     }
   }
@@ -535,6 +633,30 @@ __global__ void k_refresh_z(Graph G, StateMix u) {
   int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= G.n_rows) return;
   u.nq[r].w = G.bathf[r];
+}
+
+// Total mass sum m_i h_i per instance from the double-float depth, combined
+// in double-double per warp (atomics on two words per instance).
+__global__ void k_mass_mix(Graph G, const float2* __restrict__ h, double* __restrict__ acc) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double v = 0.0;
+  int b = -1;
+  if (r < G.n_rows && G.len[r] > 0) { b = G.slice_inst[r >> 5]; v = G.lumped[r] * df_to_double(h[r]); }
+  double cmp = 0.0;
+  for (int off = 16; off > 0; off >>= 1) {
+    const double o = __shfl_down_sync(0xffffffffu, v, off);
+    const double oc = __shfl_down_sync(0xffffffffu, cmp, off);
+    const double s = v + o;              // two-sum
+    const double bb = s - v;
+    const double e = (v - (s - bb)) + (o - bb);
+    v = s;
+    cmp = cmp + oc + e;
+  }
+  const int b0 = __shfl_sync(0xffffffffu, b, 0);
+  if ((threadIdx.x & 31) == 0 && b0 >= 0) {
+    atomicAdd(&acc[2 * b0], v);
+    atomicAdd(&acc[2 * b0 + 1], cmp);
+  }
 }
 
 static inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
@@ -562,10 +684,10 @@ void launch_kernel_mix(int kind, const StageArgsMix& a, const KernelTune& t, cud
                                                                        a.w, a.w.res, a.err);
             break;
     case 3: SWE_DISPATCH_B(t.batch[3], k_fct_mix, nblk(n, t.block[3]), t.block[3], a.G, a.C, a.St, a.u, a.w.dL,
-                           a.w.muL, a.w, a.w.res, a.w.rminus, a.err)
+                           a.w.muL, a.w, a.w.res, a.err)
             break;
     case 4: SWE_DISPATCH_B(t.batch[4], k_update_mix, nblk(n, t.block[4]), t.block[4], a.G, a.C, a.St, a.u, a.w.dL,
-                           a.w.muL, a.w, a.w.res, a.w.rminus, a.u0, a.out, a.rk_stage, a.err)
+                           a.w.muL, a.w, a.w.res, a.u0, a.out, a.rk_stage, a.err)
             break;
     default: break;
   }
@@ -586,6 +708,10 @@ void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const Stat
 
 void launch_refresh_z(const Graph& G, StateMix u, cudaStream_t s) {
   k_refresh_z<<<nblk(G.n_rows, 256), 256, 0, s>>>(G, u);
+}
+
+void launch_mass_mix(const Graph& G, const float2* h, double* acc, cudaStream_t s) {
+  k_mass_mix<<<nblk(G.n_rows, 256), 256, 0, s>>>(G, h, acc);
 }
 
 }  // namespace swe

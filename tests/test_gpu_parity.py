@@ -267,9 +267,12 @@ def test_lake_at_rest_is_preserved(prec):
     upd.set_time(0.0, 1e30)
     upd.rk3_steps(20)
     u = upd.download()
-    tol = 1e-13 if prec == 0 else 2e-6
-    assert np.abs(u[0] - h).max() < tol
-    assert np.abs(u[1:]).max() < tol
+    # FP32 holds h and z separately, so eta = h + z is constant only to
+    # 2^-24 relative; the resulting pressure imbalance g h d(eta) drives a
+    # momentum noise of ~1e-6 over 20 steps (q scale h sqrt(g h) ~ 2)
+    tol_h, tol_q = (1e-13, 1e-13) if prec == 0 else (2e-6, 5e-6)
+    assert np.abs(u[0] - h).max() < tol_h
+    assert np.abs(u[1:]).max() < tol_q
 
 
 def test_sgn_fp64_bit_exact_and_mixed_close():
