@@ -229,6 +229,7 @@ static int build_device(swe_ctx* c, const std::vector<std::vector<double>>& bath
     w.alpha = c->buf.alloc<float>(n, st); w.res = c->buf.alloc<float>(n, st);
     w.rminus = c->buf.alloc<float>(n, st); w.rneg = c->buf.alloc<float>(n, st);
     w.dL = c->buf.alloc<float>(ne, st); w.muL = c->buf.alloc<float>(ne, st);
+    w.dlam = c->buf.alloc<float>(ne, st);
     w.hL = c->buf.alloc<float2>(n, st);
     w.qL = c->buf.alloc<float2>(n, st);
     if (c->S == 5) { w.q3L = c->buf.alloc<float>(n, st); w.q4L = c->buf.alloc<float>(n, st); }
@@ -372,7 +373,7 @@ static void enqueue_step(swe_ctx* c, const KernelEvents* kev = nullptr, double* 
   if (kev) cudaEventRecord(kev->ev[0], s);
   if (c->precision == SWE_PREC_FP64)
     launch_dt_f64(c->G, c->d_C, c->d_St, c->A, nullptr, nullptr, c->d_err, c->block, s);
-  else launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->d_err, c->tune, s);
+  else launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->wm.dlam, c->d_err, c->tune, s);
   if (kev) cudaEventRecord(kev->ev[1], s);
   harvest(0, 0);
   launch_step_begin(c->d_C, c->d_St, c->n_inst, s);
@@ -758,41 +759,48 @@ static int autotune(swe_ctx* c) {
   const cudaStream_t s = c->stream;
   StageArgsMix a{c->G, c->d_C, c->d_St, c->mA, c->mA, c->mB, c->wm, 1, c->d_err, c->block};
   KernelTune t = c->tune;
-  launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->d_err, t, s);   // populate every work array once
+  launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->wm.dlam, c->d_err, t, s);   // populate every work array once
   launch_stage_mix(a, s, nullptr, t);
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   const int blocks[3] = {64, 128, 256};
-  const int batches[3] = {1, 2, 4};
+  const int batches[4] = {1, 2, 4, 8};
+  // k_low is timed as in stages 2 and 3 (lambda_max computed, not reused)
+  StageArgsMix a_low = a;
+  a_low.rk_stage = 2;
   std::string desc;
   const char* names[5] = {"dt", "node", "low", "fct", "update"};
   for (int kind = 0; kind < 5; kind++) {
     float best = 1e30f;
-    int bb = t.block[kind], bt = t.batch[kind];
+    int bb = t.block[kind], bt = t.batch[kind], bc = t.cap_low;
     for (int ib = 0; ib < 3; ib++)
-      for (int it = 0; it < 3; it++) {
-        if (kind == 2 && batches[it] > 2) continue;
-        KernelTune v = t;
-        v.block[kind] = blocks[ib];
-        v.batch[kind] = batches[it];
-        float tmin = 1e30f;
-        for (int rep = 0; rep < 3; rep++) {
-          cudaEventRecord(e0, s);
-          if (kind == 0) launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->d_err, v, s);
-          else launch_kernel_mix(kind, a, v, s);
-          cudaEventRecord(e1, s);
-          CK(cudaEventSynchronize(e1));
-          float ms = 0.f;
-          cudaEventElapsedTime(&ms, e0, e1);
-          tmin = std::min(tmin, ms);
+      for (int it = 0; it < 4; it++)
+        for (int cap = 0; cap < (kind == 2 ? 2 : 1); cap++) {
+          if (kind == 2 && batches[it] > 2) continue;
+          KernelTune v = t;
+          v.block[kind] = blocks[ib];
+          v.batch[kind] = batches[it];
+          if (kind == 2) v.cap_low = cap;
+          float tmin = 1e30f;
+          for (int rep = 0; rep < 3; rep++) {
+            cudaEventRecord(e0, s);
+            if (kind == 0) launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->wm.dlam, c->d_err, v, s);
+            else launch_kernel_mix(kind, kind == 2 ? a_low : a, v, s);
+            cudaEventRecord(e1, s);
+            CK(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            tmin = std::min(tmin, ms);
+          }
+          if (tmin < best) { best = tmin; bb = blocks[ib]; bt = batches[it]; if (kind == 2) bc = cap; }
         }
-        if (tmin < best) { best = tmin; bb = blocks[ib]; bt = batches[it]; }
-      }
     t.block[kind] = bb;
     t.batch[kind] = bt;
-    char buf[64];
-    snprintf(buf, sizeof buf, "%s%s:block%d/batch%d", kind ? " " : "", names[kind], bb, bt);
+    if (kind == 2) t.cap_low = bc;
+    char buf[80];
+    snprintf(buf, sizeof buf, "%s%s:block%d/batch%d%s", kind ? " " : "", names[kind], bb, bt,
+             kind == 2 ? (bc ? "/regs64" : "/regs85") : "");
     desc += buf;
   }
   cudaEventDestroy(e0);

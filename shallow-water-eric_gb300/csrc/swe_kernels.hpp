@@ -38,6 +38,7 @@ struct WorkMix {
   float* rminus;                         // per row: R^-_i
   float* rneg;                           // per row: R^-_i * sum_{f_ij<0} f_ij
   float *dL, *muL;                       // per entry
+  float* dlam;                           // per entry: |c_ij| lambda_max from k_dt_mix (stage 1)
   float2* hL;                            // low-order depth (double-float)
   float2* qL;                            // low-order momenta
   float *q3L, *q4L;                      // low-order h*eta, h*w (type 13)
@@ -82,18 +83,21 @@ void launch_fct_positivity_f64(const Graph& G, const InstConst* C, const double*
 void launch_mass_f64(const Graph& G, const double* h, double* acc, cudaStream_t s);
 
 // Launch configuration of the mixed kernels, per kernel kind (0 dt, 1 node,
-// 2 low, 3 fct, 4 update): block size and entry batch (1, 2 or 4; 1 or 2 for
-// low).  Chosen by the autotuner in swe_api.cu.  Every choice sums in the same
-// entry order; the batch variants are separate instantiations whose FMA
-// contraction may differ, so results agree to FP32 rounding.
+// 2 low, 3 fct, 4 update): block size and entry batch (1, 2, 4 or 8; 1 or 2
+// for low), and for low the tighter of two register caps (cap_low: 64
+// instead of 85 registers).  Chosen by the
+// autotuner in swe_api.cu.  Every choice sums in the same entry order; the
+// variants are separate instantiations whose FMA contraction may differ, so
+// results agree to FP32 rounding.
 struct KernelTune {
   int block[5] = {128, 128, 128, 128, 128};
   int batch[5] = {1, 1, 1, 1, 1};
+  int cap_low = 0;
 };
 
 void launch_stage_mix(const StageArgsMix& a, cudaStream_t s, const KernelEvents* kev, const KernelTune& t);
 void launch_kernel_mix(int kind, const StageArgsMix& a, const KernelTune& t, cudaStream_t s);
-void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, unsigned* err,
+void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, float* dlam, unsigned* err,
                    const KernelTune& t, cudaStream_t s);
 void launch_refresh_z(const Graph& G, StateMix u, cudaStream_t s);
 void launch_mass_mix(const Graph& G, const float2* h, double* acc, cudaStream_t s);

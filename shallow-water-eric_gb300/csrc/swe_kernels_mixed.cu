@@ -211,12 +211,12 @@ __device__ __forceinline__ float sgn_pressure(float lambda_sgn, float g, float m
 // formed once and shared by mu_ij, lambda_max and the Galerkin flux.  The
 // diagonal entry only enters through terms that vanish identically
 // (u_i rat_ii - u_i rat_ii) and the Galerkin boundary term -c_ii.v_i.
-template <int B>
-__global__ void __launch_bounds__(256) k_low_mix(Graph G, const InstConst* __restrict__ C,
-                                                 const InstState* __restrict__ St, StateMix u,
-                                                 const float* __restrict__ alpha, float* __restrict__ dL,
-                                                 float* __restrict__ muL, WorkMix w, float* __restrict__ res,
-                                                 unsigned* __restrict__ err) {
+template <int B, bool LAMIN, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_low_mix(Graph G, const InstConst* __restrict__ C,
+                                                       const InstState* __restrict__ St, StateMix u,
+                                                       const float* __restrict__ alpha, float* __restrict__ dL,
+                                                       float* __restrict__ muL, WorkMix w, float* __restrict__ res,
+                                                       unsigned* __restrict__ err) {
   int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= G.n_rows) return;
   const int L = G.len[r];
@@ -264,14 +264,15 @@ __global__ void __launch_bounds__(256) k_low_mix(Graph G, const InstConst* __res
   }
   for (int k0 = 0; k0 < L; k0 += B) {
    int jb[B];
-   float cxb[B], cyb[B];
+   float cxb[B], cyb[B], dlb[B];
 #pragma unroll
    for (int q = 0; q < B; q++) {
      if (k0 + q < L) {
        const int64_t e = base + 32 * (k0 + q);
        jb[q] = G.col[e]; cxb[q] = G.cxf[e]; cyb[q] = G.cyf[e];
+       dlb[q] = LAMIN ? w.dlam[e] : 0.f;
      } else {
-       jb[q] = (int)r; cxb[q] = 0.f; cyb[q] = 0.f;
+       jb[q] = (int)r; cxb[q] = 0.f; cyb[q] = 0.f; dlb[q] = 0.f;
      }
    }
    float4 nqb[B];
@@ -286,16 +287,21 @@ __global__ void __launch_bounds__(256) k_low_mix(Graph G, const InstConst* __res
     const int j = jb[q];
     const NodeF nj = node_from(nqb[q], htiny);
     // --- viscosities: compute_dij, compute_muij, MAX, alpha_limit
-    const float n2 = cxe * cxe + cye * cye;
-    const float inv = rsqrtf(n2);
-    const float norm = n2 * inv;
     const float cvi = dotc(cxe, cye, ni.v1, ni.v2);                   // c.v_i (compute_muij)
     const float cvj = dotc(cxe, cye, nj.v1, nj.v2);                   // c.v_j
-    float lam;
-    if (!lambda_f(ni.h, nj.h, cvi * inv, cvj * inv, ni.ovh, nj.ovh, sqi, sqrtf(g * fabsf(nj.h)), lk, &lam))
-      delta_bad = true;
+    float dlam;                                                       // |c_ij| lambda_max
+    if (LAMIN) {
+      dlam = dlb[q];                                                  // from k_dt_mix on this state
+    } else {
+      const float n2 = cxe * cxe + cye * cye;
+      const float inv = rsqrtf(n2);
+      float lam;
+      if (!lambda_f(ni.h, nj.h, cvi * inv, cvj * inv, ni.ovh, nj.ovh, sqi, sqrtf(g * fabsf(nj.h)), lk, &lam))
+        delta_bad = true;
+      dlam = (n2 * inv) * lam;
+    }
     float mu = fmaxf(fmaxf(-cvi, 0.f), fmaxf(cvj, 0.f));
-    float d = fmaxf(norm * lam, mu);
+    float d = fmaxf(dlam, mu);
     if (c.alpha_limit) {
       const float s = fmaxf(ai, alb[q]);
       d *= s;
@@ -316,24 +322,31 @@ __global__ void __launch_bounds__(256) k_low_mix(Graph G, const InstConst* __res
     const float rjit = (nj.h <= htiny) ? 0.f : rji;
     const float cvj_flux = sgn ? dotc(cxe, cye, nj.v1, 0.f) : cvj;   // c.velocity_j of flux()
     const float topo = g * ni.h * ((nj.h - ni.h) + dz);               // g h_i (eta_j - eta_i)
-    // --- smb_2_roundoff mass row (fix_roundoff, rk_1)
-    fix += -mu - (d - mu) * rijt;
-    rk0 += (mu - cvj_flux) * nj.h + fmaxf((d - mu) * R.Hji, 0.f);
-    // --- smb_2 mass row
-    g0 += -cvj_flux * nj.h + d * (nj.h * rji - ni.h * rij) + mu * (nj.h * (1.f - rji) - ni.h * (1.f - rij));
-    // --- momenta (both RHS) and topography
-    rk1 += -cvj_flux * nj.q1 + d * (nj.q1 * rjit - ni.q1 * rijt) + mu * (nj.q1 * (1.f - rjit) - ni.q1 * (1.f - rijt));
-    rk2_ += -cvj_flux * nj.q2 + d * (nj.q2 * rjit - ni.q2 * rijt) + mu * (nj.q2 * (1.f - rjit) - ni.q2 * (1.f - rijt));
-    g1 += -cvj_flux * nj.q1 + d * (nj.q1 * rji - ni.q1 * rij) + mu * (nj.q1 * (1.f - rji) - ni.q1 * (1.f - rij));
-    g2 += -cvj_flux * nj.q2 + d * (nj.q2 * rji - ni.q2 * rij) + mu * (nj.q2 * (1.f - rji) - ni.q2 * (1.f - rij));
+    // --- smb_2_roundoff mass row (fix_roundoff, rk_1), in the reference's
+    // form: its sign properties give h^L >= 0
+    const float dmu = d - mu;
+    fix += -mu - dmu * rijt;
+    rk0 += (mu - cvj_flux) * nj.h + fmaxf(dmu * R.Hji, 0.f);
+    // --- smb_2 mass row and the momenta of both RHS, written as
+    // -c.v_j u_j + mu (u_j - u_i) + (d - mu) (u_j rat_ji - u_i rat_ij), which
+    // equals d (u_j rat_ji - u_i rat_ij) + mu (u_j (1 - rat_ji) - u_i (1 - rat_ij))
+    g0 += -cvj_flux * nj.h + mu * (nj.h - ni.h) + dmu * (nj.h * rji - ni.h * rij);
+    const float A1 = mu * (nj.q1 - ni.q1) - cvj_flux * nj.q1;
+    const float A2 = mu * (nj.q2 - ni.q2) - cvj_flux * nj.q2;
+    rk1 += A1 + dmu * (nj.q1 * rjit - ni.q1 * rijt);
+    rk2_ += A2 + dmu * (nj.q2 * rjit - ni.q2 * rijt);
+    g1 += A1 + dmu * (nj.q1 * rji - ni.q1 * rij);
+    g2 += A2 + dmu * (nj.q2 * rji - ni.q2 * rij);
     rk1 -= topo * cxe; rk2_ -= topo * cye;
     g1 -= topo * cxe; g2 -= topo * cye;
     if (S == 5) {
       const float uj3 = u.q3[j], uj4 = u.q4[j];
-      rk3 += -cvj_flux * uj3 + d * (uj3 * rjit - ui3 * rijt) + mu * (uj3 * (1.f - rjit) - ui3 * (1.f - rijt));
-      rk4 += -cvj_flux * uj4 + d * (uj4 * rjit - ui4 * rijt) + mu * (uj4 * (1.f - rjit) - ui4 * (1.f - rijt));
-      g3 += -cvj_flux * uj3 + d * (uj3 * rji - ui3 * rij) + mu * (uj3 * (1.f - rji) - ui3 * (1.f - rij));
-      g4 += -cvj_flux * uj4 + d * (uj4 * rji - ui4 * rij) + mu * (uj4 * (1.f - rji) - ui4 * (1.f - rij));
+      const float A3 = mu * (uj3 - ui3) - cvj_flux * uj3;
+      const float A4 = mu * (uj4 - ui4) - cvj_flux * uj4;
+      rk3 += A3 + dmu * (uj3 * rjit - ui3 * rijt);
+      rk4 += A4 + dmu * (uj4 * rjit - ui4 * rijt);
+      g3 += A3 + dmu * (uj3 * rji - ui3 * rij);
+      g4 += A4 + dmu * (uj4 * rji - ui4 * rij);
       if (sgn) {
         const float pt = sgn_pressure(c.lambda_sgnf, g, G.lumpedf[j], nj.h, uj3);
         ptx -= pt * cxe;
@@ -518,13 +531,15 @@ __global__ void __launch_bounds__(256) k_update_mix(Graph G, const InstConst* __
     const float f = fct_from(ddr, dmr, hi, nj.x, R);
     float lf = Ri;
     if (f >= 0.f) { lf = Rjb[q]; pos = __fmaf_rn(lf, f, pos); }
-    const float dd = ddr * lf, dm = dmr * lf;
-    x1 += dd * (nj.y * R.rji - ni.y * R.rij) + dm * (nj.y * (1.f - R.rji) - ni.y * (1.f - R.rij));
-    x2 += dd * (nj.z * R.rji - ni.z * R.rij) + dm * (nj.z * (1.f - R.rji) - ni.z * (1.f - R.rij));
+    // l (dd (u_j rat_ji - u_i rat_ij) + dm (u_j (1 - rat_ji) - u_i (1 - rat_ij)))
+    // = l (dm (u_j - u_i) + (dd - dm) (u_j rat_ji - u_i rat_ij))
+    const float dm = dmr * lf, dx = (ddr - dmr) * lf;
+    x1 += dm * (nj.y - ni.y) + dx * (nj.y * R.rji - ni.y * R.rij);
+    x2 += dm * (nj.z - ni.z) + dx * (nj.z * R.rji - ni.z * R.rij);
     if (S == 5) {
       const float uj3 = u.q3[j], uj4 = u.q4[j];
-      x3 += dd * (uj3 * R.rji - ui3 * R.rij) + dm * (uj3 * (1.f - R.rji) - ui3 * (1.f - R.rij));
-      x4 += dd * (uj4 * R.rji - ui4 * R.rij) + dm * (uj4 * (1.f - R.rji) - ui4 * (1.f - R.rij));
+      x3 += dm * (uj3 - ui3) + dx * (uj3 * R.rji - ui3 * R.rij);
+      x4 += dm * (uj4 - ui4) + dx * (uj4 * R.rji - ui4 * R.rij);
     }
    }
   }
@@ -571,7 +586,7 @@ __global__ void __launch_bounds__(256) k_update_mix(Graph G, const InstConst* __
 // k_dt_mix: FP32 lambda_max, max |d_ii|/m_i per instance (main.f90:166-174)
 template <int B>
 __global__ void __launch_bounds__(256) k_dt_mix(Graph G, const InstConst* __restrict__ C, InstState* __restrict__ St, StateMix u,
-                         unsigned* __restrict__ err) {
+                         float* __restrict__ dlam, unsigned* __restrict__ err) {
   int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   float val = 0.f;
   if (r < G.n_rows && G.len[r] > 0) {
@@ -612,7 +627,9 @@ __global__ void __launch_bounds__(256) k_dt_mix(Graph G, const InstConst* __rest
         if (!lambda_f(ni.h, nj.h, dotc(cxe, cye, ni.v1, ni.v2) * inv, dotc(cxe, cye, nj.v1, nj.v2) * inv, ni.ovh,
                       nj.ovh, sqi, sqrtf(g * fabsf(nj.h)), lk, &lam))
           bad = true;
-        s += (n2 * inv) * lam;
+        const float dl = (n2 * inv) * lam;
+        if (dlam) dlam[base + 32 * (k0 + q)] = dl;
+        s += dl;
        }
       }
       val = s * G.inv_lumpedf[r];
@@ -666,22 +683,33 @@ static inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) 
 
 #define SWE_DISPATCH_B(b, KERNEL, GRID, BS, ...)                         \
   switch (b) {                                                           \
+    case 8: KERNEL<8><<<GRID, BS, 0, s>>>(__VA_ARGS__); break;           \
     case 4: KERNEL<4><<<GRID, BS, 0, s>>>(__VA_ARGS__); break;           \
     case 2: KERNEL<2><<<GRID, BS, 0, s>>>(__VA_ARGS__); break;           \
     default: KERNEL<1><<<GRID, BS, 0, s>>>(__VA_ARGS__); break;          \
   }
+
+// k_low variants: entry batch 1 or 2, lambda_max computed or taken from
+// k_dt_mix (stage 1), registers capped at 85 or 64 (3 or 4 resident blocks
+// of 256 threads per SM; the compiler would take ~106 with no cap)
+template <bool LAMIN>
+static void launch_low(const StageArgsMix& a, int batch, int cap, unsigned grid, int block, cudaStream_t s) {
+#define SWE_LOW(BB, MB) \
+  k_low_mix<BB, LAMIN, MB><<<grid, block, 0, s>>>(a.G, a.C, a.St, a.u, a.w.alpha, a.w.dL, a.w.muL, a.w, a.w.res, a.err)
+  if (batch >= 2) { if (cap) SWE_LOW(2, 4); else SWE_LOW(2, 3); }
+  else { if (cap) SWE_LOW(1, 4); else SWE_LOW(1, 3); }
+#undef SWE_LOW
+}
 
 void launch_kernel_mix(int kind, const StageArgsMix& a, const KernelTune& t, cudaStream_t s) {
   const int64_t n = a.G.n_rows;
   switch (kind) {
     case 1: SWE_DISPATCH_B(t.batch[1], k_node_mix, nblk(n, t.block[1]), t.block[1], a.G, a.C, a.St, a.u, a.w.alpha)
             break;
-    case 2: if (t.batch[2] >= 2)
-              k_low_mix<2><<<nblk(n, t.block[2]), t.block[2], 0, s>>>(a.G, a.C, a.St, a.u, a.w.alpha, a.w.dL, a.w.muL,
-                                                                       a.w, a.w.res, a.err);
+    case 2: if (a.rk_stage == 1 && a.w.dlam)   // stage 1 follows k_dt_mix on the same state
+              launch_low<true>(a, t.batch[2], t.cap_low, nblk(n, t.block[2]), t.block[2], s);
             else
-              k_low_mix<1><<<nblk(n, t.block[2]), t.block[2], 0, s>>>(a.G, a.C, a.St, a.u, a.w.alpha, a.w.dL, a.w.muL,
-                                                                       a.w, a.w.res, a.err);
+              launch_low<false>(a, t.batch[2], t.cap_low, nblk(n, t.block[2]), t.block[2], s);
             break;
     case 3: SWE_DISPATCH_B(t.batch[3], k_fct_mix, nblk(n, t.block[3]), t.block[3], a.G, a.C, a.St, a.u, a.w.dL,
                            a.w.muL, a.w, a.w.res, a.err)
@@ -701,9 +729,9 @@ void launch_stage_mix(const StageArgsMix& a, cudaStream_t s, const KernelEvents*
   }
 }
 
-void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, unsigned* err,
+void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, float* dlam, unsigned* err,
                    const KernelTune& t, cudaStream_t s) {
-  SWE_DISPATCH_B(t.batch[0], k_dt_mix, nblk(G.n_rows, t.block[0]), t.block[0], G, C, St, u, err)
+  SWE_DISPATCH_B(t.batch[0], k_dt_mix, nblk(G.n_rows, t.block[0]), t.block[0], G, C, St, u, dlam, err)
 }
 
 void launch_refresh_z(const Graph& G, StateMix u, cudaStream_t s) {
