@@ -133,6 +133,13 @@ int swe_euler_intermediates(swe_ctx* ctx, int inst, double* dij_low, double* mui
  * mat = f_ij (nnz, CSR order) -> lij (nnz, CSR order). */
 int swe_fct_positivity(swe_ctx* ctx, int inst, const double* unext, const double* mat, double* lij);
 
+/* FCT_generic (SOURCES/SAFE/fct.f90:3-43), the two-sided Zalesak limiter with
+ * local bounds: unext (np, in/out) is limited in place using maxn, minn (np),
+ * the antidiffusive matrix mat (nnz, CSR order, diagonal included) and dg
+ * (np; NULL = the lumped mass).  FP64 contexts only. */
+int swe_fct_generic(swe_ctx* ctx, int inst, double* unext, const double* maxn, const double* minn,
+                    const double* mat, const double* dg);
+
 /* Device-resident fast path.  upload/download move every instance's state;
  * un is the concatenation of the instances' un(S, np_b) blocks. */
 int swe_upload(swe_ctx* ctx, const double* un);

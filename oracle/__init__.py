@@ -81,6 +81,7 @@ def lib():
         L.orc_compute_dij.argtypes = [vp, dp, dp, dp]
         L.orc_euler.argtypes = [vp, dp, dp, ctypes.POINTER(Dump)]
         L.orc_fct_positivity.argtypes = [vp, dp, dp, dp]
+        L.orc_fct_generic.argtypes = [vp, dp, dp, dp, dp, dp]
         L.orc_rk3_step.argtypes = [vp, dp, dp, ctypes.c_double]
         L.orc_run.argtypes = [vp, dp, dp, ctypes.c_double, ctypes.c_int, ip]
         L.orc_last_dt.restype = ctypes.c_double
@@ -195,6 +196,13 @@ class Oracle:
         lij = np.zeros(self.nnz)
         lib().orc_fct_positivity(self.h, _dp(u), _dp(f), _dp(lij))
         return lij
+
+    def fct_generic(self, unext, maxn, minn, fmat, dg):
+        """FCT_generic (SAFE/fct.f90:3-43); returns the limited copy of unext."""
+        u = np.array(unext, np.float64)
+        args = [np.ascontiguousarray(a, np.float64) for a in (maxn, minn, fmat, dg)]
+        lib().orc_fct_generic(self.h, _dp(u), *[_dp(a) for a in args])
+        return u
 
     def rk3_step(self, un, time, fixed_dt=0.0):
         t = ctypes.c_double(time)

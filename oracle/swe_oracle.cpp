@@ -663,6 +663,41 @@ void fct_positivity(const Oracle& o, const double* unext, const double* fmat, do
   if (Rm_out) std::copy(Rminus.begin(), Rminus.end(), Rm_out);
 }
 
+// FCT_generic: SOURCES/SAFE/fct.f90:3-43.  Two-sided Zalesak limiter with
+// local bounds: Q+ = dg (maxn - u), Q- = dg (minn - u); P+- = +-1e-15 plus the
+// row's positive / negative fluxes (CSR order); R+- = MIN(Q+-/P+-, 1);
+// l_ij = MIN(R+_i, R-_j) for f_ij >= 0 else MIN(R-_i, R+_j);
+// u_i += (sum_j l_ij f_ij) / dg_i.
+void fct_generic(const Oracle& o, double* unext, const double* maxn, const double* minn, const double* fmat,
+                 const double* dg) {
+  const double smallplus = 1.e-15, smallminus = -1.e-15;
+  std::vector<double> Rplus(o.np), Rminus(o.np);
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < o.np; i++) {
+    const double Qplus = dg[i] * (maxn[i] - unext[i]);
+    const double Qminus = dg[i] * (minn[i] - unext[i]);
+    double Pplus = smallplus, Pminus = smallminus;
+    for (int p = o.ia[i]; p < o.ia[i + 1]; p++) {
+      if (fmat[p] >= 0.0) Pplus = Pplus + fmat[p];
+      else Pminus = Pminus + fmat[p];
+    }
+    Rplus[i] = fmin_(Qplus / Pplus, 1.0);
+    Rminus[i] = fmin_(Qminus / Pminus, 1.0);
+  }
+  std::vector<double> x(o.np);
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < o.np; i++) {
+    double xx = 0.0;
+    for (int p = o.ia[i]; p < o.ia[i + 1]; p++) {
+      const int j = o.ja[p];
+      const double l = (fmat[p] >= 0.0) ? fmin_(Rplus[i], Rminus[j]) : fmin_(Rminus[i], Rplus[j]);
+      xx = xx + l * fmat[p];
+    }
+    x[i] = xx;
+  }
+  for (int i = 0; i < o.np; i++) unext[i] = unext[i] + x[i] / dg[i];
+}
+
 // apply_viscosity: SOURCES/update.f90:684-718
 void apply_viscosity(Oracle& o, const double* un, std::vector<double>& rk) {
   const int S = o.P.syst_size;
@@ -915,6 +950,13 @@ int orc_euler(void* h, const double* un, double* unext, orc_dump* dump) {
 // already-scaled (lumped/dt)*h^L vector, fmat the antidiffusive matrix.
 void orc_fct_positivity(void* h, const double* unext, const double* fmat, double* lij) {
   fct_positivity(*static_cast<Oracle*>(h), unext, fmat, lij, nullptr);
+}
+
+// FCT_generic as a stand-alone call (SOURCES/SAFE/fct.f90:3-43); unext is
+// limited in place.
+void orc_fct_generic(void* h, double* unext, const double* maxn, const double* minn, const double* fmat,
+                     const double* dg) {
+  fct_generic(*static_cast<Oracle*>(h), unext, maxn, minn, fmat, dg);
 }
 
 static void bdy(Oracle& o, double* uu) {

@@ -109,14 +109,28 @@ static InstConst make_const(const swe_params& p) {
   return k;
 }
 
+static bool has_entropy(const swe_ctx* c) {
+  for (const swe_params& p : c->params)
+    if (p.viscosity_type == SWE_VISC_ENTROPY) return true;
+  return false;
+}
+
 static int check_params(swe_ctx* c, const swe_params& p) {
   if (p.syst_size != 3 && p.syst_size != 5) return fail(c, SWE_ERR_ARG, "syst_size must be 3 or 5");
   if ((p.syst_size == 5) != (p.type_test == 13)) return fail(c, SWE_ERR_ARG, "syst_size 5 goes with type_test 13");
   if (!p.if_lumped) return fail(c, SWE_ERR_ARG, "only the lumped-mass step is supported (if_lumped)");
-  if (p.viscosity_type != SWE_VISC_FCT && p.viscosity_type != SWE_VISC_VISCOUS)
-    return fail(c, SWE_ERR_ARG, "viscosity_type must be 'fct' or 'viscous'");
-  if (p.viscous_type != 2) return fail(c, SWE_ERR_ARG, "viscous_type must be 'type2'");
+  if (p.viscosity_type < SWE_VISC_GALERKIN || p.viscosity_type > SWE_VISC_FCT)
+    return fail(c, SWE_ERR_ARG, "viscosity_type must be galerkin, viscous, entropy_visc or fct");
+  if (p.viscous_type != 1 && p.viscous_type != 2) return fail(c, SWE_ERR_ARG, "viscous_type must be 1 or 2");
+  // the reference STOPs on these combinations (update.f90:244-245, 264-266)
+  if (p.viscous_type == 1 && p.viscosity_type == SWE_VISC_ENTROPY)
+    return fail(c, SWE_ERR_ARG, "Bug: entropy viscosity programmed only with type 2");
+  if (p.viscous_type == 1 && p.viscosity_type == SWE_VISC_FCT)
+    return fail(c, SWE_ERR_ARG, "BUG: FCT programmed with type2 only");
   if (p.precision != SWE_PREC_FP64 && p.precision != SWE_PREC_MIXED) return fail(c, SWE_ERR_ARG, "bad precision");
+  if (p.precision == SWE_PREC_MIXED &&
+      (p.viscosity_type == SWE_VISC_ENTROPY || (p.viscous_type == 1 && p.viscosity_type != SWE_VISC_GALERKIN)))
+    return fail(c, SWE_ERR_ARG, "mixed precision builds 'galerkin', 'viscous' (type2) and 'fct'");
   if (!(p.htiny >= 0.0) || !(p.gravity > 0.0)) return fail(c, SWE_ERR_ARG, "gravity must be > 0, htiny >= 0");
   return SWE_OK;
 }
@@ -373,13 +387,14 @@ static void enqueue_step(swe_ctx* c, const KernelEvents* kev = nullptr, double* 
   if (kev) cudaEventRecord(kev->ev[0], s);
   if (c->precision == SWE_PREC_FP64)
     launch_dt_f64(c->G, c->d_C, c->d_St, c->A, nullptr, nullptr, c->d_err, c->block, s);
-  else launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->wm.dlam, c->d_err, c->tune, s);
+  else launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->wm.dlam, c->wm.alpha, c->d_err, c->tune, s);
   if (kev) cudaEventRecord(kev->ev[1], s);
   harvest(0, 0);
   launch_step_begin(c->d_C, c->d_St, c->n_inst, s);
   for (int stage = 1; stage <= 3; stage++) {
     if (c->precision == SWE_PREC_FP64) {
       StageArgs a{c->G, c->d_C, c->d_St, c->A, c->A, c->B, c->w, stage, nullptr, c->d_err, c->block};
+      a.entropy = has_entropy(c);
       if (stage == 2) { a.u = c->B; a.out = c->Cs; }
       if (stage == 3) { a.u = c->Cs; a.out = c->A; }
       launch_stage_f64(a, s, kev);
@@ -625,6 +640,7 @@ SWE_API int swe_euler(swe_ctx* c, int inst, const double* un, double* unext) {
   if ((rc = set_inst_state_dt(c, inst, c->params[inst].dt, 1))) return rc;
   if (c->precision == SWE_PREC_FP64) {
     StageArgs a{c->G, c->d_C, c->d_St, c->A, c->A, c->B, c->w, 0, c->d_lij, c->d_err, c->block};
+    a.entropy = has_entropy(c);
     launch_stage_f64(a, c->stream);
   } else {
     StageArgsMix a{c->G, c->d_C, c->d_St, c->mA, c->mA, c->mB, c->wm, 0, c->d_err, c->block};
@@ -695,6 +711,43 @@ SWE_API int swe_fct_positivity(swe_ctx* c, int inst, const double* unext, const 
   return entries_to_csr(c, inst, c->d_lij, lij, c->w.rminus);   // l_ii = R_i
 }
 
+SWE_API int swe_fct_generic(swe_ctx* c, int inst, double* unext, const double* maxn, const double* minn,
+                            const double* mat, const double* dg) {
+  if (!c || inst < 0 || inst >= c->n_inst || !unext || !maxn || !minn || !mat)
+    return fail(c, SWE_ERR_ARG, "bad arguments");
+  if (c->precision != SWE_PREC_FP64) return fail(c, SWE_ERR_ARG, "swe_fct_generic is an FP64 operator");
+  const Layout& L = c->L;
+  const HostMesh& m = c->meshes[inst];
+  const size_t nr = L.n_rows;
+  std::vector<double> hu(nr, 0.0), hmax(nr, 0.0), hmin(nr, 0.0), hdg(nr, 1.0), hdiag(nr, 0.0),
+      hent(L.n_entries, 0.0);
+  for (int i = 0; i < m.np; i++) {
+    const int64_t r = L.new_of_old[inst][i];
+    hu[r] = unext[i];
+    hmax[r] = maxn[i];
+    hmin[r] = minn[i];
+    hdg[r] = dg ? dg[i] : m.lumped[i];
+    hdiag[r] = mat[m.diag[i]];
+  }
+  const int64_t s0 = L.row_off[inst] / 32, s1 = L.row_off[inst + 1] / 32;
+  for (int64_t e = L.slice_ptr[s0]; e < L.slice_ptr[s1]; e++)
+    if (L.ref_pos[e] >= 0) hent[e] = mat[L.ref_pos[e]];
+  WorkF64& w = c->w;   // per-stage scratch, reused: u, bounds, dg, R+-, f_ij
+  CK(cudaMemcpyAsync(w.uL.h, hu.data(), nr * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(w.v1, hmax.data(), nr * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(w.v2, hmin.data(), nr * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(w.ovh, hdg.data(), nr * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(w.dLii, hdiag.data(), nr * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(w.fct, hent.data(), L.n_entries * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  launch_fct_generic_f64(c->G, w.uL.h, w.v1, w.v2, w.ovh, w.fct, w.dLii, w.ent, w.rminus, c->stream);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(hu.data(), w.uL.h, nr * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  for (int i = 0; i < m.np; i++) unext[i] = hu[L.new_of_old[inst][i]];
+  c->euler_done = false;
+  return SWE_OK;
+}
+
 SWE_API int swe_upload(swe_ctx* c, const double* un) {
   if (!c || !un) return fail(c, SWE_ERR_ARG, "bad arguments");
   int rc = to_device(c, un, false, 0, c->node_off[c->n_inst]);
@@ -759,7 +812,7 @@ static int autotune(swe_ctx* c) {
   const cudaStream_t s = c->stream;
   StageArgsMix a{c->G, c->d_C, c->d_St, c->mA, c->mA, c->mB, c->wm, 1, c->d_err, c->block};
   KernelTune t = c->tune;
-  launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->wm.dlam, c->d_err, t, s);   // populate every work array once
+  launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->wm.dlam, c->wm.alpha, c->d_err, t, s);   // populate every work array once
   launch_stage_mix(a, s, nullptr, t);
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
@@ -785,7 +838,7 @@ static int autotune(swe_ctx* c) {
           float tmin = 1e30f;
           for (int rep = 0; rep < 3; rep++) {
             cudaEventRecord(e0, s);
-            if (kind == 0) launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->wm.dlam, c->d_err, v, s);
+            if (kind == 0) launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->wm.dlam, c->wm.alpha, c->d_err, v, s);
             else launch_kernel_mix(kind, kind == 2 ? a_low : a, v, s);
             cudaEventRecord(e1, s);
             CK(cudaEventSynchronize(e1));
@@ -837,7 +890,8 @@ SWE_API int swe_rk3_steps(swe_ctx* c, int nsteps, double* time_out, double* dt_o
   if (!c->t0) { CK(cudaEventCreate(&c->t0)); CK(cudaEventCreate(&c->t1)); }
   if (nsteps >= chunk && chunk > 1 && (rc = build_graph(c, chunk))) return rc;
   CK(cudaEventRecord(c->t0, c->stream));
-  const long long per_step = 3LL * kLaunchesPerStage + kLaunchesPerStepExtra;
+  // the mixed stage 1 takes alpha from k_dt_mix: one k_node launch fewer
+  const long long per_step = 3LL * kLaunchesPerStage + kLaunchesPerStepExtra - (c->precision == SWE_PREC_MIXED ? 1 : 0);
   if (nsteps >= chunk && chunk > 1) {
     for (int k = 0; k + chunk <= nsteps; k += chunk) {
       CK(cudaGraphLaunch(c->gexec, c->stream));

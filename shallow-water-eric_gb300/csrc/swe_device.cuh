@@ -10,6 +10,9 @@ namespace swe {
 // SWE_ERR_* after each launch sequence.
 enum : unsigned { ERRB_NEG_H = 1u, ERRB_DELTA = 2u, ERRB_NAN = 4u };
 
+// inputs%viscosity_type (the values of SWE_VISC_* in the C ABI header)
+enum : int { VISC_GALERKIN = 0, VISC_VISCOUS = 1, VISC_ENTROPY = 2, VISC_FCT = 3 };
+
 // Per-instance constants (one record per mesh of a batch).  The FP32 copies
 // are rounded once on the host: the mixed kernels never convert per row
 // (a float<->double conversion issues on GB300's narrow FP64 pipe).

@@ -54,6 +54,7 @@ struct StageArgs {
   double* lij_out;
   unsigned* err;
   int block;
+  int entropy = 0;   // some instance uses 'entropy_visc': launch k_entropy
 };
 
 struct StageArgsMix {
@@ -80,6 +81,8 @@ void launch_step_begin(const InstConst* C, InstState* St, int n_inst, cudaStream
 void launch_step_end(InstState* St, int n_inst, cudaStream_t s);
 void launch_fct_positivity_f64(const Graph& G, const InstConst* C, const double* unext, const double* mat,
                                const double* matii, double* rtmp, double* lij, cudaStream_t s);
+void launch_fct_generic_f64(const Graph& G, double* unext, const double* maxn, const double* minn, const double* dg,
+                            const double* mat, const double* matii, double* rplus, double* rminus, cudaStream_t s);
 void launch_mass_f64(const Graph& G, const double* h, double* acc, cudaStream_t s);
 
 // Launch configuration of the mixed kernels, per kernel kind (0 dt, 1 node,
@@ -97,8 +100,8 @@ struct KernelTune {
 
 void launch_stage_mix(const StageArgsMix& a, cudaStream_t s, const KernelEvents* kev, const KernelTune& t);
 void launch_kernel_mix(int kind, const StageArgsMix& a, const KernelTune& t, cudaStream_t s);
-void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, float* dlam, unsigned* err,
-                   const KernelTune& t, cudaStream_t s);
+void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, float* dlam, float* alpha,
+                   unsigned* err, const KernelTune& t, cudaStream_t s);
 void launch_refresh_z(const Graph& G, StateMix u, cudaStream_t s);
 void launch_mass_mix(const Graph& G, const float2* h, double* acc, cudaStream_t s);
 

@@ -112,6 +112,147 @@ __device__ __forceinline__ void sgn_node_f64(const InstConst& c, double m, doubl
   *s = 3.0 * pc * (t * t) * psi;
 }
 
+// Viscosities seen by the row sums: the low-order (alpha-limited) d_ij, mu_ij,
+// or the entropy-viscosity d^H = MIN(d, res_ij), mu^H = MIN(mu, res_ij) of
+// update.f90:232-239 (applied to the diagonal too: res_ii = res_i).
+struct LowVisc {
+  const double* dL;
+  const double* muL;
+  double dii, muii;
+  __device__ void get(bool isd, int64_t e, int, double& d, double& mu) const {
+    d = isd ? dii : dL[e];
+    mu = isd ? muii : muL[e];
+  }
+};
+struct HighVisc {
+  const double* dL;
+  const double* muL;
+  const double* res;
+  double dii, muii, resi;
+  __device__ void get(bool isd, int64_t e, int j, double& d, double& mu) const {
+    const double rij = isd ? tmax(resi, resi) : tmax(resi, res[j]);
+    d = tmin(isd ? dii : dL[e], 1.0 * rij);
+    mu = tmin(isd ? muii : muL[e], 1.0 * rij);
+  }
+};
+
+struct RowSums {
+  double rk[5] = {0, 0, 0, 0, 0};    // smb_2_roundoff (htiny tests), with fix
+  double rk2[5] = {0, 0, 0, 0, 0};   // smb_2 (h <= 0 tests)
+  double rk1[5] = {0, 0, 0, 0, 0};   // smb_1 ('type1')
+  double fix = 0.0;                   // fix_roundoff
+  double emax = 0.0, emin = 0.0;      // maxmin of the entropy over the row
+};
+
+// One row of smb_2_roundoff (update.f90:554-624), smb_2 (:626-682) and smb_1
+// (:366-423), each with its source terms (:425-551), over the row's entries
+// in reference order with the diagonal at dp; the entropy max/min of maxmin
+// (:924-935) on the way.  Undivided by the lumped mass.
+template <class V>
+__device__ __forceinline__ void smb_rows_f64(const Graph& G, const InstConst& c, const InstState& st, const StateF64& u,
+                                             const NodeF64& nd, int64_t r, int64_t base, int L, int dp,
+                                             const double* ui, double zi, double m, const V& visc, bool want_round,
+                                             bool want_plain, bool want_t1, RowSums& o) {
+  const int S = c.S;
+  const double g = c.g, htiny = c.htiny;
+  const double v1i = nd.v1[r], v2i = nd.v2[r];
+  double* rk = o.rk;
+  double* rk2 = o.rk2;
+  double* rk1 = o.rk1;
+  o.emax = nd.ent[r];
+  o.emin = o.emax;
+  for (int kk = 0; kk <= L; kk++) {
+    const bool isd = (kk == dp);
+    const int64_t e = base + 32 * (kk - (kk > dp ? 1 : 0));
+    const int j = isd ? (int)r : G.col[e];
+    double uj[5];
+    uj[0] = u.h[j]; uj[1] = u.q1[j]; uj[2] = u.q2[j];
+    if (S == 5) { uj[3] = u.q3[j]; uj[4] = u.q4[j]; }
+    const double zj = G.bath[j];
+    const double v1j = nd.v1[j], v2j = nd.v2[j];
+    double d, mu;
+    visc.get(isd, e, j, d, mu);
+    const double cxe = isd ? G.cxii[r] : G.cx[e], cye = isd ? G.cyii[r] : G.cy[e];
+    const double ej = nd.ent[j];
+    o.emax = tmax(o.emax, ej);
+    o.emin = tmin(o.emin, ej);
+    const double zmax = tmax(zi, zj);
+    const double Hij = tmax(0.0, ui[0] + zi - zmax);
+    const double Hji = tmax(0.0, uj[0] + zj - zmax);
+    if (want_round) {   // smb_2_roundoff (htiny tests)
+      const double ratij = (ui[0] <= htiny) ? 0.0 : Hij / ui[0];
+      const double ratji = (uj[0] <= htiny) ? 0.0 : Hji / uj[0];
+      double xx = 0.0;
+      xx = xx - cxe * (v1j);
+      xx = xx - cye * (v2j);
+      if (isd) {
+        o.fix = o.fix + xx;
+      } else {
+        o.fix = o.fix - mu + (d - mu) * (-ratij);
+        rk[0] = rk[0] + (xx + mu) * uj[0] + tmax((d - mu) * Hji, 0.0);
+      }
+      for (int q = 1; q < S; q++) {
+        double x2 = 0.0;
+        x2 = x2 - cxe * (v1j * uj[q]);
+        x2 = x2 - cye * (v2j * uj[q]);
+        rk[q] = rk[q] + x2 + d * (uj[q] * ratji - ui[q] * ratij) + mu * (uj[q] * (1.0 - ratji) - ui[q] * (1.0 - ratij));
+      }
+      rk[1] = rk[1] - g * ui[0] * (uj[0] + zj - ui[0] - zi) * cxe;
+      rk[2] = rk[2] - g * ui[0] * (uj[0] + zj - ui[0] - zi) * cye;
+    }
+    if (want_plain) {   // smb_2 (h <= 0 tests)
+      const double ratij = (ui[0] <= 0.0) ? 0.0 : Hij / ui[0];
+      const double ratji = (uj[0] <= 0.0) ? 0.0 : Hji / uj[0];
+      for (int q = 0; q < S; q++) {
+        double x2 = 0.0;
+        x2 = x2 - cxe * (v1j * uj[q]);
+        x2 = x2 - cye * (v2j * uj[q]);
+        rk2[q] = rk2[q] + x2 + d * (uj[q] * ratji - ui[q] * ratij) + mu * (uj[q] * (1.0 - ratji) - ui[q] * (1.0 - ratij));
+      }
+      rk2[1] = rk2[1] - g * ui[0] * (uj[0] + zj - ui[0] - zi) * cxe;
+      rk2[2] = rk2[2] - g * ui[0] * (uj[0] + zj - ui[0] - zi) * cye;
+    }
+    if (want_t1) {      // smb_1 (htiny tests, flux vv = velocity u_k)
+      const double ratij = (ui[0] <= htiny) ? 0.0 : Hij / ui[0];
+      const double ratji = (uj[0] <= htiny) ? 0.0 : Hji / uj[0];
+      for (int q = 0; q < S; q++) {
+        double xx = 0.0;
+        xx = xx - cxe * ((v1j * uj[q]) * ratji + (v1i * ui[q]) * ratij);
+        xx = xx - cye * ((v2j * uj[q]) * ratji + (v2i * ui[q]) * ratij);
+        rk1[q] = rk1[q] + xx + d * (uj[q] * ratji - ui[q] * ratij);
+      }
+      rk1[1] = rk1[1] - 0.5 * g * (Hji * Hji - Hij * Hij) * cxe;
+      rk1[2] = rk1[2] - 0.5 * g * (Hji * Hji - Hij * Hij) * cye;
+    }
+  }
+  // source terms
+  if (c.type_test == 13) {
+    // mSGN_RHS adds -pTilde_j c_ij after the smb loops, entry by entry, onto
+    // the momentum rows: redo that accumulation in entry order on top of rk.
+    double s_i, p_i;
+    sgn_node_f64(c, m, ui[0], ui[3], &p_i, &s_i);
+    double ax = rk[1], ay = rk[2], bx = rk2[1], by = rk2[2], tx = rk1[1], ty = rk1[2];
+    for (int kk = 0; kk <= L; kk++) {
+      const bool isd = (kk == dp);
+      const int64_t e = base + 32 * (kk - (kk > dp ? 1 : 0));
+      const int j = isd ? (int)r : G.col[e];
+      const double cxe = isd ? G.cxii[r] : G.cx[e], cye = isd ? G.cyii[r] : G.cy[e];
+      double pj, sj;
+      sgn_node_f64(c, G.lumped[j], u.h[j], u.q3[j], &pj, &sj);
+      ax = ax - pj * cxe; ay = ay - pj * cye;
+      bx = bx - pj * cxe; by = by - pj * cye;
+      tx = tx - pj * cxe; ty = ty - pj * cye;
+    }
+    if (want_round) source_f64(c, st, m, ui, v1i, v2i, rk, ax, ay, s_i);
+    if (want_plain) source_f64(c, st, m, ui, v1i, v2i, rk2, bx, by, s_i);
+    if (want_t1) source_f64(c, st, m, ui, v1i, v2i, rk1, tx, ty, s_i);
+  } else {
+    if (want_round) source_f64(c, st, m, ui, v1i, v2i, rk, 0, 0, 0);
+    if (want_plain) source_f64(c, st, m, ui, v1i, v2i, rk2, 0, 0, 0);
+    if (want_t1) source_f64(c, st, m, ui, v1i, v2i, rk1, 0, 0, 0);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // k_low: compute_dij + compute_muij + MAX + alpha_limit (update.f90:180-187,
 // 291-364, 782-798), smb_2_roundoff (:554-624) -> low-order state
@@ -143,9 +284,10 @@ __global__ void k_low_f64(Graph G, const InstConst* __restrict__ C, const InstSt
   bool delta_bad = false;
 
   // pass 1: raw d_ij (lambda_max) and mu_ij, diagonals = -row sums (the
-  // diagonal's own value, 0, adds nothing to the sums)
+  // diagonal's own value, 0, adds nothing to the sums).  'galerkin' sets
+  // every d_ij and mu_ij to 0 (update.f90:155-158).
   double sd = 0.0, sm = 0.0;
-  for (int k = 0; k < L; k++) {
+  for (int k = 0; k < (c.visc == VISC_GALERKIN ? 0 : L); k++) {
     const int64_t e = base + 32 * k;
     const int j = G.col[e];
     double d = 0.0, mu = 0.0;
@@ -186,7 +328,11 @@ __global__ void k_low_f64(Graph G, const InstConst* __restrict__ C, const InstSt
   sd = 0.0; sm = 0.0;
   double dii = tmax(dii_raw, muii_raw), muii = muii_raw;
   if (c.alpha_limit) dii = 0.0;
-  for (int kk = 0; kk <= L; kk++) {
+  if (c.visc == VISC_GALERKIN) {
+    for (int k = 0; k < L; k++) { dL[base + 32 * k] = 0.0; muL[base + 32 * k] = 0.0; }
+    dii = 0.0; muii = 0.0;
+  }
+  for (int kk = 0; kk <= (c.visc == VISC_GALERKIN ? -1 : L); kk++) {
     if (kk == dp) {
       sd = sd + dii;
       sm = sm + muii;
@@ -205,105 +351,46 @@ __global__ void k_low_f64(Graph G, const InstConst* __restrict__ C, const InstSt
     dL[e] = d;
     muL[e] = mu;
   }
-  if (c.alpha_limit) {
+  if (c.alpha_limit && c.visc != VISC_GALERKIN) {
     dii = -sd;
     muii = -sm;
   }
   dLii[r] = dii;
   muLii[r] = muii;
 
-  // pass 3: smb_2_roundoff and smb_2 rows, maxmin of the entropy, in
-  // reference order with the diagonal at dp
-  double rk[5] = {0, 0, 0, 0, 0}, rk2[5] = {0, 0, 0, 0, 0};
-  double fix = 0.0;
-  double emax = nd.ent[r], emin = emax;
-  for (int kk = 0; kk <= L; kk++) {
-    const bool isd = (kk == dp);
-    const int64_t e = base + 32 * (kk - (kk > dp ? 1 : 0));
-    const int j = isd ? (int)r : G.col[e];
-    double uj[5];
-    uj[0] = u.h[j]; uj[1] = u.q1[j]; uj[2] = u.q2[j];
-    if (S == 5) { uj[3] = u.q3[j]; uj[4] = u.q4[j]; }
-    const double zj = G.bath[j];
-    const double v1j = nd.v1[j], v2j = nd.v2[j];
-    const double d = isd ? dii : dL[e], mu = isd ? muii : muL[e];
-    const double cxe = isd ? G.cxii[r] : G.cx[e], cye = isd ? G.cyii[r] : G.cy[e];
-    const double ej = nd.ent[j];
-    emax = tmax(emax, ej);
-    emin = tmin(emin, ej);
-    const double zmax = tmax(zi, zj);
-    const double Hij = tmax(0.0, ui[0] + zi - zmax);
-    const double Hji = tmax(0.0, uj[0] + zj - zmax);
-    // smb_2_roundoff (htiny tests)
-    {
-      const double ratij = (ui[0] <= htiny) ? 0.0 : Hij / ui[0];
-      const double ratji = (uj[0] <= htiny) ? 0.0 : Hji / uj[0];
-      double xx = 0.0;
-      xx = xx - cxe * (v1j);
-      xx = xx - cye * (v2j);
-      if (isd) {
-        fix = fix + xx;
-      } else {
-        fix = fix - mu + (d - mu) * (-ratij);
-        rk[0] = rk[0] + (xx + mu) * uj[0] + tmax((d - mu) * Hji, 0.0);
-      }
-      for (int q = 1; q < S; q++) {
-        double x2 = 0.0;
-        x2 = x2 - cxe * (v1j * uj[q]);
-        x2 = x2 - cye * (v2j * uj[q]);
-        rk[q] = rk[q] + x2 + d * (uj[q] * ratji - ui[q] * ratij) + mu * (uj[q] * (1.0 - ratji) - ui[q] * (1.0 - ratij));
-      }
-      rk[1] = rk[1] - g * ui[0] * (uj[0] + zj - ui[0] - zi) * cxe;
-      rk[2] = rk[2] - g * ui[0] * (uj[0] + zj - ui[0] - zi) * cye;
-    }
-    // smb_2 (h <= 0 tests)
-    {
-      const double ratij = (ui[0] <= 0.0) ? 0.0 : Hij / ui[0];
-      const double ratji = (uj[0] <= 0.0) ? 0.0 : Hji / uj[0];
-      for (int q = 0; q < S; q++) {
-        double x2 = 0.0;
-        x2 = x2 - cxe * (v1j * uj[q]);
-        x2 = x2 - cye * (v2j * uj[q]);
-        rk2[q] = rk2[q] + x2 + d * (uj[q] * ratji - ui[q] * ratij) + mu * (uj[q] * (1.0 - ratji) - ui[q] * (1.0 - ratij));
-      }
-      rk2[1] = rk2[1] - g * ui[0] * (uj[0] + zj - ui[0] - zi) * cxe;
-      rk2[2] = rk2[2] - g * ui[0] * (uj[0] + zj - ui[0] - zi) * cye;
-    }
-  }
-  // source terms
-  if (c.type_test == 13) {
-    // mSGN_RHS adds -pTilde_j c_ij after the smb loops, entry by entry, onto
-    // the momentum rows: redo that accumulation in entry order on top of rk.
-    double s_i, p_i;
-    sgn_node_f64(c, m, ui[0], ui[3], &p_i, &s_i);
-    double ax = rk[1], ay = rk[2], bx = rk2[1], by = rk2[2];
-    for (int kk = 0; kk <= L; kk++) {
-      const bool isd = (kk == dp);
-      const int64_t e = base + 32 * (kk - (kk > dp ? 1 : 0));
-      const int j = isd ? (int)r : G.col[e];
-      const double cxe = isd ? G.cxii[r] : G.cx[e], cye = isd ? G.cyii[r] : G.cy[e];
-      double pj, sj;
-      sgn_node_f64(c, G.lumped[j], u.h[j], u.q3[j], &pj, &sj);
-      ax = ax - pj * cxe; ay = ay - pj * cye;
-      bx = bx - pj * cxe; by = by - pj * cye;
-    }
-    source_f64(c, st, m, ui, v1i, v2i, rk, ax, ay, s_i);
-    source_f64(c, st, m, ui, v1i, v2i, rk2, bx, by, s_i);
-  } else {
-    source_f64(c, st, m, ui, v1i, v2i, rk, 0, 0, 0);
-    source_f64(c, st, m, ui, v1i, v2i, rk2, 0, 0, 0);
-  }
-  // divide_by_lumped and the low-order state (update.f90:202-210)
-  for (int q = 0; q < S; q++) { rk[q] = rk[q] / m; rk2[q] = rk2[q] / m; }
+  // pass 3: smb_2_roundoff / smb_2 / smb_1 rows and maxmin of the entropy,
+  // in reference order with the diagonal at dp
+  const bool galerkin = c.visc == VISC_GALERKIN;
+  const bool type1 = !galerkin && c.viscous_type == 1;
+  const bool need_res = c.visc == VISC_ENTROPY || c.visc == VISC_FCT;
+  RowSums rs;
+  const LowVisc lv{dL, muL, dii, muii};
+  smb_rows_f64(G, c, st, u, nd, r, base, L, dp, ui, zi, m, lv,
+               !galerkin && !type1 && c.roundoff_fix,              // smb_2_roundoff: low order
+               galerkin || need_res || (!type1 && !c.roundoff_fix), // smb_2: Galerkin, residual, plain type2
+               type1, rs);
+  const double* rk2 = rs.rk2;
+  // divide_by_lumped (:801-808) and the low-order state (:202-215)
   double ul[5];
-  if (c.roundoff_fix) ul[0] = ui[0] * (1 + dt * fix / m) + dt * rk[0];
-  else ul[0] = tmax(ui[0] + dt * rk[0], 0.0);
-  for (int q = 1; q < S; q++) ul[q] = ui[q] + dt * rk[q];
+  if (type1) {
+    for (int q = 0; q < S; q++) ul[q] = ui[q] + dt * (rs.rk1[q] / m);
+  } else if (!galerkin && c.roundoff_fix) {
+    ul[0] = ui[0] * (1 + dt * rs.fix / m) + dt * (rs.rk[0] / m);
+    for (int q = 1; q < S; q++) ul[q] = ui[q] + dt * (rs.rk[q] / m);
+  } else {
+    ul[0] = tmax(ui[0] + dt * (rk2[0] / m), 0.0);
+    for (int q = 1; q < S; q++) ul[q] = ui[q] + dt * (rk2[q] / m);
+  }
   uL.h[r] = ul[0]; uL.q1[r] = ul[1]; uL.q2[r] = ul[2];
   if (S == 5) { uL.q3[r] = ul[3]; uL.q4[r] = ul[4]; }
+  if (delta_bad) atomicOr(err, ERRB_DELTA);
+  if (!need_res) return;
+  const double emax = rs.emax, emin = rs.emin;
+  double rk2m[5];
+  for (int q = 0; q < S; q++) rk2m[q] = rk2[q] / m;
   // entropy residual (update.f90:838-868), rescale hoisted
   double un_[5];
-  for (int q = 0; q < S; q++) un_[q] = ui[q] + dt * rk2[q];
+  for (int q = 0; q < S; q++) un_[q] = ui[q] + dt * rk2m[q];
   const double on = one_over_h(un_[0], htiny);
   const double vn1 = un_[1] * on, vn2 = un_[2] * on;
   double En = g * (un_[0] * un_[0]);
@@ -317,11 +404,10 @@ __global__ void k_low_f64(Graph G, const InstConst* __restrict__ C, const InstSt
   Ep[1] = v1i;
   Ep[0] = Ep[0] - 0.5 * (v2i * v2i);
   Ep[2] = v2i;
-  double rs = m * (En - E) / dt;
-  for (int q = 0; q < S; q++) rs = rs - m * rk2[q] * Ep[q];
+  double rsd = m * (En - E) / dt;
+  for (int q = 0; q < S; q++) rsd = rsd - m * rk2m[q] * Ep[q];
   const double rescale = tabs(emax - emin) / 2 + c.rescale_floor;
-  res[r] = tabs(rs) / rescale;
-  if (delta_bad) atomicOr(err, ERRB_DELTA);
+  res[r] = tabs(rsd) / rescale;
 }
 
 // ---------------------------------------------------------------------------
@@ -341,6 +427,7 @@ __global__ void k_fct_f64(Graph G, const InstConst* __restrict__ C, const InstSt
   const InstState st = St[b];
   if (st.done) return;
   const InstConst& c = C[b];
+  if (c.visc != VISC_FCT) return;
   const int64_t base = entry_base(G, r);
   const double hi = u.h[r], zi = G.bath[r], resi = res[r];
   double P = -1.e-15;
@@ -369,6 +456,47 @@ __global__ void k_fct_f64(Graph G, const InstConst* __restrict__ C, const InstSt
   rminus[r] = R;
 }
 
+// Component q of a state at row r (no local arrays of pointers: the row's
+// values stay in registers).
+__device__ __forceinline__ double comp_f64(const StateF64& s, int q, int64_t r) {
+  switch (q) {
+    case 0: return s.h[r];
+    case 1: return s.q1[r];
+    case 2: return s.q2[r];
+    case 3: return s.q3[r];
+    default: return s.q4[r];
+  }
+}
+__device__ __forceinline__ void store_f64(const StateF64& s, int q, int64_t r, double v) {
+  switch (q) {
+    case 0: s.h[r] = v; break;
+    case 1: s.q1[r] = v; break;
+    case 2: s.q2[r] = v; break;
+    case 3: s.q3[r] = v; break;
+    default: s.q4[r] = v; break;
+  }
+}
+
+// End of a stage for one row: check_hmin (when the mode has it), non-finite
+// check, the SSP-RK combination and bdy of the time loop (main.f90:77-90)
+// when rk_stage > 0, and the store.
+__device__ __forceinline__ void finish_row_f64(const Graph& G, int64_t r, int S, double (&un)[5], bool check_hmin,
+                                               int rk_stage, const StateF64& u0, const StateF64& out,
+                                               unsigned* err) {
+  if (check_hmin && un[0] < 0.0) atomicOr(err, ERRB_NEG_H);
+  if (!(un[0] == un[0]) || !(un[1] == un[1]) || !(un[2] == un[2])) atomicOr(err, ERRB_NAN);
+  const unsigned msk = (rk_stage >= 1 && G.dir_mask) ? G.dir_mask[r] : 0u;
+#pragma unroll
+  for (int q = 0; q < 5; q++) {
+    if (q >= S) break;
+    double v = un[q];
+    if (rk_stage == 2) v = (3 * comp_f64(u0, q, r) + v) / 4;
+    else if (rk_stage == 3) v = (comp_f64(u0, q, r) + 2 * v) / 3;
+    if (msk & (1u << q)) v = G.dir_val[(int64_t)q * G.n_rows + r];
+    store_f64(out, q, r, v);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // k_update: l_ij (fct.f90:31-41), (d^H-d^L) l_ij and (mu^H-mu^L) l_ij
 // (update.f90:278-279), apply_viscosity (:684-718), unext = u^L + dt rk/m
@@ -392,14 +520,16 @@ __global__ void k_update_f64(Graph G, const InstConst* __restrict__ C, const Ins
   const InstState st = St[b];
   if (st.done) return;
   const InstConst& c = C[b];
+  if (c.visc == VISC_ENTROPY) return;          // k_entropy_f64 writes these rows
+  const bool fct_mode = c.visc == VISC_FCT;
   const int S = c.S;
   const int64_t base = entry_base(G, r);
   double ui[5];
   ui[0] = u.h[r]; ui[1] = u.q1[r]; ui[2] = u.q2[r];
   if (S == 5) { ui[3] = u.q3[r]; ui[4] = u.q4[r]; }
-  const double zi = G.bath[r], resi = res[r], Ri = rminus[r];
+  const double zi = G.bath[r], resi = res[r], Ri = fct_mode ? rminus[r] : 0.0;
   double xx[5] = {0, 0, 0, 0, 0};
-  for (int k = 0; k < L; k++) {
+  for (int k = 0; k < (fct_mode ? L : 0); k++) {   // 'galerkin' / 'viscous': u^L is the result
     const int64_t e = base + 32 * k;
     const int j = G.col[e];
     const double f = fct[e];
@@ -422,23 +552,53 @@ __global__ void k_update_f64(Graph G, const InstConst* __restrict__ C, const Ins
       xx[q] = xx[q] + dd * (uj[q] * ratji - ui[q] * ratij) + dm * (uj[q] * (1.0 - ratji) - ui[q] * (1.0 - ratij));
   }
   const double m = G.lumped[r], dt = st.dt;
-  double un[5];
+  double un[5] = {0, 0, 0, 0, 0};
   const double* ulp[5] = {uL.h, uL.q1, uL.q2, uL.q3, uL.q4};
   for (int q = 0; q < S; q++) un[q] = ulp[q][r] + dt * (xx[q] / m);
-  if (un[0] < 0.0) atomicOr(err, ERRB_NEG_H);
-  if (!(un[0] == un[0]) || !(un[1] == un[1]) || !(un[2] == un[2])) atomicOr(err, ERRB_NAN);
-  if (rk_stage >= 2) {
-    const double* u0p[5] = {u0.h, u0.q1, u0.q2, u0.q3, u0.q4};
-    for (int q = 0; q < S; q++)
-      un[q] = (rk_stage == 2) ? (3 * u0p[q][r] + un[q]) / 4 : (u0p[q][r] + 2 * un[q]) / 3;
+  // check_hmin follows 'fct' (update.f90:285); 'viscous' and 'galerkin' return
+  // before it (:219-222, :155-176)
+  finish_row_f64(G, r, S, un, fct_mode, rk_stage, u0, out, err);
+}
+
+// ---------------------------------------------------------------------------
+// k_entropy: 'entropy_visc' (update.f90:225-262): the smb_2_roundoff (or
+// smb_2) rows with d^H = MIN(d, res_ij), mu^H = MIN(mu, res_ij), the update
+// u = u(1 + dt fix/m) + dt rk/m, check_hmin (:285), then the RK combination
+// and bdy like k_update.
+// ---------------------------------------------------------------------------
+__global__ void k_entropy_f64(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St,
+                              StateF64 u, NodeF64 nd, const double* __restrict__ dL, const double* __restrict__ muL,
+                              const double* __restrict__ dLii, const double* __restrict__ muLii,
+                              const double* __restrict__ res, StateF64 u0, StateF64 out, int rk_stage,
+                              unsigned* __restrict__ err) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= G.n_rows) return;
+  const int L = G.len[r];
+  if (L == 0) return;
+  const int b = G.slice_inst[r >> 5];
+  const InstState st = St[b];
+  if (st.done) return;
+  const InstConst& c = C[b];
+  if (c.visc != VISC_ENTROPY) return;
+  const int S = c.S;
+  const int64_t base = entry_base(G, r);
+  const int dp = G.dpos[r];
+  double ui[5];
+  ui[0] = u.h[r]; ui[1] = u.q1[r]; ui[2] = u.q2[r];
+  if (S == 5) { ui[3] = u.q3[r]; ui[4] = u.q4[r]; }
+  const double zi = G.bath[r], m = G.lumped[r], dt = st.dt;
+  const HighVisc hv{dL, muL, res, dLii[r], muLii[r], res[r]};
+  RowSums rs;
+  smb_rows_f64(G, c, st, u, nd, r, base, L, dp, ui, zi, m, hv, c.roundoff_fix != 0, c.roundoff_fix == 0, false, rs);
+  double un[5] = {0, 0, 0, 0, 0};
+  if (c.roundoff_fix) {
+    un[0] = ui[0] * (1 + dt * rs.fix / m) + dt * (rs.rk[0] / m);
+    for (int q = 1; q < S; q++) un[q] = ui[q] + dt * (rs.rk[q] / m);
+  } else {
+    un[0] = tmax(ui[0] + dt * (rs.rk2[0] / m), 0.0);
+    for (int q = 1; q < S; q++) un[q] = ui[q] + dt * (rs.rk2[q] / m);
   }
-  if (rk_stage >= 1 && G.dir_mask) {
-    const unsigned msk = G.dir_mask[r];
-    for (int q = 0; q < S; q++)
-      if (msk & (1u << q)) un[q] = G.dir_val[(int64_t)q * G.n_rows + r];
-  }
-  out.h[r] = un[0]; out.q1[r] = un[1]; out.q2[r] = un[2];
-  if (S == 5) { out.q3[r] = un[3]; out.q4[r] = un[4]; }
+  finish_row_f64(G, r, S, un, true, rk_stage, u0, out, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -550,6 +710,45 @@ __global__ void k_fct_positivity_f64(Graph G, const InstConst* __restrict__ C, c
   }
 }
 
+// FCT_generic (SOURCES/SAFE/fct.f90:3-43) as a stand-alone operator: the
+// two-sided Zalesak limiter with local bounds maxn/minn.  Pass 0: P+-, Q+-,
+// R+- per row (entries in reference order, the diagonal at dpos); pass 1:
+// sum_j l_ij f_ij with l_ij = MIN(R+_i, R-_j) (f >= 0) or MIN(R-_i, R+_j), and
+// u_i += x / dg_i.
+__global__ void k_fct_generic_f64(Graph G, double* __restrict__ unext, const double* __restrict__ maxn,
+                                  const double* __restrict__ minn, const double* __restrict__ dg,
+                                  const double* __restrict__ mat, const double* __restrict__ matii,
+                                  double* __restrict__ rplus, double* __restrict__ rminus, int pass) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= G.n_rows) return;
+  const int L = G.len[r];
+  if (L == 0) return;
+  const int64_t base = entry_base(G, r);
+  const int dp = G.dpos[r];
+  if (pass == 0) {
+    const double Qplus = dg[r] * (maxn[r] - unext[r]);
+    const double Qminus = dg[r] * (minn[r] - unext[r]);
+    double Pplus = 1.e-15, Pminus = -1.e-15;
+    for (int kk = 0; kk <= L; kk++) {
+      const double f = (kk == dp) ? matii[r] : mat[base + 32 * (kk - (kk > dp ? 1 : 0))];
+      if (f >= 0.0) Pplus = Pplus + f;
+      else Pminus = Pminus + f;
+    }
+    rplus[r] = tmin(Qplus / Pplus, 1.0);
+    rminus[r] = tmin(Qminus / Pminus, 1.0);
+  } else {
+    double x = 0.0;
+    for (int kk = 0; kk <= L; kk++) {
+      const int64_t e = base + 32 * (kk - (kk > dp ? 1 : 0));
+      const double f = (kk == dp) ? matii[r] : mat[e];
+      const int64_t j = (kk == dp) ? r : (int64_t)G.col[e];
+      const double l = (f >= 0.0) ? tmin(rplus[r], rminus[j]) : tmin(rminus[r], rplus[j]);
+      x = x + l * f;
+    }
+    unext[r] = unext[r] + x / dg[r];
+  }
+}
+
 // Total mass sum m_i h_i per instance, Kahan-compensated per thread then
 // combined in double-double per warp (atomics on two words per instance).
 __global__ void k_mass_f64(Graph G, const double* __restrict__ h, double* __restrict__ acc) {
@@ -594,6 +793,9 @@ void launch_stage_f64(const StageArgs& a, cudaStream_t s, const KernelEvents* ke
   EV_END(3); EV_BEGIN(4);
   k_update_f64<<<nblk(a.G.n_rows, bs), bs, 0, s>>>(a.G, a.C, a.St, a.u, a.w.dL, a.w.muL, a.w.uL, a.w.res, a.w.fct,
                                                    a.w.rminus, a.u0, a.out, a.rk_stage, a.lij_out, a.err);
+  if (a.entropy)
+    k_entropy_f64<<<nblk(a.G.n_rows, bs), bs, 0, s>>>(a.G, a.C, a.St, a.u, nd, a.w.dL, a.w.muL, a.w.dLii, a.w.muLii,
+                                                      a.w.res, a.u0, a.out, a.rk_stage, a.err);
   EV_END(4);
 }
 
@@ -614,6 +816,12 @@ void launch_fct_positivity_f64(const Graph& G, const InstConst* C, const double*
                                const double* matii, double* rtmp, double* lij, cudaStream_t s) {
   k_fct_positivity_f64<<<nblk(G.n_rows, 128), 128, 0, s>>>(G, C, unext, mat, matii, rtmp, lij, 0);
   k_fct_positivity_f64<<<nblk(G.n_rows, 128), 128, 0, s>>>(G, C, unext, mat, matii, rtmp, lij, 1);
+}
+
+void launch_fct_generic_f64(const Graph& G, double* unext, const double* maxn, const double* minn, const double* dg,
+                            const double* mat, const double* matii, double* rplus, double* rminus, cudaStream_t s) {
+  k_fct_generic_f64<<<nblk(G.n_rows, 128), 128, 0, s>>>(G, unext, maxn, minn, dg, mat, matii, rplus, rminus, 0);
+  k_fct_generic_f64<<<nblk(G.n_rows, 128), 128, 0, s>>>(G, unext, maxn, minn, dg, mat, matii, rplus, rminus, 1);
 }
 
 void launch_mass_f64(const Graph& G, const double* h, double* acc, cudaStream_t s) {

@@ -95,9 +95,15 @@ __device__ __forceinline__ LamK lam_k(float g, float htiny) { return LamK{g, hti
 __device__ __forceinline__ float phi_f(float h, float vl, float hl, float vr, float hr, float ovhl, float ovhr,
                                        float sql, float sqr, const LamK& k) {
   const float ovh = ovh_f(h, k.htiny);
-  const float sgh = sqrtf(k.g * h);
-  const float fl = (h > hl) ? (h - hl) * sqrtf(0.5f * k.g * (ovh + ovhl)) : 2.f * (sgh - sql);
-  const float fr = (h > hr) ? (h - hr) * sqrtf(0.5f * k.g * (ovh + ovhr)) : 2.f * (sgh - sqr);
+  float fl, fr;
+  if (h > hl && h > hr) {              // two shocks: the usual case at h = x0 h_min
+    fl = (h - hl) * sqrtf(0.5f * k.g * (ovh + ovhl));
+    fr = (h - hr) * sqrtf(0.5f * k.g * (ovh + ovhr));
+  } else {
+    const float sgh = sqrtf(k.g * h);
+    fl = (h > hl) ? (h - hl) * sqrtf(0.5f * k.g * (ovh + ovhl)) : 2.f * (sgh - sql);
+    fr = (h > hr) ? (h - hr) * sqrtf(0.5f * k.g * (ovh + ovhr)) : 2.f * (sgh - sqr);
+  }
   return fl + fr + vr - vl;
 }
 
@@ -227,6 +233,7 @@ __global__ void __launch_bounds__(256, MINB) k_low_mix(Graph G, const InstConst*
   const InstConst& c = C[b];
   const int S = c.S;
   const bool sgn = c.type_test == 13;
+  const bool galerkin = c.visc == VISC_GALERKIN;   // every d_ij, mu_ij = 0 (update.f90:155-158)
   const float g = c.gf, htiny = c.htinyf, dtf = st.dtf;
   const LamK lk = lam_k(g, htiny);
   const int64_t base = entry_base(G, r);
@@ -290,7 +297,7 @@ __global__ void __launch_bounds__(256, MINB) k_low_mix(Graph G, const InstConst*
     const float cvi = dotc(cxe, cye, ni.v1, ni.v2);                   // c.v_i (compute_muij)
     const float cvj = dotc(cxe, cye, nj.v1, nj.v2);                   // c.v_j
     float dlam;                                                       // |c_ij| lambda_max
-    if (LAMIN) {
+    if (LAMIN || galerkin) {
       dlam = dlb[q];                                                  // from k_dt_mix on this state
     } else {
       const float n2 = cxe * cxe + cye * cye;
@@ -300,8 +307,8 @@ __global__ void __launch_bounds__(256, MINB) k_low_mix(Graph G, const InstConst*
         delta_bad = true;
       dlam = (n2 * inv) * lam;
     }
-    float mu = fmaxf(fmaxf(-cvi, 0.f), fmaxf(cvj, 0.f));
-    float d = fmaxf(dlam, mu);
+    float mu = galerkin ? 0.f : fmaxf(fmaxf(-cvi, 0.f), fmaxf(cvj, 0.f));
+    float d = galerkin ? 0.f : fmaxf(dlam, mu);
     if (c.alpha_limit) {
       const float s = fmaxf(ai, alb[q]);
       d *= s;
@@ -383,15 +390,21 @@ __global__ void __launch_bounds__(256, MINB) k_low_mix(Graph G, const InstConst*
   const float a = dtf * invm;
   const float2 h = u.h[r];
   float2 hL;
-  if (c.roundoff_fix) {
+  if (c.roundoff_fix && !galerkin) {
     hL = df_add_f(h, a * __fmaf_rn(fix, ni.h, rk0));   // h + a (fix h + rk_1), a |fix| <= CFL
-  } else {
+    w.qL[r] = make_float2(ni.q1 + dtf * (rk1 * invm), ni.q2 + dtf * (rk2_ * invm));
+    if (S == 5) { w.q3L[r] = ui3 + dtf * (rk3 * invm); w.q4L[r] = ui4 + dtf * (rk4 * invm); }
+  } else {                                             // smb_2 and MAX(h + dt rk, 0)
     hL = df_add_f(h, a * g0);
     if (hL.x < 0.f) hL = make_float2(0.f, 0.f);
+    w.qL[r] = make_float2(ni.q1 + dtf * (g1 * invm), ni.q2 + dtf * (g2 * invm));
+    if (S == 5) { w.q3L[r] = ui3 + dtf * (g3 * invm); w.q4L[r] = ui4 + dtf * (g4 * invm); }
   }
   w.hL[r] = hL;
-  w.qL[r] = make_float2(ni.q1 + dtf * (rk1 * invm), ni.q2 + dtf * (rk2_ * invm));
-  if (S == 5) { w.q3L[r] = ui3 + dtf * (rk3 * invm); w.q4L[r] = ui4 + dtf * (rk4 * invm); }
+  if (c.visc != VISC_FCT) {
+    if (delta_bad) atomicOr(err, ERRB_DELTA);
+    return;
+  }
   // entropy residual (update.f90:838-868), rescale once per node
   const float un0 = ni.h + dtf * (g0 * invm);
   const float un1 = ni.q1 + dtf * (g1 * invm);
@@ -430,6 +443,7 @@ __global__ void __launch_bounds__(256) k_fct_mix(Graph G, const InstConst* __res
   const InstState& st = St[b];
   if (st.done) return;
   const InstConst& c = C[b];
+  if (c.visc != VISC_FCT) return;
   const int64_t base = entry_base(G, r);
   const float4 ni = u.nq[r];
   const float hi = ni.x, zi = ni.w, resi = res[r];
@@ -494,16 +508,17 @@ __global__ void __launch_bounds__(256) k_update_mix(Graph G, const InstConst* __
   if (st.done) return;
   const InstConst& c = C[b];
   const int S = c.S;
+  const bool fct_mode = c.visc == VISC_FCT;     // 'galerkin' / 'viscous': u^L is the result
   const int64_t base = entry_base(G, r);
   const float4 ni = u.nq[r];
-  const float hi = ni.x, zi = ni.w, resi = res[r];
+  const float hi = ni.x, zi = ni.w, resi = fct_mode ? res[r] : 0.f;
   const float invhi = inv_pos(hi);
-  const float Ri = w.rminus[r];
+  const float Ri = fct_mode ? w.rminus[r] : 0.f;
   float ui3 = 0.f, ui4 = 0.f;
   if (S == 5) { ui3 = u.q3[r]; ui4 = u.q4[r]; }
   float pos = 0.f;                       // sum_{f >= 0} R_j f_ij
   float x1 = 0.f, x2 = 0.f, x3 = 0.f, x4 = 0.f;
-  for (int k0 = 0; k0 < L; k0 += B) {    // the diagonal's terms vanish: (u_i rat_ii - u_i rat_ii) = 0
+  for (int k0 = 0; k0 < (fct_mode ? L : 0); k0 += B) {   // the diagonal's terms vanish: u_i rat_ii - u_i rat_ii = 0
    int jb[B];
    float d0b[B], m0b[B];
 #pragma unroll
@@ -544,14 +559,14 @@ __global__ void __launch_bounds__(256) k_update_mix(Graph G, const InstConst* __
    }
   }
   const float invm = G.inv_lumpedf[r], dtf = st.dtf;
-  const float sh = __fadd_rn(w.rneg[r], pos);
+  const float sh = fct_mode ? __fadd_rn(w.rneg[r], pos) : 0.f;
   float2 hn = df_add_f(w.hL[r], __fmul_rn(__fmul_rn(dtf, invm), sh));
   const float2 qL = w.qL[r];
   float q1 = qL.x + dtf * (x1 * invm);
   float q2 = qL.y + dtf * (x2 * invm);
   float q3 = 0.f, q4 = 0.f;
   if (S == 5) { q3 = w.q3L[r] + dtf * (x3 * invm); q4 = w.q4L[r] + dtf * (x4 * invm); }
-  if (hn.x < 0.f) atomicOr(err, ERRB_NEG_H);
+  if (fct_mode && hn.x < 0.f) atomicOr(err, ERRB_NEG_H);   // check_hmin follows 'fct' only
   if (!(hn.x == hn.x) || !(q1 == q1) || !(q2 == q2)) atomicOr(err, ERRB_NAN);
   if (rk_stage >= 2) {
     const float4 a0 = u0.nq[r];
@@ -583,10 +598,13 @@ __global__ void __launch_bounds__(256) k_update_mix(Graph G, const InstConst* __
   if (S == 5) { out.q3[r] = q3; out.q4[r] = q4; }
 }
 
-// k_dt_mix: FP32 lambda_max, max |d_ii|/m_i per instance (main.f90:166-174)
+// k_dt_mix: FP32 lambda_max, max |d_ii|/m_i per instance (main.f90:166-174).
+// It walks the neighbours of the state that stage 1 starts from, so it also
+// stores |c_ij| lambda_max per entry (dlam, reused by stage 1's k_low_mix)
+// and alpha_i (alpha_out, stage 1's k_node_mix), when those are non-null.
 template <int B>
 __global__ void __launch_bounds__(256) k_dt_mix(Graph G, const InstConst* __restrict__ C, InstState* __restrict__ St, StateMix u,
-                         float* __restrict__ dlam, unsigned* __restrict__ err) {
+                         float* __restrict__ dlam, float* __restrict__ alpha_out, unsigned* __restrict__ err) {
   int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   float val = 0.f;
   if (r < G.n_rows && G.len[r] > 0) {
@@ -600,6 +618,7 @@ __global__ void __launch_bounds__(256) k_dt_mix(Graph G, const InstConst* __rest
       const NodeF ni = node_from(u.nq[r], htiny);
       const float sqi = sqrtf(g * fabsf(ni.h));
       float s = 0.f;
+      float num = 0.f, denom = 0.f;          // alpha_limit stencil (as k_node_mix)
       bool bad = false;
       for (int k0 = 0; k0 < L; k0 += B) {
        int jb[B];
@@ -630,9 +649,20 @@ __global__ void __launch_bounds__(256) k_dt_mix(Graph G, const InstConst* __rest
         const float dl = (n2 * inv) * lam;
         if (dlam) dlam[base + 32 * (k0 + q)] = dl;
         s += dl;
+        num += nj.h - ni.h;
+        denom += fabsf(nj.h - ni.h);
        }
       }
       val = s * G.inv_lumpedf[r];
+      if (alpha_out) {
+        float alpha = 1.0f;
+        if (c.alpha_limit && !(ni.h <= c.htinyf)) {
+          const float a = (denom <= fabsf(num)) ? 1.0f : fdiv(fabsf(num), denom);
+          const float a2 = a * a, a4 = a2 * a2;
+          alpha = a4 * a4;
+        }
+        alpha_out[r] = alpha;
+      }
       if (bad) atomicOr(err, ERRB_DELTA);
     }
   }
@@ -724,14 +754,15 @@ void launch_kernel_mix(int kind, const StageArgsMix& a, const KernelTune& t, cud
 void launch_stage_mix(const StageArgsMix& a, cudaStream_t s, const KernelEvents* kev, const KernelTune& t) {
   for (int kind = 1; kind <= 4; kind++) {
     EV_BEGIN(kind);
-    launch_kernel_mix(kind, a, t, s);
+    // stage 1 follows k_dt_mix on the same state, which already stored alpha
+    if (!(kind == 1 && a.rk_stage == 1 && a.w.dlam)) launch_kernel_mix(kind, a, t, s);
     EV_END(kind);
   }
 }
 
-void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, float* dlam, unsigned* err,
-                   const KernelTune& t, cudaStream_t s) {
-  SWE_DISPATCH_B(t.batch[0], k_dt_mix, nblk(G.n_rows, t.block[0]), t.block[0], G, C, St, u, dlam, err)
+void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, float* dlam, float* alpha,
+                   unsigned* err, const KernelTune& t, cudaStream_t s) {
+  SWE_DISPATCH_B(t.batch[0], k_dt_mix, nblk(G.n_rows, t.block[0]), t.block[0], G, C, St, u, dlam, alpha, err)
 }
 
 void launch_refresh_z(const Graph& G, StateMix u, cudaStream_t s) {

@@ -33,7 +33,7 @@ EXPORTS = [
     "swe_create", "swe_create_batch", "swe_destroy", "swe_last_error", "swe_set_params", "swe_set_bath",
     "swe_set_dirichlet",
     "swe_sizes", "swe_get_matrices", "swe_compute_dij", "swe_euler", "swe_euler_intermediates",
-    "swe_fct_positivity", "swe_upload", "swe_download", "swe_upload_device", "swe_download_device",
+    "swe_fct_positivity", "swe_fct_generic", "swe_upload", "swe_download", "swe_upload_device", "swe_download_device",
     "swe_set_time", "swe_rk3_steps", "swe_mass", "swe_last_launch_count", "swe_tuning",
     "swe_last_device_ms", "swe_profile_kernels", "swe_fct_positivity_noalloc", "swe_autotune",
 ]
@@ -78,6 +78,7 @@ def load(build: bool = True):
         "swe_euler": ([vp, ctypes.c_int, dp, dp], ctypes.c_int),
         "swe_euler_intermediates": ([vp, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp, dp], ctypes.c_int),
         "swe_fct_positivity": ([vp, ctypes.c_int, dp, dp, dp], ctypes.c_int),
+        "swe_fct_generic": ([vp, ctypes.c_int, dp, dp, dp, dp, dp], ctypes.c_int),
         "swe_upload": ([vp, dp], ctypes.c_int),
         "swe_download": ([vp, dp], ctypes.c_int),
         "swe_upload_device": ([vp, ctypes.c_void_p], ctypes.c_int),

@@ -139,6 +139,16 @@ class Update:
         self._check(self._L.swe_fct_positivity(self.h, inst, _L.dp(u), _L.dp(f), _L.dp(lij)))
         return lij
 
+    def fct_generic(self, unext, maxn, minn, fctmat, dg=None, inst=0):
+        """FCT_generic (SOURCES/SAFE/fct.f90:3-43): returns the limited copy of
+        unext; dg defaults to the lumped mass."""
+        u = np.array(unext, np.float64)
+        a = [np.ascontiguousarray(x, np.float64) for x in (maxn, minn, fctmat)]
+        d = None if dg is None else np.ascontiguousarray(dg, np.float64)
+        self._check(self._L.swe_fct_generic(self.h, inst, _L.dp(u), _L.dp(a[0]), _L.dp(a[1]), _L.dp(a[2]),
+                                            None if d is None else _L.dp(d)))
+        return u
+
     # ---- device-resident time loop ----------------------------------------
     def upload(self, un):
         """un: (S, sum np) concatenation of the instances' states, or a list."""

@@ -83,6 +83,60 @@ def test_euler_stage_and_intermediates_bit_exact(golden):
         np.testing.assert_array_equal(inter[k], dump[k], err_msg=k)
 
 
+MODES = [  # (viscosity_type, viscous_type, if_roundoff_fix)
+    ("galerkin", 2, 1), ("viscous", 1, 1), ("viscous", 2, 1), ("viscous", 2, 0),
+    ("entropy_visc", 2, 1), ("entropy_visc", 2, 0), ("fct", 2, 0),
+]
+
+
+@pytest.mark.parametrize("visc,vtype,roundoff", MODES)
+def test_viscosity_modes_fp64_bit_exact(visc, vtype, roundoff):
+    """Every viscosity_type / viscous_type / roundoff combination of euler
+    (update.f90:134-289): one stage and three RK3 steps equal the oracle."""
+    base = C.dam_break_case(n=21, tfinal=0.05)
+    p = replace(base.params, viscosity_type=C.VISC[visc], viscous_type=vtype, if_roundoff_fix=roundoff)
+    case = replace(base, params=p)
+    o = _oracle_for(case)
+    u = case.u0.copy(order="F")
+    _, dt = o.compute_dij(u)
+    pd = replace(p, dt=dt)
+    o.set_params(oracle.Params(*pd.fields()))
+    upd = from_case(case)
+    upd.set_params(pd)
+    np.testing.assert_array_equal(upd.euler(u), o.euler(u))
+    o.set_params(oracle.Params(*p.fields()))
+    upd.set_params(p)
+    t = 0.0
+    for _ in range(3):
+        t = o.rk3_step(u, t)
+    upd.upload(case.u0)
+    upd.set_time(0.0, 1e30)
+    upd.rk3_steps(3)
+    np.testing.assert_array_equal(upd.download(), u)
+
+
+@pytest.mark.parametrize("visc", ["galerkin", "viscous"])
+def test_viscosity_modes_mixed(visc):
+    """'galerkin' and 'viscous' in mixed precision against the FP64 oracle."""
+    base = C.dam_break_case(n=41, tfinal=0.05)
+    p = replace(base.params, viscosity_type=C.VISC[visc], precision=1)
+    case = replace(base, params=p)
+    u, ug, n, ng, lump = _mixed_vs_oracle(case, nsteps=5)
+    assert _rel_l1(ug[0], u[0], lump) <= MIXED_L1_TOL
+
+
+def test_mode_combinations_the_reference_stops_on():
+    base = C.dam_break_case(n=11)
+    for visc in ("entropy_visc", "fct"):
+        p = replace(base.params, viscosity_type=C.VISC[visc], viscous_type=1)
+        with pytest.raises(L.SweError) as ei:
+            from_case(replace(base, params=p))
+        assert ei.value.code == L.SWE_ERR_ARG
+    p = replace(base.params, viscosity_type=C.VISC["entropy_visc"], precision=1)
+    with pytest.raises(L.SweError):
+        from_case(replace(base, params=p))
+
+
 def test_fct_positivity_operator_bit_exact():
     rng = np.random.default_rng(7)
     mesh = M.jittered_mesh(15, 15, 0, 1, 0, 1, seed=7)
@@ -93,6 +147,27 @@ def test_fct_positivity_operator_bit_exact():
     hs = rng.random(225) * 2e-3        # straddles the htiny test
     f = rng.normal(size=nnz)
     np.testing.assert_array_equal(upd.fct_positivity(hs, f), o.fct_positivity(hs, f))
+
+
+def test_fct_generic_operator_bit_exact():
+    """FCT_generic (two-sided Zalesak, SAFE/fct.f90:3-43) through the C ABI vs
+    the oracle: random bounds that make some R+- < 1 and zero fluxes."""
+    rng = np.random.default_rng(8)
+    mesh = M.jittered_mesh(17, 13, 0, 1, 0, 1, seed=8)
+    n = mesh["rr"].shape[1]
+    case = C.Case("x", mesh, C.Params(htiny=1e-3, dt=1e-3), np.zeros(n), np.zeros((3, n), order="F"), 1.0)
+    upd = from_case(case)
+    o = _oracle_for(case)
+    nnz = upd.sizes()[1]
+    u = rng.random(n)
+    maxn = u + rng.random(n) * 0.02
+    minn = u - rng.random(n) * 0.02
+    f = rng.normal(size=nnz) * 0.01
+    f[rng.random(nnz) < 0.1] = 0.0
+    lump = o.matrices()["lumped"]
+    np.testing.assert_array_equal(upd.fct_generic(u, maxn, minn, f), o.fct_generic(u, maxn, minn, f, lump))
+    dg = rng.random(n) + 0.5
+    np.testing.assert_array_equal(upd.fct_generic(u, maxn, minn, f, dg), o.fct_generic(u, maxn, minn, f, dg))
 
 
 def test_rk3_trajectory_matches_golden(golden):
