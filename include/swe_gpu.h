@@ -140,6 +140,24 @@ int swe_fct_positivity(swe_ctx* ctx, int inst, const double* unext, const double
 int swe_fct_generic(swe_ctx* ctx, int inst, double* unext, const double* maxn, const double* minn,
                     const double* mat, const double* dg);
 
+/* Gauss weights rj (3 per element) and points rr_gauss ((2, 3*me)
+ * column-major) of the 3-point rule (SFEMaNS/GAUSS_POINTS_OBJET/
+ * gauss_points_2d_p1.f90, r_gauss of SOURCES/main.f90:207), in the caller's
+ * element order, to evaluate analytic data for swe_norms.  Either may be
+ * NULL. */
+int swe_gauss_points(swe_ctx* ctx, int inst, double* rj, double* rr_gauss);
+
+/* Quadrature norms of one field of the device-resident state (after
+ * swe_upload / swe_rk3_steps), with no download of the state:
+ * l1 = sum |f - f_anal| rj, l2 = sqrt(sum (f - f_anal)^2 rj) over the Gauss
+ * points (ns_anal_l1, ns_anal_0, ns_l1: SFEMaNS/FEMSUB_OBJET/
+ * fem_tn.f90:1513-1553, 1679-1716).  field: component 0..syst_size-1, or
+ * SWE_FIELD_H32 for h^(3/2) (the monitor of SOURCES/main.f90:94-99).
+ * f_anal: 3 values per element at the Gauss points, or NULL for zero.
+ * l1, l2 may be NULL. */
+#define SWE_FIELD_H32 16
+int swe_norms(swe_ctx* ctx, int inst, int field, const double* f_anal, double* l1, double* l2);
+
 /* Device-resident fast path.  upload/download move every instance's state;
  * un is the concatenation of the instances' un(S, np_b) blocks. */
 int swe_upload(swe_ctx* ctx, const double* un);

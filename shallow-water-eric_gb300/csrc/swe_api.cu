@@ -62,6 +62,12 @@ struct swe_ctx {
   StateMix mA{}, mB{}, mC{};
   WorkMix wm{};
   double* d_mass_acc = nullptr;
+  // diagnostics: per-instance element lists and Gauss weights, on first use
+  std::vector<int*> d_jj_inst;
+  std::vector<double*> d_rj_inst;
+  double* d_norm_acc = nullptr;
+  double* d_fanal = nullptr;
+  size_t fanal_cap = 0;
   // graph of `graph_steps` time steps
   cudaGraphExec_t gexec = nullptr;
   int graph_steps = 0;
@@ -461,8 +467,11 @@ static int create_common(swe_ctx** out, int n_inst, const int* np, const int* me
     baths[b].assign(bath + roff, bath + roff + np[b]);
     joff += (int64_t)3 * me[b];
     roff += np[b];
-    std::string e = construct_matrices(m);
-    if (!e.empty()) { *out = c; return fail(c, SWE_ERR_MESH, e); }
+    std::string e = construct_matrices_device(m);   // CSR pattern + mass/c_ij assembly on the GPU
+    if (!e.empty()) {
+      *out = c;
+      return fail(c, e.rfind("device setup", 0) == 0 ? SWE_ERR_CUDA : SWE_ERR_MESH, e);
+    }
   }
   *out = c;
   if (cuda_check(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate")) return SWE_ERR_CUDA;
@@ -748,6 +757,51 @@ SWE_API int swe_fct_generic(swe_ctx* c, int inst, double* unext, const double* m
   return SWE_OK;
 }
 
+SWE_API int swe_gauss_points(swe_ctx* c, int inst, double* rj, double* rr_gauss) {
+  if (!c || inst < 0 || inst >= c->n_inst) return fail(c, SWE_ERR_ARG, "bad instance");
+  gauss_points(c->meshes[inst], rj, rr_gauss);
+  return SWE_OK;
+}
+
+SWE_API int swe_norms(swe_ctx* c, int inst, int field, const double* f_anal, double* l1, double* l2) {
+  if (!c || inst < 0 || inst >= c->n_inst) return fail(c, SWE_ERR_ARG, "bad instance");
+  if (!((field >= 0 && field < c->S) || field == SWE_FIELD_H32)) return fail(c, SWE_ERR_ARG, "bad field");
+  const HostMesh& m = c->meshes[inst];
+  cudaError_t st = cudaSuccess;
+  if (c->d_jj_inst.empty()) {
+    c->d_jj_inst.assign(c->n_inst, nullptr);
+    c->d_rj_inst.assign(c->n_inst, nullptr);
+    c->d_norm_acc = c->buf.alloc<double>(4, st);
+  }
+  if (!c->d_jj_inst[inst]) {
+    std::vector<double> rj((size_t)3 * m.me);
+    gauss_points(m, rj.data(), nullptr);
+    c->d_jj_inst[inst] = c->buf.alloc<int>(m.jj.size(), st);
+    c->d_rj_inst[inst] = c->buf.alloc<double>(rj.size(), st);
+    if (st == cudaSuccess) st = cudaMemcpy(c->d_jj_inst[inst], m.jj.data(), m.jj.size() * sizeof(int),
+                                           cudaMemcpyHostToDevice);
+    if (st == cudaSuccess) st = cudaMemcpy(c->d_rj_inst[inst], rj.data(), rj.size() * sizeof(double),
+                                           cudaMemcpyHostToDevice);
+  }
+  if (f_anal && c->fanal_cap < (size_t)3 * m.me) {
+    c->d_fanal = c->buf.alloc<double>((size_t)3 * m.me, st);
+    c->fanal_cap = (size_t)3 * m.me;
+  }
+  if (st != cudaSuccess) return cuda_check(c, st, "swe_norms allocation");
+  if (f_anal)
+    CK(cudaMemcpyAsync(c->d_fanal, f_anal, (size_t)3 * m.me * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemsetAsync(c->d_norm_acc, 0, 4 * sizeof(double), c->stream));
+  launch_norms(field, c->precision == SWE_PREC_FP64 ? 0 : 1, c->A, c->mA, c->d_jj_inst[inst], c->d_rj_inst[inst],
+               m.me, c->d_row_of_node + c->node_off[inst], f_anal ? c->d_fanal : nullptr, c->d_norm_acc, c->stream);
+  CK(cudaGetLastError());
+  double acc[4];
+  CK(cudaMemcpyAsync(acc, c->d_norm_acc, sizeof acc, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (l1) *l1 = acc[0] + acc[1];
+  if (l2) *l2 = std::sqrt(acc[2] + acc[3]);
+  return SWE_OK;
+}
+
 SWE_API int swe_upload(swe_ctx* c, const double* un) {
   if (!c || !un) return fail(c, SWE_ERR_ARG, "bad arguments");
   int rc = to_device(c, un, false, 0, c->node_off[c->n_inst]);
@@ -819,7 +873,8 @@ static int autotune(swe_ctx* c) {
   CK(cudaEventCreate(&e1));
   const int blocks[3] = {64, 128, 256};
   const int batches[4] = {1, 2, 4, 8};
-  // k_low is timed as in stages 2 and 3 (lambda_max computed, not reused)
+  // kernels are timed as in stages 2 and 3 (k_low computes lambda_max, k_update
+  // reads u0 for the RK combination): two of the three stages of a step
   StageArgsMix a_low = a;
   a_low.rk_stage = 2;
   std::string desc;
@@ -839,7 +894,7 @@ static int autotune(swe_ctx* c) {
           for (int rep = 0; rep < 3; rep++) {
             cudaEventRecord(e0, s);
             if (kind == 0) launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->wm.dlam, c->wm.alpha, c->d_err, v, s);
-            else launch_kernel_mix(kind, kind == 2 ? a_low : a, v, s);
+            else launch_kernel_mix(kind, a_low, v, s);
             cudaEventRecord(e1, s);
             CK(cudaEventSynchronize(e1));
             float ms = 0.f;

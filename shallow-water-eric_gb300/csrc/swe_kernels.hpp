@@ -105,6 +105,11 @@ void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const Stat
 void launch_refresh_z(const Graph& G, StateMix u, cudaStream_t s);
 void launch_mass_mix(const Graph& G, const float2* h, double* acc, cudaStream_t s);
 
+// Diagnostics (swe_diag.cu): field index kFieldH32 selects h^(3/2)
+constexpr int kFieldH32 = 16;
+void launch_norms(int field, int precision, const StateF64& a, const StateMix& mx, const int* jj, const double* rj,
+                  int me, const int* row_of_node, const double* f_anal, double* acc, cudaStream_t s);
+
 // kernels launched per stage / per step (for launch accounting)
 constexpr int kLaunchesPerStage = 4;
 constexpr int kLaunchesPerStepExtra = 3;   // k_dt, k_step_begin, k_step_end

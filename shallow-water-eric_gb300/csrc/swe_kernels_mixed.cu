@@ -234,8 +234,13 @@ __global__ void __launch_bounds__(256, MINB) k_low_mix(Graph G, const InstConst*
   const int S = c.S;
   const bool sgn = c.type_test == 13;
   const bool galerkin = c.visc == VISC_GALERKIN;   // every d_ij, mu_ij = 0 (update.f90:155-158)
+  const float vis = galerkin ? 0.f : 1.f;
   const float g = c.gf, htiny = c.htinyf, dtf = st.dtf;
   const LamK lk = lam_k(g, htiny);
+  // the low-order momenta: smb_2_roundoff's htiny tests, or smb_2's h <= 0
+  // tests (rat = 0 already where h <= 0) when the step is not roundoff-fixed
+  const bool roundoff = c.roundoff_fix && !galerkin;
+  const float hthr = roundoff ? htiny : 0.f;
   const int64_t base = entry_base(G, r);
   const NodeF ni = node_from(u.nq[r], htiny);
   const float sqi = sqrtf(g * fabsf(ni.h));
@@ -297,7 +302,7 @@ __global__ void __launch_bounds__(256, MINB) k_low_mix(Graph G, const InstConst*
     const float cvi = dotc(cxe, cye, ni.v1, ni.v2);                   // c.v_i (compute_muij)
     const float cvj = dotc(cxe, cye, nj.v1, nj.v2);                   // c.v_j
     float dlam;                                                       // |c_ij| lambda_max
-    if (LAMIN || galerkin) {
+    if (LAMIN) {
       dlam = dlb[q];                                                  // from k_dt_mix on this state
     } else {
       const float n2 = cxe * cxe + cye * cye;
@@ -307,13 +312,11 @@ __global__ void __launch_bounds__(256, MINB) k_low_mix(Graph G, const InstConst*
         delta_bad = true;
       dlam = (n2 * inv) * lam;
     }
-    float mu = galerkin ? 0.f : fmaxf(fmaxf(-cvi, 0.f), fmaxf(cvj, 0.f));
-    float d = galerkin ? 0.f : fmaxf(dlam, mu);
-    if (c.alpha_limit) {
-      const float s = fmaxf(ai, alb[q]);
-      d *= s;
-      mu *= s;
-    }
+    float mu = fmaxf(fmaxf(-cvi, 0.f), fmaxf(cvj, 0.f));
+    float d = fmaxf(dlam, mu);
+    const float s = (c.alpha_limit ? fmaxf(ai, alb[q]) : 1.f) * vis;
+    d *= s;
+    mu *= s;
     dL[e] = d;
     muL[e] = mu;
     // --- entropy stencil
@@ -325,8 +328,8 @@ __global__ void __launch_bounds__(256, MINB) k_low_mix(Graph G, const InstConst*
     const float dz = nj.z - ni.z;
     const Recon R = recon(ni.h, nj.h, dz, invhi, inv_pos(nj.h));
     const float rij = R.rij, rji = R.rji;                             // h <= 0 tests (smb_2)
-    const float rijt = (ni.h <= htiny) ? 0.f : rij;                   // h <= htiny tests
-    const float rjit = (nj.h <= htiny) ? 0.f : rji;
+    const float rijt = (ni.h <= hthr) ? 0.f : rij;                    // h <= htiny tests
+    const float rjit = (nj.h <= hthr) ? 0.f : rji;
     const float cvj_flux = sgn ? dotc(cxe, cye, nj.v1, 0.f) : cvj;   // c.velocity_j of flux()
     const float topo = g * ni.h * ((nj.h - ni.h) + dz);               // g h_i (eta_j - eta_i)
     // --- smb_2_roundoff mass row (fix_roundoff, rk_1), in the reference's
@@ -390,21 +393,15 @@ __global__ void __launch_bounds__(256, MINB) k_low_mix(Graph G, const InstConst*
   const float a = dtf * invm;
   const float2 h = u.h[r];
   float2 hL;
-  if (c.roundoff_fix && !galerkin) {
+  if (roundoff) {
     hL = df_add_f(h, a * __fmaf_rn(fix, ni.h, rk0));   // h + a (fix h + rk_1), a |fix| <= CFL
-    w.qL[r] = make_float2(ni.q1 + dtf * (rk1 * invm), ni.q2 + dtf * (rk2_ * invm));
-    if (S == 5) { w.q3L[r] = ui3 + dtf * (rk3 * invm); w.q4L[r] = ui4 + dtf * (rk4 * invm); }
   } else {                                             // smb_2 and MAX(h + dt rk, 0)
     hL = df_add_f(h, a * g0);
     if (hL.x < 0.f) hL = make_float2(0.f, 0.f);
-    w.qL[r] = make_float2(ni.q1 + dtf * (g1 * invm), ni.q2 + dtf * (g2 * invm));
-    if (S == 5) { w.q3L[r] = ui3 + dtf * (g3 * invm); w.q4L[r] = ui4 + dtf * (g4 * invm); }
   }
   w.hL[r] = hL;
-  if (c.visc != VISC_FCT) {
-    if (delta_bad) atomicOr(err, ERRB_DELTA);
-    return;
-  }
+  w.qL[r] = make_float2(ni.q1 + dtf * (rk1 * invm), ni.q2 + dtf * (rk2_ * invm));
+  if (S == 5) { w.q3L[r] = ui3 + dtf * (rk3 * invm); w.q4L[r] = ui4 + dtf * (rk4 * invm); }
   // entropy residual (update.f90:838-868), rescale once per node
   const float un0 = ni.h + dtf * (g0 * invm);
   const float un1 = ni.q1 + dtf * (g1 * invm);
@@ -491,6 +488,42 @@ __global__ void __launch_bounds__(256) k_fct_mix(Graph G, const InstConst* __res
   w.rneg[r] = __fmul_rn(R, neg);
 }
 
+// End of a stage for one row: non-finite check, the SSP-RK combination and
+// bdy of the time loop (main.f90:77-90) when rk_stage > 0, and the store.
+__device__ __forceinline__ void finish_mix(const Graph& G, const InstConst& c, int64_t r, int S, float2 hn, float q1,
+                                           float q2, float q3, float q4, float zi, int rk_stage, const StateMix& u0,
+                                           const StateMix& out, unsigned* err) {
+  if (!(hn.x == hn.x) || !(q1 == q1) || !(q2 == q2)) atomicOr(err, ERRB_NAN);
+  if (rk_stage >= 2) {
+    const float4 a0 = u0.nq[r];
+    const float2 h0 = u0.h[r];
+    if (rk_stage == 2) {
+      hn = df_scale(df_add(df_mul_f(h0, 3.f), hn), 0.25f);
+      q1 = (3.f * a0.y + q1) * 0.25f;
+      q2 = (3.f * a0.z + q2) * 0.25f;
+      if (S == 5) { q3 = (3.f * u0.q3[r] + q3) * 0.25f; q4 = (3.f * u0.q4[r] + q4) * 0.25f; }
+    } else {
+      hn = df_div3(df_add(h0, df_scale(hn, 2.f)));
+      q1 = (a0.y + 2.f * q1) * (1.f / 3.f);
+      q2 = (a0.z + 2.f * q2) * (1.f / 3.f);
+      if (S == 5) { q3 = (u0.q3[r] + 2.f * q3) * (1.f / 3.f); q4 = (u0.q4[r] + 2.f * q4) * (1.f / 3.f); }
+    }
+  }
+  if (rk_stage >= 1 && G.dir_mask) {
+    const unsigned msk = G.dir_mask[r];
+    if (msk) {
+      if (msk & 1u) hn = df_from_double(G.dir_val[r]);
+      if (msk & 2u) q1 = (float)G.dir_val[G.n_rows + r];
+      if (msk & 4u) q2 = (float)G.dir_val[2 * G.n_rows + r];
+      if (S == 5 && (msk & 8u)) q3 = (float)G.dir_val[3 * G.n_rows + r];
+      if (S == 5 && (msk & 16u)) q4 = (float)G.dir_val[4 * G.n_rows + r];
+    }
+  }
+  out.h[r] = hn;
+  out.nq[r] = make_float4(shadow_df(hn, c), q1, q2, zi);
+  if (S == 5) { out.q3[r] = q3; out.q4[r] = q4; }
+}
+
 // k_update_mix: limited antidiffusion (update.f90:276-282, apply_viscosity
 // :684-718), RK combination and Dirichlet data (main.f90:77-90).  The h-row
 // sum is R^-_i P_i (from k_fct_mix) plus sum_{f_ij >= 0} R^-_j f_ij.
@@ -508,17 +541,22 @@ __global__ void __launch_bounds__(256) k_update_mix(Graph G, const InstConst* __
   if (st.done) return;
   const InstConst& c = C[b];
   const int S = c.S;
-  const bool fct_mode = c.visc == VISC_FCT;     // 'galerkin' / 'viscous': u^L is the result
-  const int64_t base = entry_base(G, r);
   const float4 ni = u.nq[r];
-  const float hi = ni.x, zi = ni.w, resi = fct_mode ? res[r] : 0.f;
+  if (c.visc != VISC_FCT) {                     // 'galerkin' / 'viscous': u^L is the result
+    const float2 qL = w.qL[r];
+    finish_mix(G, c, r, S, w.hL[r], qL.x, qL.y, S == 5 ? w.q3L[r] : 0.f, S == 5 ? w.q4L[r] : 0.f, ni.w, rk_stage,
+               u0, out, err);
+    return;
+  }
+  const int64_t base = entry_base(G, r);
+  const float hi = ni.x, zi = ni.w, resi = res[r];
   const float invhi = inv_pos(hi);
-  const float Ri = fct_mode ? w.rminus[r] : 0.f;
+  const float Ri = w.rminus[r];
   float ui3 = 0.f, ui4 = 0.f;
   if (S == 5) { ui3 = u.q3[r]; ui4 = u.q4[r]; }
   float pos = 0.f;                       // sum_{f >= 0} R_j f_ij
   float x1 = 0.f, x2 = 0.f, x3 = 0.f, x4 = 0.f;
-  for (int k0 = 0; k0 < (fct_mode ? L : 0); k0 += B) {   // the diagonal's terms vanish: u_i rat_ii - u_i rat_ii = 0
+  for (int k0 = 0; k0 < L; k0 += B) {    // the diagonal's terms vanish: u_i rat_ii - u_i rat_ii = 0
    int jb[B];
    float d0b[B], m0b[B];
 #pragma unroll
@@ -559,43 +597,15 @@ __global__ void __launch_bounds__(256) k_update_mix(Graph G, const InstConst* __
    }
   }
   const float invm = G.inv_lumpedf[r], dtf = st.dtf;
-  const float sh = fct_mode ? __fadd_rn(w.rneg[r], pos) : 0.f;
-  float2 hn = df_add_f(w.hL[r], __fmul_rn(__fmul_rn(dtf, invm), sh));
+  const float sh = __fadd_rn(w.rneg[r], pos);
+  const float2 hn = df_add_f(w.hL[r], __fmul_rn(__fmul_rn(dtf, invm), sh));
   const float2 qL = w.qL[r];
-  float q1 = qL.x + dtf * (x1 * invm);
-  float q2 = qL.y + dtf * (x2 * invm);
+  const float q1 = qL.x + dtf * (x1 * invm);
+  const float q2 = qL.y + dtf * (x2 * invm);
   float q3 = 0.f, q4 = 0.f;
   if (S == 5) { q3 = w.q3L[r] + dtf * (x3 * invm); q4 = w.q4L[r] + dtf * (x4 * invm); }
-  if (fct_mode && hn.x < 0.f) atomicOr(err, ERRB_NEG_H);   // check_hmin follows 'fct' only
-  if (!(hn.x == hn.x) || !(q1 == q1) || !(q2 == q2)) atomicOr(err, ERRB_NAN);
-  if (rk_stage >= 2) {
-    const float4 a0 = u0.nq[r];
-    const float2 h0 = u0.h[r];
-    if (rk_stage == 2) {
-      hn = df_scale(df_add(df_mul_f(h0, 3.f), hn), 0.25f);
-      q1 = (3.f * a0.y + q1) * 0.25f;
-      q2 = (3.f * a0.z + q2) * 0.25f;
-      if (S == 5) { q3 = (3.f * u0.q3[r] + q3) * 0.25f; q4 = (3.f * u0.q4[r] + q4) * 0.25f; }
-    } else {
-      hn = df_div3(df_add(h0, df_scale(hn, 2.f)));
-      q1 = (a0.y + 2.f * q1) * (1.f / 3.f);
-      q2 = (a0.z + 2.f * q2) * (1.f / 3.f);
-      if (S == 5) { q3 = (u0.q3[r] + 2.f * q3) * (1.f / 3.f); q4 = (u0.q4[r] + 2.f * q4) * (1.f / 3.f); }
-    }
-  }
-  if (rk_stage >= 1 && G.dir_mask) {
-    const unsigned msk = G.dir_mask[r];
-    if (msk) {
-      if (msk & 1u) hn = df_from_double(G.dir_val[r]);
-      if (msk & 2u) q1 = (float)G.dir_val[G.n_rows + r];
-      if (msk & 4u) q2 = (float)G.dir_val[2 * G.n_rows + r];
-      if (S == 5 && (msk & 8u)) q3 = (float)G.dir_val[3 * G.n_rows + r];
-      if (S == 5 && (msk & 16u)) q4 = (float)G.dir_val[4 * G.n_rows + r];
-    }
-  }
-  out.h[r] = hn;
-  out.nq[r] = make_float4(shadow_df(hn, c), q1, q2, zi);
-  if (S == 5) { out.q3[r] = q3; out.q4[r] = q4; }
+  if (hn.x < 0.f) atomicOr(err, ERRB_NEG_H);   // check_hmin (update.f90:285)
+  finish_mix(G, c, r, S, hn, q1, q2, q3, q4, zi, rk_stage, u0, out, err);
 }
 
 // k_dt_mix: FP32 lambda_max, max |d_ii|/m_i per instance (main.f90:166-174).

@@ -1,5 +1,5 @@
-// Host-side setup: CSR pattern, mass, lumped mass, diag and c_ij following
-// the reference's arithmetic order, then the GB300 edge-graph layout.
+// Host-side setup: the RCM renumbering and the GB300 edge-graph layout of
+// matrices assembled on the device (swe_setup_gpu.cu).
 #include "swe_setup.hpp"
 
 #include <algorithm>
@@ -9,51 +9,7 @@
 
 namespace swe {
 
-// CSR pattern of st_csr (SFEMaNS/FEMSUB/st_sparsekit.f90:788-863): row i
-// holds i and every node sharing an element with i, sorted ascending.  The
-// reference caps rows at nparm = 90 entries (:801, :836-839).
-static std::string build_pattern(HostMesh& m) {
-  const int nparm = 90;
-  std::vector<int> ecount(m.np + 1, 0);
-  for (int e = 0; e < m.me; e++)
-    for (int n = 0; n < 3; n++) ecount[m.jj[e * 3 + n] + 1]++;
-  for (int i = 0; i < m.np; i++) ecount[i + 1] += ecount[i];
-  std::vector<int> elist(ecount[m.np]);
-  std::vector<int> fill(ecount.begin(), ecount.end() - 1);
-  for (int e = 0; e < m.me; e++)
-    for (int n = 0; n < 3; n++) elist[fill[m.jj[e * 3 + n]]++] = e;
-  m.ia.assign(m.np + 1, 0);
-  std::vector<int> buf;
-  std::vector<std::vector<int>> rows(m.np);
-  for (int i = 0; i < m.np; i++) {
-    buf.clear();
-    buf.push_back(i);
-    for (int q = ecount[i]; q < ecount[i + 1]; q++)
-      for (int n = 0; n < 3; n++) buf.push_back(m.jj[elist[q] * 3 + n]);
-    std::sort(buf.begin(), buf.end());
-    buf.erase(std::unique(buf.begin(), buf.end()), buf.end());
-    if ((int)buf.size() > nparm) return "a CSR row exceeds 90 entries (st_csr nparm)";
-    rows[i] = buf;
-    m.ia[i + 1] = m.ia[i] + (int)buf.size();
-  }
-  m.ja.resize(m.ia[m.np]);
-  for (int i = 0; i < m.np; i++) std::copy(rows[i].begin(), rows[i].end(), m.ja.begin() + m.ia[i]);
-  return "";
-}
-
-static inline int find_p(const HostMesh& m, int i, int j) {
-  for (int p = m.ia[i]; p < m.ia[i + 1]; p++) if (m.ja[p] == j) return p;
-  return -1;
-}
-
-std::string construct_matrices(HostMesh& m) {
-  for (int q = 0; q < 3 * m.me; q++)
-    if (m.jj[q] < 0 || m.jj[q] >= m.np) return "element node index out of range";
-  std::string err = build_pattern(m);
-  if (!err.empty()) return err;
-  const size_t nnz = m.ja.size();
-  // P1 reference element and 3-point rule of gauss_points_2d_p1
-  // (SFEMaNS/GAUSS_POINTS_OBJET/gauss_points_2d_p1.f90:95-128, 347-393).
+void gauss_points(const HostMesh& m, double* rj, double* rr_gauss) {
   const double one = 1, two = 2, three = 3, six = 6;
   const double xx[3] = {one / six, two / three, one / six};
   const double yy[3] = {one / six, one / six, two / three};
@@ -61,12 +17,9 @@ std::string construct_matrices(HostMesh& m) {
   double ww[3][3];
   for (int l = 0; l < 3; l++) { ww[0][l] = one - xx[l] - yy[l]; ww[1][l] = xx[l]; ww[2][l] = yy[l]; }
   const double pp = one / six;
-  m.mass.assign(nnz, 0.0);
-  m.cx.assign(nnz, 0.0);
-  m.cy.assign(nnz, 0.0);
+#pragma omp parallel for schedule(static)
   for (int e = 0; e < m.me; e++) {
     const int nd[3] = {m.jj[e * 3], m.jj[e * 3 + 1], m.jj[e * 3 + 2]};
-    double dw[3][3][2], rj[3];   // dw[l][n][d]
     for (int l = 0; l < 3; l++) {
       double dr[2][2];
       for (int k = 0; k < 2; k++)
@@ -76,67 +29,15 @@ std::string construct_matrices(HostMesh& m) {
           dr[k][k1] = s;
         }
       const double rjac = dr[0][0] * dr[1][1] - dr[0][1] * dr[1][0];
-      for (int n = 0; n < 3; n++) {
-        dw[l][n][0] = (+dd[0][n] * dr[1][1] - dd[1][n] * dr[1][0]) / rjac;
-        dw[l][n][1] = (-dd[0][n] * dr[0][1] + dd[1][n] * dr[0][0]) / rjac;
-      }
-      rj[l] = rjac * pp;
-    }
-    // consistent mass, qs_00_M (SFEMaNS/FEMSUB_OBJET/fem_sparsekit.f90:6-53)
-    for (int l = 0; l < 3; l++) {
-      const double al = 1.0 * rj[l];
-      for (int nj = 0; nj < 3; nj++)
-        for (int ni = 0; ni < 3; ni++) {
-          const double x = ww[nj][l] * al * ww[ni][l];
-          const int p = find_p(m, nd[ni], nd[nj]);
-          m.mass[p] = m.mass[p] + x;
-        }
-    }
-  }
-  // c_ij = sum_K int_K grad(phi_j) phi_i (SOURCES/update.f90:100-124), in the
-  // reference's loop order: elements, then ni, then nj.
-  for (int e = 0; e < m.me; e++) {
-    const int nd[3] = {m.jj[e * 3], m.jj[e * 3 + 1], m.jj[e * 3 + 2]};
-    double dw[3][3][2], rj[3];
-    for (int l = 0; l < 3; l++) {
-      double dr[2][2];
-      for (int k = 0; k < 2; k++)
-        for (int k1 = 0; k1 < 2; k1++) {
+      if (rj) rj[(size_t)e * 3 + l] = rjac * pp;
+      if (rr_gauss)
+        for (int k = 0; k < 2; k++) {
           double s = 0.0;
-          for (int n = 0; n < 3; n++) s = s + m.rr[(size_t)nd[n] * 2 + k] * dd[k1][n];
-          dr[k][k1] = s;
+          for (int n = 0; n < 3; n++) s = s + ww[n][l] * m.rr[(size_t)nd[n] * 2 + k];
+          rr_gauss[((size_t)e * 3 + l) * 2 + k] = s;
         }
-      const double rjac = dr[0][0] * dr[1][1] - dr[0][1] * dr[1][0];
-      for (int n = 0; n < 3; n++) {
-        dw[l][n][0] = (+dd[0][n] * dr[1][1] - dd[1][n] * dr[1][0]) / rjac;
-        dw[l][n][1] = (-dd[0][n] * dr[0][1] + dd[1][n] * dr[0][0]) / rjac;
-      }
-      rj[l] = rjac * pp;
     }
-    for (int ni = 0; ni < 3; ni++)
-      for (int nj = 0; nj < 3; nj++) {
-        double x[2];
-        for (int d = 0; d < 2; d++) {
-          double s = 0.0;
-          for (int l = 0; l < 3; l++) s = s + dw[l][nj][d] * ww[ni][l] * rj[l];
-          x[d] = s;
-        }
-        const int p = find_p(m, nd[ni], nd[nj]);
-        m.cx[p] = m.cx[p] + x[0];
-        m.cy[p] = m.cy[p] + x[1];
-      }
   }
-  // lumped = row sums of the mass (SOURCES/update.f90:35-38); diag (:41-49)
-  m.lumped.assign(m.np, 0.0);
-  m.diag.assign(m.np, -1);
-  for (int i = 0; i < m.np; i++) {
-    double s = 0.0;
-    for (int p = m.ia[i]; p < m.ia[i + 1]; p++) s = s + m.mass[p];
-    m.lumped[i] = s;
-    m.diag[i] = find_p(m, i, i);
-    if (!(s > 0.0)) return "non-positive lumped mass (clockwise or degenerate triangle)";
-  }
-  return "";
 }
 
 // Reverse Cuthill-McKee: BFS from a pseudo-peripheral node of each connected
@@ -211,10 +112,14 @@ Layout build_layout(const std::vector<HostMesh>& meshes, const std::vector<std::
   L.slice_inst.assign(L.n_slices, 0);
   L.slice_w.assign(L.n_slices, 0);
   L.new_of_old.resize(L.n_inst);
+  std::vector<std::vector<int>> nofs(L.n_inst);
+#pragma omp parallel for schedule(dynamic)
+  for (int b = 0; b < L.n_inst; b++) nofs[b] = rcm_order(meshes[b]);   // sequential per instance
   for (int b = 0; b < L.n_inst; b++) {
     const HostMesh& m = meshes[b];
-    std::vector<int> nof = rcm_order(m);
+    const std::vector<int>& nof = nofs[b];
     L.new_of_old[b].resize(m.np);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < m.np; i++) {
       int64_t r = L.row_off[b] + nof[i];
       L.new_of_old[b][i] = (int)r;
@@ -231,17 +136,19 @@ Layout build_layout(const std::vector<HostMesh>& meshes, const std::vector<std::
     for (int64_t s = L.row_off[b] / 32; s < L.row_off[b + 1] / 32; s++) L.slice_inst[s] = b;
   }
   L.slice_ptr.assign(L.n_slices + 1, 0);
+#pragma omp parallel for schedule(static)
   for (int64_t s = 0; s < L.n_slices; s++) {
     uint8_t w = 0;
     for (int l = 0; l < 32; l++) w = std::max(w, L.len[s * 32 + l]);
     L.slice_w[s] = w;
-    L.slice_ptr[s + 1] = L.slice_ptr[s] + 32 * (int64_t)w;
   }
+  for (int64_t s = 0; s < L.n_slices; s++) L.slice_ptr[s + 1] = L.slice_ptr[s] + 32 * (int64_t)L.slice_w[s];
   L.n_entries = L.slice_ptr[L.n_slices];
   L.col.assign(L.n_entries, 0);
   L.cx.assign(L.n_entries, 0.0);
   L.cy.assign(L.n_entries, 0.0);
   L.ref_pos.assign(L.n_entries, -1);
+#pragma omp parallel for schedule(static)
   for (int64_t s = 0; s < L.n_slices; s++)
     for (int l = 0; l < 32; l++) {
       int64_t r = s * 32 + l;
@@ -249,6 +156,7 @@ Layout build_layout(const std::vector<HostMesh>& meshes, const std::vector<std::
     }
   for (int b = 0; b < L.n_inst; b++) {
     const HostMesh& m = meshes[b];
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < m.np; i++) {
       int64_t r = L.new_of_old[b][i];
       int64_t base = L.slice_ptr[r / 32] + (r % 32);

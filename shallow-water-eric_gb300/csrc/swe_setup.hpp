@@ -1,7 +1,6 @@
-// Host-side setup of the edge graph: the reference's construct_matrices
-// (SOURCES/update.f90:18-132) plus the GB300 layout (RCM renumbering, SELL-32
-// slices).  Compiled with -ffp-contract=off so the assembled matrices are
-// bit-identical on x86-64 and aarch64 hosts.
+// Setup of the edge graph: the reference's construct_matrices
+// (SOURCES/update.f90:18-132) on the device, then the GB300 layout (RCM
+// renumbering, SELL-32 slices) on the host.
 #pragma once
 #include <cstdint>
 #include <string>
@@ -20,8 +19,14 @@ struct HostMesh {
   std::vector<int> diag;                 // CSR position of (i, i)
 };
 
-// Builds ia/ja/mass/lumped/diag/cx/cy.  Returns "" or an error message.
-std::string construct_matrices(HostMesh& m);
+// Builds ia/ja/mass/lumped/diag/cx/cy on the current CUDA device
+// (swe_setup_gpu.cu) and copies them into m.  Returns "" or an error message.
+std::string construct_matrices_device(HostMesh& m);
+
+// Weights rj (3 per element) and points rr_gauss ((2, 3 me)) of the 3-point
+// rule of gauss_points_2d_p1 (SFEMaNS/GAUSS_POINTS_OBJET/
+// gauss_points_2d_p1.f90:95-128, 347-393); either may be null.
+void gauss_points(const HostMesh& m, double* rj, double* rr_gauss);
 
 // Reverse Cuthill-McKee ordering of the CSR graph: new_of_old[old] = new.
 std::vector<int> rcm_order(const HostMesh& m);

@@ -29,6 +29,8 @@ UNITS = {
     "swe_kernels_mixed.cu": ["--use_fast_math", "-Xptxas", "-warn-spills"],
     "swe_api.cu": [],
     "swe_noalloc.cu": ["-fmad=false"],
+    "swe_setup_gpu.cu": ["-fmad=false"],
+    "swe_diag.cu": ["-fmad=false"],
     "swe_setup.cpp": None,   # host C++
 }
 
@@ -47,8 +49,8 @@ def _compile(src: str, extra, verbose=False):
     if o.exists() and o.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
         return o
     if extra is None:
-        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off", f"-I{INCLUDE}",
-               "-c", str(s), "-o", str(o)]
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off", "-fopenmp",
+               f"-I{INCLUDE}", "-c", str(s), "-o", str(o)]
     else:
         cmd = [_nvcc(), *NVCC_COMMON, *extra, "-c", str(s), "-o", str(o)]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -69,7 +71,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         objs = list(ex.map(lambda kv: _compile(kv[0], kv[1], verbose), UNITS.items()))
     if not LIB.exists() or any(o.stat().st_mtime > LIB.stat().st_mtime for o in objs):
         tmp = LIB.with_name(f"libswe_gpu.{os.getpid()}.so")
-        cmd = [_nvcc(), "-shared", *ARCH, "-o", str(tmp), *map(str, objs)]
+        cmd = [_nvcc(), "-shared", *ARCH, "-Xcompiler", "-fopenmp", "-o", str(tmp), *map(str, objs)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

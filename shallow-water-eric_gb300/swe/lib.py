@@ -13,6 +13,7 @@ import numpy as np
 
 from . import build as _build
 
+FIELD_H32 = 16
 SWE_OK, SWE_ERR_NEG_H, SWE_ERR_DELTA, SWE_ERR_NAN, SWE_ERR_TIMEOUT, SWE_ERR_CUDA, SWE_ERR_ARG, SWE_ERR_MESH = range(8)
 ERROR_NAMES = {1: "NEG_H", 2: "DELTA", 3: "NAN", 4: "TIMEOUT", 5: "CUDA", 6: "ARG", 7: "MESH"}
 
@@ -33,7 +34,7 @@ EXPORTS = [
     "swe_create", "swe_create_batch", "swe_destroy", "swe_last_error", "swe_set_params", "swe_set_bath",
     "swe_set_dirichlet",
     "swe_sizes", "swe_get_matrices", "swe_compute_dij", "swe_euler", "swe_euler_intermediates",
-    "swe_fct_positivity", "swe_fct_generic", "swe_upload", "swe_download", "swe_upload_device", "swe_download_device",
+    "swe_fct_positivity", "swe_fct_generic", "swe_gauss_points", "swe_norms", "swe_upload", "swe_download", "swe_upload_device", "swe_download_device",
     "swe_set_time", "swe_rk3_steps", "swe_mass", "swe_last_launch_count", "swe_tuning",
     "swe_last_device_ms", "swe_profile_kernels", "swe_fct_positivity_noalloc", "swe_autotune",
 ]
@@ -79,6 +80,8 @@ def load(build: bool = True):
         "swe_euler_intermediates": ([vp, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp, dp], ctypes.c_int),
         "swe_fct_positivity": ([vp, ctypes.c_int, dp, dp, dp], ctypes.c_int),
         "swe_fct_generic": ([vp, ctypes.c_int, dp, dp, dp, dp, dp], ctypes.c_int),
+        "swe_gauss_points": ([vp, ctypes.c_int, dp, dp], ctypes.c_int),
+        "swe_norms": ([vp, ctypes.c_int, ctypes.c_int, dp, dp, dp], ctypes.c_int),
         "swe_upload": ([vp, dp], ctypes.c_int),
         "swe_download": ([vp, dp], ctypes.c_int),
         "swe_upload_device": ([vp, ctypes.c_void_p], ctypes.c_int),

@@ -37,6 +37,7 @@ class Update:
         self.params = [p for _, _, p in items]
         self.np_ = np.array([m["rr"].shape[1] for m, _, _ in items], np.int32)
         me = np.array([m["jj"].shape[1] for m, _, _ in items], np.int32)
+        self._me = me
         jj = np.concatenate([np.asfortranarray(m["jj"], np.int32).ravel(order="F") for m, _, _ in items])
         rr = np.concatenate([np.asfortranarray(m["rr"], np.float64).ravel(order="F") for m, _, _ in items])
         bb = np.concatenate([np.ascontiguousarray(b, np.float64) for _, b, _ in items])
@@ -148,6 +149,23 @@ class Update:
         self._check(self._L.swe_fct_generic(self.h, inst, _L.dp(u), _L.dp(a[0]), _L.dp(a[1]), _L.dp(a[2]),
                                             None if d is None else _L.dp(d)))
         return u
+
+    # ---- diagnostics on the device-resident state ---------------------------
+    def gauss_points(self, inst=0):
+        """(rj (3 me,), rr_gauss (2, 3 me)) of the 3-point rule."""
+        me = int(self._me[inst])
+        rj = np.zeros(3 * me); rg = np.zeros(6 * me)
+        self._check(self._L.swe_gauss_points(self.h, inst, _L.dp(rj), _L.dp(rg)))
+        return rj, rg.reshape(-1, 2).T.copy()
+
+    def norms(self, field=0, f_anal=None, inst=0):
+        """(L1, L2) quadrature norms of field - f_anal on the device state
+        (ns_anal_l1 / ns_anal_0); field may be lib.FIELD_H32."""
+        fa = None if f_anal is None else np.ascontiguousarray(f_anal, np.float64)
+        l1 = ctypes.c_double(); l2 = ctypes.c_double()
+        self._check(self._L.swe_norms(self.h, inst, field, None if fa is None else _L.dp(fa),
+                                      ctypes.byref(l1), ctypes.byref(l2)))
+        return l1.value, l2.value
 
     # ---- device-resident time loop ----------------------------------------
     def upload(self, un):

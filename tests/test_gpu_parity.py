@@ -137,6 +137,30 @@ def test_mode_combinations_the_reference_stops_on():
         from_case(replace(base, params=p))
 
 
+def test_device_norms_match_oracle(golden):
+    """compute_errors' quadrature norms on the device state vs the oracle
+    (ns_anal_l1, ns_anal_0; order-independent sums: 1e-13 relative)."""
+    case = _thacker(golden, "0.1", periods=1.0, cfl=0.3)
+    for prec in (0, 1):
+        upd = from_case(case, precision=prec)
+        o = _oracle_for(case)
+        rj_g, rg_g = upd.gauss_points()
+        rj_o, rg_o = o.gauss()
+        np.testing.assert_array_equal(rj_g, rj_o)
+        np.testing.assert_array_equal(rg_g, rg_o)
+        upd.upload(case.u0)
+        upd.set_time(0.0, 1e30)
+        upd.rk3_steps(10)
+        u = upd.download()
+        ex = case.exact(1, rg_o, 0.0)
+        for field, f_anal in ((0, ex), (0, None), (1, None), (L.FIELD_H32, None)):
+            g1, g2 = upd.norms(field, f_anal)
+            ff = u[0] * np.sqrt(u[0]) if field == L.FIELD_H32 else u[field]
+            o1, o2 = o.norms(ff, np.zeros_like(rj_o) if f_anal is None else f_anal)
+            assert g1 == pytest.approx(o1, rel=1e-13, abs=1e-300)
+            assert g2 == pytest.approx(o2, rel=1e-13, abs=1e-300)
+
+
 def test_fct_positivity_operator_bit_exact():
     rng = np.random.default_rng(7)
     mesh = M.jittered_mesh(15, 15, 0, 1, 0, 1, seed=7)
