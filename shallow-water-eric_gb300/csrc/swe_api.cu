@@ -248,7 +248,7 @@ static int build_device(swe_ctx* c, const std::vector<std::vector<double>>& bath
     WorkMix& w = c->wm;
     w.alpha = c->buf.alloc<float>(n, st); w.res = c->buf.alloc<float>(n, st);
     w.rminus = c->buf.alloc<float>(n, st); w.rneg = c->buf.alloc<float>(n, st);
-    w.dL = c->buf.alloc<float>(ne, st); w.muL = c->buf.alloc<float>(ne, st);
+    w.dmu = c->buf.alloc<float2>(ne, st);
     w.dlam = c->buf.alloc<float>(ne, st);
     w.hL = c->buf.alloc<float2>(n, st);
     w.qL = c->buf.alloc<float2>(n, st);
@@ -585,8 +585,12 @@ SWE_API int swe_get_matrices(swe_ctx* c, int inst, int* ia, int* ja, double* mas
 
 // copy a per-entry device array of one instance back into CSR order; the
 // diagonal positions come from a per-row device array (or are 0 if null)
+template <typename T> static double comp_of(const T& v, int) { return (double)v; }
+static double comp_of(const float2& v, int k) { return (double)(k ? v.y : v.x); }
+
 template <typename T, typename U = T>
-static int entries_to_csr(swe_ctx* c, int inst, const T* d_arr, double* out, const U* d_diag_rows = nullptr) {
+static int entries_to_csr(swe_ctx* c, int inst, const T* d_arr, double* out, const U* d_diag_rows = nullptr,
+                          int comp = 0) {
   const Layout& L = c->L;
   const int64_t s0 = L.row_off[inst] / 32, s1 = L.row_off[inst + 1] / 32;
   const int64_t e0 = L.slice_ptr[s0], e1 = L.slice_ptr[s1];
@@ -598,7 +602,7 @@ static int entries_to_csr(swe_ctx* c, int inst, const T* d_arr, double* out, con
     CK(cudaMemcpyAsync(hd.data(), d_diag_rows + r0, (r1 - r0) * sizeof(U), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   for (int64_t e = e0; e < e1; e++)
-    if (L.ref_pos[e] >= 0) out[L.ref_pos[e]] = (double)h[e - e0];
+    if (L.ref_pos[e] >= 0) out[L.ref_pos[e]] = comp_of(h[e - e0], comp);
   for (int64_t r = r0; r < r1; r++)
     if (L.ref_pos_diag[r] >= 0) out[L.ref_pos_diag[r]] = (double)hd[r - r0];
   return SWE_OK;
@@ -684,8 +688,8 @@ SWE_API int swe_euler_intermediates(swe_ctx* c, int inst, double* dij_low, doubl
     if (u_low && (rc = from_device_state(c, u_low, false, c->node_off[inst], c->node_off[inst + 1], &c->w.uL, nullptr)))
       return rc;
   } else {
-    if (dij_low && (rc = entries_to_csr(c, inst, c->wm.dL, dij_low))) return rc;
-    if (muij_low && (rc = entries_to_csr(c, inst, c->wm.muL, muij_low))) return rc;
+    if (dij_low && (rc = entries_to_csr(c, inst, c->wm.dmu, dij_low, (const float*)nullptr, 0))) return rc;
+    if (muij_low && (rc = entries_to_csr(c, inst, c->wm.dmu, muij_low, (const float*)nullptr, 1))) return rc;
     if (alpha && (rc = rows_to_nodes(c, inst, c->wm.alpha, alpha))) return rc;
     if (res && (rc = rows_to_nodes(c, inst, c->wm.res, res))) return rc;
     if (rminus && (rc = rows_to_nodes(c, inst, c->wm.rminus, rminus))) return rc;
@@ -881,34 +885,40 @@ static int autotune(swe_ctx* c) {
   const char* names[5] = {"dt", "node", "low", "fct", "update"};
   for (int kind = 0; kind < 5; kind++) {
     float best = 1e30f;
-    int bb = t.block[kind], bt = t.batch[kind], bc = t.cap_low;
+    int bb = t.block[kind], bt = t.batch[kind], bc = t.cap_low, bg = t.grid[kind];
     for (int ib = 0; ib < 3; ib++)
       for (int it = 0; it < 4; it++)
-        for (int cap = 0; cap < (kind == 2 ? 2 : 1); cap++) {
-          if (kind == 2 && batches[it] > 2) continue;
-          KernelTune v = t;
-          v.block[kind] = blocks[ib];
-          v.batch[kind] = batches[it];
-          if (kind == 2) v.cap_low = cap;
-          float tmin = 1e30f;
-          for (int rep = 0; rep < 3; rep++) {
-            cudaEventRecord(e0, s);
-            if (kind == 0) launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->wm.dlam, c->wm.alpha, c->d_err, v, s);
-            else launch_kernel_mix(kind, a_low, v, s);
-            cudaEventRecord(e1, s);
-            CK(cudaEventSynchronize(e1));
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, e0, e1);
-            tmin = std::min(tmin, ms);
+        for (int cap = 0; cap < (kind == 2 ? 2 : 1); cap++)
+          for (int gm = 0; gm < 2; gm++) {
+            if (kind == 2 && batches[it] > 2) continue;
+            KernelTune v = t;
+            v.block[kind] = blocks[ib];
+            v.batch[kind] = batches[it];
+            v.grid[kind] = gm;
+            if (kind == 2) v.cap_low = cap;
+            float tmin = 1e30f;
+            for (int rep = 0; rep < 3; rep++) {
+              cudaEventRecord(e0, s);
+              if (kind == 0) launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->wm.dlam, c->wm.alpha, c->d_err, v, s);
+              else launch_kernel_mix(kind, a_low, v, s);
+              cudaEventRecord(e1, s);
+              CK(cudaEventSynchronize(e1));
+              float ms = 0.f;
+              cudaEventElapsedTime(&ms, e0, e1);
+              tmin = std::min(tmin, ms);
+            }
+            if (tmin < best) {
+              best = tmin; bb = blocks[ib]; bt = batches[it]; bg = gm;
+              if (kind == 2) bc = cap;
+            }
           }
-          if (tmin < best) { best = tmin; bb = blocks[ib]; bt = batches[it]; if (kind == 2) bc = cap; }
-        }
     t.block[kind] = bb;
     t.batch[kind] = bt;
+    t.grid[kind] = bg;
     if (kind == 2) t.cap_low = bc;
-    char buf[80];
-    snprintf(buf, sizeof buf, "%s%s:block%d/batch%d%s", kind ? " " : "", names[kind], bb, bt,
-             kind == 2 ? (bc ? "/regs64" : "/regs85") : "");
+    char buf[96];
+    snprintf(buf, sizeof buf, "%s%s:block%d/batch%d%s%s", kind ? " " : "", names[kind], bb, bt,
+             kind == 2 ? (bc ? "/regs64" : "/regs85") : "", bg ? "/resident" : "");
     desc += buf;
   }
   cudaEventDestroy(e0);

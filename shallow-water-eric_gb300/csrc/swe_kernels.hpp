@@ -37,7 +37,7 @@ struct WorkMix {
   float *alpha, *res;                    // per row
   float* rminus;                         // per row: R^-_i
   float* rneg;                           // per row: R^-_i * sum_{f_ij<0} f_ij
-  float *dL, *muL;                       // per entry
+  float2* dmu;                           // per entry: (d_ij, mu_ij), one 8-byte load
   float* dlam;                           // per entry: |c_ij| lambda_max from k_dt_mix (stage 1)
   float2* hL;                            // low-order depth (double-float)
   float2* qL;                            // low-order momenta
@@ -86,15 +86,17 @@ void launch_fct_generic_f64(const Graph& G, double* unext, const double* maxn, c
 void launch_mass_f64(const Graph& G, const double* h, double* acc, cudaStream_t s);
 
 // Launch configuration of the mixed kernels, per kernel kind (0 dt, 1 node,
-// 2 low, 3 fct, 4 update): block size and entry batch (1, 2, 4 or 8; 1 or 2
-// for low), and for low the tighter of two register caps (cap_low: 64
-// instead of 85 registers).  Chosen by the
+// 2 low, 3 fct, 4 update): block size, entry batch (1, 2, 4 or 8; 1 or 2
+// for low), grid (one thread per row, or a resident grid striding over the
+// rows), and for low the tighter of two register caps (cap_low: 64 instead of
+// 85 registers).  Chosen by the
 // autotuner in swe_api.cu.  Every choice sums in the same entry order; the
 // variants are separate instantiations whose FMA contraction may differ, so
 // results agree to FP32 rounding.
 struct KernelTune {
   int block[5] = {128, 128, 128, 128, 128};
   int batch[5] = {1, 1, 1, 1, 1};
+  int grid[5] = {0, 0, 0, 0, 0};   // 0: a thread per row; k: k resident grids striding over the rows
   int cap_low = 0;
 };
 

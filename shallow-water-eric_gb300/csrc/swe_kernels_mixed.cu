@@ -153,11 +153,9 @@ __device__ __forceinline__ bool lambda_f(float hl, float hr, float vl, float vr,
 
 // k_node_mix: alpha_i (SOURCES/update.f90:758-781) from the FP32 depth.
 template <int B>
-__global__ void __launch_bounds__(256) k_node_mix(Graph G, const InstConst* __restrict__ C,
+__device__ __forceinline__ void node_row(int64_t r, Graph G, const InstConst* __restrict__ C,
                                                   const InstState* __restrict__ St, StateMix u,
                                                   float* __restrict__ alpha_out) {
-  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (r >= G.n_rows) return;
   const int L = G.len[r];
   if (L == 0) return;
   const int b = G.slice_inst[r >> 5];
@@ -190,6 +188,14 @@ __global__ void __launch_bounds__(256) k_node_mix(Graph G, const InstConst* __re
   alpha_out[r] = alpha;
 }
 
+template <int B>
+__global__ void __launch_bounds__(256) k_node_mix(Graph G, const InstConst* __restrict__ C,
+                                                  const InstState* __restrict__ St, StateMix u,
+                                                  float* __restrict__ alpha_out) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < G.n_rows; r += (int64_t)gridDim.x * blockDim.x)
+    node_row<B>(r, G, C, St, u, alpha_out);
+}
+
 struct NodeF {   // FP32 view of one node used by the edge loop
   float h, q1, q2, z, ovh, v1, v2;
 };
@@ -218,13 +224,10 @@ __device__ __forceinline__ float sgn_pressure(float lambda_sgn, float g, float m
 // diagonal entry only enters through terms that vanish identically
 // (u_i rat_ii - u_i rat_ii) and the Galerkin boundary term -c_ii.v_i.
 template <int B, bool LAMIN, int MINB>
-__global__ void __launch_bounds__(256, MINB) k_low_mix(Graph G, const InstConst* __restrict__ C,
+__device__ __forceinline__ void low_row(int64_t r, Graph G, const InstConst* __restrict__ C,
                                                        const InstState* __restrict__ St, StateMix u,
-                                                       const float* __restrict__ alpha, float* __restrict__ dL,
-                                                       float* __restrict__ muL, WorkMix w, float* __restrict__ res,
-                                                       unsigned* __restrict__ err) {
-  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (r >= G.n_rows) return;
+                                                       const float* __restrict__ alpha, float2* __restrict__ dmu,
+                                                       WorkMix w, float* __restrict__ res, unsigned* __restrict__ err) {
   const int L = G.len[r];
   if (L == 0) return;
   const int b = G.slice_inst[r >> 5];
@@ -317,8 +320,7 @@ __global__ void __launch_bounds__(256, MINB) k_low_mix(Graph G, const InstConst*
     const float s = (c.alpha_limit ? fmaxf(ai, alb[q]) : 1.f) * vis;
     d *= s;
     mu *= s;
-    dL[e] = d;
-    muL[e] = mu;
+    dmu[e] = make_float2(d, mu);
     // --- entropy stencil
     const float v2j_flux = sgn ? 0.f : nj.v2;
     const float Ej = 0.5f * (g * nj.h * nj.h + nj.v1 * nj.q1 + v2j_flux * nj.q2);
@@ -343,10 +345,17 @@ __global__ void __launch_bounds__(256, MINB) k_low_mix(Graph G, const InstConst*
     g0 += -cvj_flux * nj.h + mu * (nj.h - ni.h) + dmu * (nj.h * rji - ni.h * rij);
     const float A1 = mu * (nj.q1 - ni.q1) - cvj_flux * nj.q1;
     const float A2 = mu * (nj.q2 - ni.q2) - cvj_flux * nj.q2;
-    rk1 += A1 + dmu * (nj.q1 * rjit - ni.q1 * rijt);
-    rk2_ += A2 + dmu * (nj.q2 * rjit - ni.q2 * rijt);
-    g1 += A1 + dmu * (nj.q1 * rji - ni.q1 * rij);
-    g2 += A2 + dmu * (nj.q2 * rji - ni.q2 * rij);
+    const float T1 = A1 + dmu * (nj.q1 * rji - ni.q1 * rij);
+    const float T2 = A2 + dmu * (nj.q2 * rji - ni.q2 * rij);
+    g1 += T1;
+    g2 += T2;
+    if (rijt == rij && rjit == rji) {                                 // both wet: same terms
+      rk1 += T1;
+      rk2_ += T2;
+    } else {
+      rk1 += A1 + dmu * (nj.q1 * rjit - ni.q1 * rijt);
+      rk2_ += A2 + dmu * (nj.q2 * rjit - ni.q2 * rijt);
+    }
     rk1 -= topo * cxe; rk2_ -= topo * cye;
     g1 -= topo * cxe; g2 -= topo * cye;
     if (S == 5) {
@@ -416,6 +425,15 @@ __global__ void __launch_bounds__(256, MINB) k_low_mix(Graph G, const InstConst*
   if (delta_bad) atomicOr(err, ERRB_DELTA);
 }
 
+template <int B, bool LAMIN, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_low_mix(Graph G, const InstConst* __restrict__ C,
+                                                       const InstState* __restrict__ St, StateMix u,
+                                                       const float* __restrict__ alpha, float2* __restrict__ dmu,
+                                                       WorkMix w, float* __restrict__ res, unsigned* __restrict__ err) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < G.n_rows; r += (int64_t)gridDim.x * blockDim.x)
+    low_row<B, LAMIN, MINB>(r, G, C, St, u, alpha, dmu, w, res, err);
+}
+
 // Limiter margin: (1 - 2^-18) Q^-.  Between the limiter and the depth update
 // the negative part of sum_j l_ij f_ij passes through at most ~12 FP32
 // roundings (h^L to FP32, m and dt and their reciprocals, two products here,
@@ -429,11 +447,9 @@ constexpr float kLimiterShrink = 1.0f - 3.814697265625e-6f;
 // stores R^-_i P_i (the limited negative part of the h-row, reused by the
 // update).
 template <int B>
-__global__ void __launch_bounds__(256) k_fct_mix(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St, StateMix u,
-                          const float* __restrict__ dL, const float* __restrict__ muL, WorkMix w,
-                          const float* __restrict__ res, unsigned* __restrict__ err) {
-  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (r >= G.n_rows) return;
+__device__ __forceinline__ void fct_row(int64_t r, Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St, StateMix u,
+                          const float2* __restrict__ dmu, WorkMix w, const float* __restrict__ res,
+                          unsigned* __restrict__ err) {
   const int L = G.len[r];
   if (L == 0) return;
   const int b = G.slice_inst[r >> 5];
@@ -453,7 +469,7 @@ __global__ void __launch_bounds__(256) k_fct_mix(Graph G, const InstConst* __res
     for (int q = 0; q < B; q++) {
       if (k0 + q < L) {
         const int64_t e = base + 32 * (k0 + q);
-        jb[q] = G.col[e]; d0b[q] = dL[e]; m0b[q] = muL[e];
+        jb[q] = G.col[e]; const float2 v = dmu[e]; d0b[q] = v.x; m0b[q] = v.y;
       } else {
         jb[q] = (int)r; d0b[q] = 0.f; m0b[q] = 0.f;
       }
@@ -486,6 +502,14 @@ __global__ void __launch_bounds__(256) k_fct_mix(Graph G, const InstConst* __res
   }
   w.rminus[r] = R;
   w.rneg[r] = __fmul_rn(R, neg);
+}
+
+template <int B>
+__global__ void __launch_bounds__(256) k_fct_mix(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St,
+                                                 StateMix u, const float2* __restrict__ dmu, WorkMix w,
+                                                 const float* __restrict__ res, unsigned* __restrict__ err) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < G.n_rows; r += (int64_t)gridDim.x * blockDim.x)
+    fct_row<B>(r, G, C, St, u, dmu, w, res, err);
 }
 
 // End of a stage for one row: non-finite check, the SSP-RK combination and
@@ -528,12 +552,10 @@ __device__ __forceinline__ void finish_mix(const Graph& G, const InstConst& c, i
 // :684-718), RK combination and Dirichlet data (main.f90:77-90).  The h-row
 // sum is R^-_i P_i (from k_fct_mix) plus sum_{f_ij >= 0} R^-_j f_ij.
 template <int B>
-__global__ void __launch_bounds__(256) k_update_mix(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St,
-                             StateMix u, const float* __restrict__ dL, const float* __restrict__ muL, WorkMix w,
+__device__ __forceinline__ void update_row(int64_t r, Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St,
+                             StateMix u, const float2* __restrict__ dmu, WorkMix w,
                              const float* __restrict__ res, StateMix u0, StateMix out, int rk_stage,
                              unsigned* __restrict__ err) {
-  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (r >= G.n_rows) return;
   const int L = G.len[r];
   if (L == 0) return;
   const int b = G.slice_inst[r >> 5];
@@ -563,7 +585,7 @@ __global__ void __launch_bounds__(256) k_update_mix(Graph G, const InstConst* __
    for (int q = 0; q < B; q++) {
      if (k0 + q < L) {
        const int64_t e = base + 32 * (k0 + q);
-       jb[q] = G.col[e]; d0b[q] = dL[e]; m0b[q] = muL[e];
+       jb[q] = G.col[e]; const float2 v = dmu[e]; d0b[q] = v.x; m0b[q] = v.y;
      } else {
        jb[q] = (int)r; d0b[q] = 0.f; m0b[q] = 0.f;
      }
@@ -608,6 +630,15 @@ __global__ void __launch_bounds__(256) k_update_mix(Graph G, const InstConst* __
   finish_mix(G, c, r, S, hn, q1, q2, q3, q4, zi, rk_stage, u0, out, err);
 }
 
+template <int B>
+__global__ void __launch_bounds__(256) k_update_mix(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St,
+                                                    StateMix u, const float2* __restrict__ dmu, WorkMix w,
+                                                    const float* __restrict__ res, StateMix u0, StateMix out,
+                                                    int rk_stage, unsigned* __restrict__ err) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < G.n_rows; r += (int64_t)gridDim.x * blockDim.x)
+    update_row<B>(r, G, C, St, u, dmu, w, res, u0, out, rk_stage, err);
+}
+
 // k_dt_mix: FP32 lambda_max, max |d_ii|/m_i per instance (main.f90:166-174).
 // It walks the neighbours of the state that stage 1 starts from, so it also
 // stores |c_ij| lambda_max per entry (dlam, reused by stage 1's k_low_mix)
@@ -615,7 +646,10 @@ __global__ void __launch_bounds__(256) k_update_mix(Graph G, const InstConst* __
 template <int B>
 __global__ void __launch_bounds__(256) k_dt_mix(Graph G, const InstConst* __restrict__ C, InstState* __restrict__ St, StateMix u,
                          float* __restrict__ dlam, float* __restrict__ alpha_out, unsigned* __restrict__ err) {
-  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  // grid-stride over block-sized row ranges: every lane of a warp runs the
+  // same iterations (the warp reduction below needs all 32)
+  for (int64_t rb = blockIdx.x * (int64_t)blockDim.x; rb < G.n_rows; rb += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t r = rb + threadIdx.x;
   float val = 0.f;
   if (r < G.n_rows && G.len[r] > 0) {
     const int b = G.slice_inst[r >> 5];
@@ -683,6 +717,7 @@ __global__ void __launch_bounds__(256) k_dt_mix(Graph G, const InstConst* __rest
     if (!St[bw].done && val > 0.f)
       atomicMax(&St[bw].maxd_bits, (unsigned long long)__double_as_longlong((double)val));
   }
+  }
 }
 
 // Copy the bathymetry into the packed node records after a bathymetry change
@@ -718,24 +753,48 @@ __global__ void k_mass_mix(Graph G, const float2* __restrict__ h, double* __rest
 
 static inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
+// Grid of a row kernel: one thread per row (mode 0), or a resident grid of
+// mode x (blocks per SM at full occupancy) x SMs whose threads stride over
+// the rows (the kernels loop), which keeps every warp slot busy instead of
+// paying a block launch per 64-256 rows.
+template <typename K>
+static unsigned row_grid(K kern, int64_t n, int block, int mode) {
+  const unsigned full = nblk(n, block);
+  if (mode <= 0) return full;
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, 0) != cudaSuccess || per_sm <= 0) {
+    cudaGetLastError();
+    return full;
+  }
+  const unsigned g = (unsigned)(per_sm * sms * mode);
+  return g < full ? g : full;
+}
+
 #define EV_BEGIN(k) if (kev) cudaEventRecord(kev->ev[2 * (k)], s)
 #define EV_END(k) if (kev) cudaEventRecord(kev->ev[2 * (k) + 1], s)
 
-#define SWE_DISPATCH_B(b, KERNEL, GRID, BS, ...)                         \
-  switch (b) {                                                           \
-    case 8: KERNEL<8><<<GRID, BS, 0, s>>>(__VA_ARGS__); break;           \
-    case 4: KERNEL<4><<<GRID, BS, 0, s>>>(__VA_ARGS__); break;           \
-    case 2: KERNEL<2><<<GRID, BS, 0, s>>>(__VA_ARGS__); break;           \
-    default: KERNEL<1><<<GRID, BS, 0, s>>>(__VA_ARGS__); break;          \
+#define SWE_DISPATCH_B(b, KERNEL, N, BS, MODE, ...)                                              \
+  switch (b) {                                                                                  \
+    case 8: KERNEL<8><<<row_grid(KERNEL<8>, N, BS, MODE), BS, 0, s>>>(__VA_ARGS__); break;      \
+    case 4: KERNEL<4><<<row_grid(KERNEL<4>, N, BS, MODE), BS, 0, s>>>(__VA_ARGS__); break;      \
+    case 2: KERNEL<2><<<row_grid(KERNEL<2>, N, BS, MODE), BS, 0, s>>>(__VA_ARGS__); break;      \
+    default: KERNEL<1><<<row_grid(KERNEL<1>, N, BS, MODE), BS, 0, s>>>(__VA_ARGS__); break;     \
   }
 
 // k_low variants: entry batch 1 or 2, lambda_max computed or taken from
 // k_dt_mix (stage 1), registers capped at 85 or 64 (3 or 4 resident blocks
 // of 256 threads per SM; the compiler would take ~106 with no cap)
 template <bool LAMIN>
-static void launch_low(const StageArgsMix& a, int batch, int cap, unsigned grid, int block, cudaStream_t s) {
-#define SWE_LOW(BB, MB) \
-  k_low_mix<BB, LAMIN, MB><<<grid, block, 0, s>>>(a.G, a.C, a.St, a.u, a.w.alpha, a.w.dL, a.w.muL, a.w, a.w.res, a.err)
+static void launch_low(const StageArgsMix& a, int batch, int cap, int mode, int block, cudaStream_t s) {
+#define SWE_LOW(BB, MB)                                                                                  \
+  k_low_mix<BB, LAMIN, MB><<<row_grid(k_low_mix<BB, LAMIN, MB>, a.G.n_rows, block, mode), block, 0, s>>>( \
+      a.G, a.C, a.St, a.u, a.w.alpha, a.w.dmu, a.w, a.w.res, a.err)
   if (batch >= 2) { if (cap) SWE_LOW(2, 4); else SWE_LOW(2, 3); }
   else { if (cap) SWE_LOW(1, 4); else SWE_LOW(1, 3); }
 #undef SWE_LOW
@@ -744,18 +803,18 @@ static void launch_low(const StageArgsMix& a, int batch, int cap, unsigned grid,
 void launch_kernel_mix(int kind, const StageArgsMix& a, const KernelTune& t, cudaStream_t s) {
   const int64_t n = a.G.n_rows;
   switch (kind) {
-    case 1: SWE_DISPATCH_B(t.batch[1], k_node_mix, nblk(n, t.block[1]), t.block[1], a.G, a.C, a.St, a.u, a.w.alpha)
+    case 1: SWE_DISPATCH_B(t.batch[1], k_node_mix, n, t.block[1], t.grid[1], a.G, a.C, a.St, a.u, a.w.alpha)
             break;
     case 2: if (a.rk_stage == 1 && a.w.dlam)   // stage 1 follows k_dt_mix on the same state
-              launch_low<true>(a, t.batch[2], t.cap_low, nblk(n, t.block[2]), t.block[2], s);
+              launch_low<true>(a, t.batch[2], t.cap_low, t.grid[2], t.block[2], s);
             else
-              launch_low<false>(a, t.batch[2], t.cap_low, nblk(n, t.block[2]), t.block[2], s);
+              launch_low<false>(a, t.batch[2], t.cap_low, t.grid[2], t.block[2], s);
             break;
-    case 3: SWE_DISPATCH_B(t.batch[3], k_fct_mix, nblk(n, t.block[3]), t.block[3], a.G, a.C, a.St, a.u, a.w.dL,
-                           a.w.muL, a.w, a.w.res, a.err)
+    case 3: SWE_DISPATCH_B(t.batch[3], k_fct_mix, n, t.block[3], t.grid[3], a.G, a.C, a.St, a.u, a.w.dmu, a.w,
+                           a.w.res, a.err)
             break;
-    case 4: SWE_DISPATCH_B(t.batch[4], k_update_mix, nblk(n, t.block[4]), t.block[4], a.G, a.C, a.St, a.u, a.w.dL,
-                           a.w.muL, a.w, a.w.res, a.u0, a.out, a.rk_stage, a.err)
+    case 4: SWE_DISPATCH_B(t.batch[4], k_update_mix, n, t.block[4], t.grid[4], a.G, a.C, a.St, a.u, a.w.dmu, a.w,
+                           a.w.res, a.u0, a.out, a.rk_stage, a.err)
             break;
     default: break;
   }
@@ -772,7 +831,7 @@ void launch_stage_mix(const StageArgsMix& a, cudaStream_t s, const KernelEvents*
 
 void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, float* dlam, float* alpha,
                    unsigned* err, const KernelTune& t, cudaStream_t s) {
-  SWE_DISPATCH_B(t.batch[0], k_dt_mix, nblk(G.n_rows, t.block[0]), t.block[0], G, C, St, u, dlam, alpha, err)
+  SWE_DISPATCH_B(t.batch[0], k_dt_mix, G.n_rows, t.block[0], t.grid[0], G, C, St, u, dlam, alpha, err)
 }
 
 void launch_refresh_z(const Graph& G, StateMix u, cudaStream_t s) {
