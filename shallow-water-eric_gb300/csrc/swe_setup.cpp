@@ -3,6 +3,7 @@
 #include "swe_setup.hpp"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <numeric>
 #include <queue>
@@ -90,6 +91,36 @@ std::vector<int> rcm_order(const HostMesh& m) {
   return new_of_old;
 }
 
+int sigma_rows() {
+  const char* e = std::getenv("SWE_SIGMA");
+  if (e) {
+    const int v = std::atoi(e);
+    if (v >= 0) return v;
+  }
+  return kSigmaRows;
+}
+
+// Within consecutive windows of `sigma` rows of an ordering, rows sorted by
+// decreasing length (stable).  A SELL-32 slice then holds rows of nearly
+// equal length, so its warp idles on few padded entries (on jittered
+// Delaunay meshes the fill of the RCM order alone is ~77%, 96% with 256-row
+// windows, 99% with 1024), while neighbours stay within the bandwidth plus
+// one window of each other.  sigma = 0 keeps the ordering.
+std::vector<int> sigma_sort(const HostMesh& m, const std::vector<int>& new_of_old, int sigma) {
+  if (sigma <= 1) return new_of_old;
+  const int n = m.np;
+  std::vector<int> old_at(n);
+  for (int i = 0; i < n; i++) old_at[new_of_old[i]] = i;
+  for (int w0 = 0; w0 < n; w0 += sigma) {
+    const int w1 = std::min(n, w0 + sigma);
+    std::stable_sort(old_at.begin() + w0, old_at.begin() + w1,
+                     [&](int a, int b) { return m.ia[a + 1] - m.ia[a] > m.ia[b + 1] - m.ia[b]; });
+  }
+  std::vector<int> out(n);
+  for (int k = 0; k < n; k++) out[old_at[k]] = k;
+  return out;
+}
+
 Layout build_layout(const std::vector<HostMesh>& meshes, const std::vector<std::vector<double>>& baths) {
   Layout L;
   L.n_inst = (int)meshes.size();
@@ -114,7 +145,7 @@ Layout build_layout(const std::vector<HostMesh>& meshes, const std::vector<std::
   L.new_of_old.resize(L.n_inst);
   std::vector<std::vector<int>> nofs(L.n_inst);
 #pragma omp parallel for schedule(dynamic)
-  for (int b = 0; b < L.n_inst; b++) nofs[b] = rcm_order(meshes[b]);   // sequential per instance
+  for (int b = 0; b < L.n_inst; b++) nofs[b] = sigma_sort(meshes[b], rcm_order(meshes[b]), sigma_rows());
   for (int b = 0; b < L.n_inst; b++) {
     const HostMesh& m = meshes[b];
     const std::vector<int>& nof = nofs[b];

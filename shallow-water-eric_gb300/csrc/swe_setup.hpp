@@ -31,7 +31,15 @@ void gauss_points(const HostMesh& m, double* rj, double* rr_gauss);
 // Reverse Cuthill-McKee ordering of the CSR graph: new_of_old[old] = new.
 std::vector<int> rcm_order(const HostMesh& m);
 
-// Global SELL-32 layout of a batch of meshes.  Row r (new numbering) of
+// An ordering with rows sorted by decreasing length inside windows of sigma
+// consecutive rows (SELL-C-sigma), new_of_old[old] = new.  sigma_rows() is
+// kSigmaRows unless SWE_SIGMA sets it (0: plain RCM).
+constexpr int kSigmaRows = 256;
+int sigma_rows();
+std::vector<int> sigma_sort(const HostMesh& m, const std::vector<int>& new_of_old, int sigma);
+
+// Global SELL-32 layout of a batch of meshes (rows in RCM order, sorted by
+// length within windows of sigma_rows()).  Row r (new numbering) of
 // instance b lives in [row_off[b], row_off[b] + np_b); each instance's row
 // range is padded to a multiple of 32 so that no slice straddles two
 // instances.  Entry k of row r sits at slice_ptr[r/32] + 32*k + r%32.  The
