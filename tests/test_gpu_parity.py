@@ -406,6 +406,31 @@ def test_sgn_fp64_bit_exact_and_mixed_close():
     assert um[0].min() >= 0.0
 
 
+@pytest.mark.parametrize("prec", [0, 1])
+def test_pinned_buffers_read_directly_match_staged_copies(prec):
+    """Uploads from / downloads to page-locked host buffers (the e2e path of
+    bench.py) equal those of pageable numpy arrays."""
+    torch = pytest.importorskip("torch")
+    case = C.dam_break_case(n=41)
+    upd = from_case(case, precision=prec)
+    pin_in = torch.from_numpy(np.asfortranarray(case.u0).ravel(order="F").copy()).pin_memory()
+    pin_out = torch.zeros_like(pin_in).pin_memory()
+    outs = []
+    for pinned in (False, True):
+        if pinned:
+            upd.upload_ptr(pin_in.data_ptr())
+        else:
+            upd.upload(case.u0)
+        upd.set_time(0.0, 1e30)
+        upd.rk3_steps(5)
+        if pinned:
+            upd.download_ptr(pin_out.data_ptr())
+            outs.append(pin_out.numpy().reshape(case.u0.shape, order="F").copy())
+        else:
+            outs.append(upd.download())
+    np.testing.assert_array_equal(outs[0], outs[1])
+
+
 def test_autotuned_variants_agree(monkeypatch):
     """The autotuner only changes block sizes and entry batching."""
     case = C.bump_basin_case(n=60)
