@@ -391,8 +391,10 @@ static void enqueue_step(swe_ctx* c, const KernelEvents* kev = nullptr, double* 
     }
   };
   if (kev) cudaEventRecord(kev->ev[0], s);
+  // FP64: k_dt keeps every d_ij (in the f_ij array, free until stage 1's
+  // k_fct) for stage 1's k_low
   if (c->precision == SWE_PREC_FP64)
-    launch_dt_f64(c->G, c->d_C, c->d_St, c->A, nullptr, nullptr, c->d_err, c->block, s);
+    launch_dt_f64(c->G, c->d_C, c->d_St, c->A, c->w.fct, nullptr, c->d_err, c->block, s);
   else launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->wm.dlam, c->wm.alpha, c->d_err, c->tune, s);
   if (kev) cudaEventRecord(kev->ev[1], s);
   harvest(0, 0);
@@ -401,6 +403,7 @@ static void enqueue_step(swe_ctx* c, const KernelEvents* kev = nullptr, double* 
     if (c->precision == SWE_PREC_FP64) {
       StageArgs a{c->G, c->d_C, c->d_St, c->A, c->A, c->B, c->w, stage, nullptr, c->d_err, c->block};
       a.entropy = has_entropy(c);
+      if (stage == 1) a.dij_in = c->w.fct;
       if (stage == 2) { a.u = c->B; a.out = c->Cs; }
       if (stage == 3) { a.u = c->Cs; a.out = c->A; }
       launch_stage_f64(a, s, kev);

@@ -55,6 +55,7 @@ struct StageArgs {
   unsigned* err;
   int block;
   int entropy = 0;   // some instance uses 'entropy_visc': launch k_entropy
+  const double* dij_in = nullptr;   // stage 1: d_ij of k_dt on the same state (bit-identical)
 };
 
 struct StageArgsMix {

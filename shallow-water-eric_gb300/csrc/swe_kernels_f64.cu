@@ -262,7 +262,7 @@ __device__ __forceinline__ void smb_rows_f64(const Graph& G, const InstConst& c,
 __global__ void k_low_f64(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St,
                           StateF64 u, NodeF64 nd, double* __restrict__ dL, double* __restrict__ muL,
                           double* __restrict__ dLii, double* __restrict__ muLii, StateF64 uL,
-                          double* __restrict__ res, unsigned* __restrict__ err) {
+                          double* __restrict__ res, const double* __restrict__ dij_in, unsigned* __restrict__ err) {
   int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= G.n_rows) return;
   const int L = G.len[r];
@@ -293,13 +293,17 @@ __global__ void k_low_f64(Graph G, const InstConst* __restrict__ C, const InstSt
     double d = 0.0, mu = 0.0;
     {
       const double cxe = G.cx[e], cye = G.cy[e];
-      const double norm = sqrt(cxe * cxe + cye * cye);
-      const double nx = cxe / norm, ny = cye / norm;
-      double lam;
-      if (!lambda_vacc(ui[0], ui[1], ui[2], ovhi, u.h[j], u.q1[j], u.q2[j], nd.ovh[j], nx, ny, g, htiny, sqrt2,
-                       &lam))
-        delta_bad = true;
-      d = norm * lam;
+      if (dij_in) {                            // stage 1: k_dt computed this d_ij on this state
+        d = dij_in[e];
+      } else {
+        const double norm = sqrt(cxe * cxe + cye * cye);
+        const double nx = cxe / norm, ny = cye / norm;
+        double lam;
+        if (!lambda_vacc(ui[0], ui[1], ui[2], ovhi, u.h[j], u.q1[j], u.q2[j], nd.ovh[j], nx, ny, g, htiny, sqrt2,
+                         &lam))
+          delta_bad = true;
+        d = norm * lam;
+      }
       const double sl = cxe * v1i + cye * v2i;
       // compute_muij uses q*ovh of the raw state, equal to velocity except
       // for type 13 whose velocity(2) is zeroed: recompute from q there
@@ -786,7 +790,7 @@ void launch_stage_f64(const StageArgs& a, cudaStream_t s, const KernelEvents* ke
   k_node_f64<<<nblk(a.G.n_rows, bs), bs, 0, s>>>(a.G, a.C, a.St, a.u, nd);
   EV_END(1); EV_BEGIN(2);
   k_low_f64<<<nblk(a.G.n_rows, bs), bs, 0, s>>>(a.G, a.C, a.St, a.u, nd, a.w.dL, a.w.muL, a.w.dLii, a.w.muLii,
-                                                a.w.uL, a.w.res, a.err);
+                                                a.w.uL, a.w.res, a.dij_in, a.err);
   EV_END(2); EV_BEGIN(3);
   k_fct_f64<<<nblk(a.G.n_rows, bs), bs, 0, s>>>(a.G, a.C, a.St, a.u, a.w.dL, a.w.muL, a.w.uL, a.w.res, a.w.fct,
                                                 a.w.rminus, a.err);
