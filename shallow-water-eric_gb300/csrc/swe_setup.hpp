@@ -1,6 +1,6 @@
 // Setup of the edge graph: the reference's construct_matrices
-// (SOURCES/update.f90:18-132) on the device, then the GB300 layout (RCM
-// renumbering, SELL-32 slices) on the host.
+// (SOURCES/update.f90:18-132) on the device, then the GB300 layout (Morton or
+// RCM renumbering, length-sorted SELL-32 slices) on the host.
 #pragma once
 #include <cstdint>
 #include <string>
@@ -35,11 +35,16 @@ std::vector<int> rcm_order(const HostMesh& m);
 // consecutive rows (SELL-C-sigma), new_of_old[old] = new.  sigma_rows() is
 // kSigmaRows unless SWE_SIGMA sets it (0: plain RCM).
 constexpr int kSigmaRows = 256;
+
+// Z-order numbering by node coordinates, the default (SWE_ORDER=rcm selects
+// RCM instead), new_of_old[old] = new.
+std::vector<int> morton_order(const HostMesh& m);
+bool use_morton();
 int sigma_rows();
 std::vector<int> sigma_sort(const HostMesh& m, const std::vector<int>& new_of_old, int sigma);
 
-// Global SELL-32 layout of a batch of meshes (rows in RCM order, sorted by
-// length within windows of sigma_rows()).  Row r (new numbering) of
+// Global SELL-32 layout of a batch of meshes (rows in Morton (or RCM) order,
+// sorted by length within windows of sigma_rows()).  Row r (new numbering) of
 // instance b lives in [row_off[b], row_off[b] + np_b); each instance's row
 // range is padded to a multiple of 32 so that no slice straddles two
 // instances.  Entry k of row r sits at slice_ptr[r/32] + 32*k + r%32.  The
