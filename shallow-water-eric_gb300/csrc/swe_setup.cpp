@@ -120,11 +120,27 @@ std::vector<int> morton_order(const HostMesh& m) {
     x = (x | (x << 1)) & 0x55555555u;
     return x;
   };
+  // Hilbert index of (x, y) on a 2^16 grid (the classic rotate-and-flip
+  // walk from the top bit down)
+  auto hilbert = [](uint32_t x, uint32_t y) {
+    uint64_t d = 0;
+    for (uint32_t sq = 1u << 15; sq > 0; sq >>= 1) {
+      const uint32_t rx = (x & sq) ? 1u : 0u, ry = (y & sq) ? 1u : 0u;
+      d += (uint64_t)sq * sq * ((3u * rx) ^ ry);
+      if (ry == 0) {
+        if (rx == 1) { x = 0xffffu - x; y = 0xffffu - y; }
+        const uint32_t t = x; x = y; y = t;
+      }
+    }
+    return d;
+  };
+  const char* ord = std::getenv("SWE_ORDER");
+  const bool hil = ord && std::string(ord) == "hilbert";
   std::vector<uint64_t> key(n);
 #pragma omp parallel for schedule(static)
   for (int i = 0; i < n; i++) {
     const uint32_t qx = (uint32_t)((m.rr[2 * (size_t)i] - x0) * sx), qy = (uint32_t)((m.rr[2 * (size_t)i + 1] - y0) * sy);
-    key[i] = ((spread(qx) | (spread(qy) << 1)) << 32) | (uint64_t)i;
+    key[i] = ((hil ? hilbert(qx, qy) : (spread(qx) | (spread(qy) << 1))) << 32) | (uint64_t)i;
   }
   std::sort(key.begin(), key.end());
   std::vector<int> out(n);

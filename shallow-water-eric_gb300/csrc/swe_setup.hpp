@@ -36,8 +36,8 @@ std::vector<int> rcm_order(const HostMesh& m);
 // kSigmaRows unless SWE_SIGMA sets it (0: plain RCM).
 constexpr int kSigmaRows = 256;
 
-// Z-order numbering by node coordinates, the default (SWE_ORDER=rcm selects
-// RCM instead), new_of_old[old] = new.
+// Z-order numbering by node coordinates, the default (SWE_ORDER=hilbert uses
+// a Hilbert curve instead, SWE_ORDER=rcm RCM), new_of_old[old] = new.
 std::vector<int> morton_order(const HostMesh& m);
 bool use_morton();
 int sigma_rows();
