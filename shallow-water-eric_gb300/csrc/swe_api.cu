@@ -61,6 +61,8 @@ struct swe_ctx {
   // mixed path
   StateMix mA{}, mB{}, mC{};
   WorkMix wm{};
+  TileCtl tiles{};                       // row tiles of the shared-memory variants
+  bool tiles_ok = false;
   double* d_mass_acc = nullptr;
   // diagnostics: per-instance element lists and Gauss weights, on first use
   std::vector<int*> d_jj_inst;
@@ -253,6 +255,19 @@ static int build_device(swe_ctx* c, const std::vector<std::vector<double>>& bath
     w.hL = c->buf.alloc<float2>(n, st);
     w.qL = c->buf.alloc<float2>(n, st);
     if (c->S == 5) { w.q3L = c->buf.alloc<float>(n, st); w.q4L = c->buf.alloc<float>(n, st); }
+    // row tiles of the shared-memory kernel variants (SWE_TILE rows, default
+    // 256; 0 disables), while the tile and its halo fit in 48 KB
+    const char* ft = getenv("SWE_TILE");
+    const int tile = ft ? atoi(ft) : 256;
+    RowTiles F;
+    if (c->S == 3 && tile > 0 && build_row_tiles(L, tile, F) && (size_t)(F.tile + F.halo_cap) * 24 <= 48 * 1024) {
+      c->tiles.loc = upload_vec(c, F.loc, st);
+      c->tiles.halo_ptr = upload_vec(c, F.halo_ptr, st);
+      c->tiles.halo_rows = upload_vec(c, F.halo_rows, st);
+      c->tiles.tile_rows = F.tile;
+      c->tiles.halo_cap = F.halo_cap;
+      c->tiles_ok = true;
+    }
   }
   if (st != cudaSuccess) return fail(c, SWE_ERR_CUDA, std::string("device allocation: ") + cudaGetErrorString(st));
   return SWE_OK;
@@ -395,7 +410,8 @@ static void enqueue_step(swe_ctx* c, const KernelEvents* kev = nullptr, double* 
   // k_fct) for stage 1's k_low
   if (c->precision == SWE_PREC_FP64)
     launch_dt_f64(c->G, c->d_C, c->d_St, c->A, c->w.fct, nullptr, c->d_err, c->block, s);
-  else launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->wm.dlam, c->wm.alpha, c->d_err, c->tune, s);
+  else launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->wm.dlam, c->wm.alpha, c->d_err, c->tune,
+                   c->tiles_ok ? &c->tiles : nullptr, s);
   if (kev) cudaEventRecord(kev->ev[1], s);
   harvest(0, 0);
   launch_step_begin(c->d_C, c->d_St, c->n_inst, s);
@@ -409,6 +425,7 @@ static void enqueue_step(swe_ctx* c, const KernelEvents* kev = nullptr, double* 
       launch_stage_f64(a, s, kev);
     } else {
       StageArgsMix a{c->G, c->d_C, c->d_St, c->mA, c->mA, c->mB, c->wm, stage, c->d_err, c->block};
+      a.tiles = c->tiles_ok ? &c->tiles : nullptr;
       if (stage == 2) { a.u = c->mB; a.out = c->mC; }
       if (stage == 3) { a.u = c->mC; a.out = c->mA; }
       launch_stage_mix(a, s, kev, c->tune);
@@ -660,6 +677,7 @@ SWE_API int swe_euler(swe_ctx* c, int inst, const double* un, double* unext) {
     launch_stage_f64(a, c->stream);
   } else {
     StageArgsMix a{c->G, c->d_C, c->d_St, c->mA, c->mA, c->mB, c->wm, 0, c->d_err, c->block};
+    a.tiles = c->tiles_ok ? &c->tiles : nullptr;
     launch_stage_mix(a, c->stream, nullptr, c->tune);
   }
   CK(cudaGetLastError());
@@ -872,8 +890,9 @@ static int autotune(swe_ctx* c) {
   if ((rc = restore_done(c, run))) return rc;
   const cudaStream_t s = c->stream;
   StageArgsMix a{c->G, c->d_C, c->d_St, c->mA, c->mA, c->mB, c->wm, 1, c->d_err, c->block};
+  a.tiles = c->tiles_ok ? &c->tiles : nullptr;
   KernelTune t = c->tune;
-  launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->wm.dlam, c->wm.alpha, c->d_err, t, s);   // populate every work array once
+  launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->wm.dlam, c->wm.alpha, c->d_err, t, a.tiles, s);   // populate every work array once
   launch_stage_mix(a, s, nullptr, t);
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
@@ -886,23 +905,29 @@ static int autotune(swe_ctx* c) {
   a_low.rk_stage = 2;
   std::string desc;
   const char* names[5] = {"dt", "node", "low", "fct", "update"};
+  // SWE_TILED=0 leaves the shared-memory variants out, SWE_TILED=1 takes them
+  const char* tenv = getenv("SWE_TILED");
   for (int kind = 0; kind < 5; kind++) {
     float best = 1e30f;
-    int bb = t.block[kind], bt = t.batch[kind], bc = t.cap_low, bg = t.grid[kind];
+    int bb = t.block[kind], bt = t.batch[kind], bc = t.cap_low, bg = t.grid[kind], btl = t.tiled[kind];
+    // grid modes: a thread per row, resident grid, shared-memory tiles
+    const bool tiles = a_low.tiles && kind_has_tiles(kind) && !(tenv && tenv[0] == '0');
+    const int gm0 = (tiles && tenv && tenv[0] == '1') ? 2 : 0, n_modes = tiles ? 3 : 2;
     for (int ib = 0; ib < 3; ib++)
       for (int it = 0; it < 4; it++)
         for (int cap = 0; cap < (kind == 2 ? 2 : 1); cap++)
-          for (int gm = 0; gm < 2; gm++) {
+          for (int gm = gm0; gm < n_modes; gm++) {
             if (kind == 2 && batches[it] > 2) continue;
             KernelTune v = t;
             v.block[kind] = blocks[ib];
             v.batch[kind] = batches[it];
-            v.grid[kind] = gm;
+            v.grid[kind] = gm == 1;
+            v.tiled[kind] = gm == 2;
             if (kind == 2) v.cap_low = cap;
             float tmin = 1e30f;
             for (int rep = 0; rep < 3; rep++) {
               cudaEventRecord(e0, s);
-              if (kind == 0) launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->wm.dlam, c->wm.alpha, c->d_err, v, s);
+              if (kind == 0) launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->wm.dlam, c->wm.alpha, c->d_err, v, a.tiles, s);
               else launch_kernel_mix(kind, a_low, v, s);
               cudaEventRecord(e1, s);
               CK(cudaEventSynchronize(e1));
@@ -911,17 +936,18 @@ static int autotune(swe_ctx* c) {
               tmin = std::min(tmin, ms);
             }
             if (tmin < best) {
-              best = tmin; bb = blocks[ib]; bt = batches[it]; bg = gm;
+              best = tmin; bb = blocks[ib]; bt = batches[it]; bg = gm == 1; btl = gm == 2;
               if (kind == 2) bc = cap;
             }
           }
     t.block[kind] = bb;
     t.batch[kind] = bt;
     t.grid[kind] = bg;
+    t.tiled[kind] = btl;
     if (kind == 2) t.cap_low = bc;
     char buf[96];
     snprintf(buf, sizeof buf, "%s%s:block%d/batch%d%s%s", kind ? " " : "", names[kind], bb, bt,
-             kind == 2 ? (bc ? "/regs64" : "/regs85") : "", bg ? "/resident" : "");
+             kind == 2 ? (bc ? "/regs64" : "/regs85") : "", bg ? "/resident" : (btl ? "/tiled" : ""));
     desc += buf;
   }
   cudaEventDestroy(e0);

@@ -58,6 +58,19 @@ struct StageArgs {
   const double* dij_in = nullptr;   // stage 1: d_ij of k_dt on the same state (bit-identical)
 };
 
+// Tiles of rows for the shared-memory variants of the entry loops: a block
+// owns `tile_rows` consecutive rows (a compact patch of the mesh in Morton
+// order) and first copies the node records of its rows and of its halo (the
+// rows outside the tile that its entries reference) into shared memory; the
+// entry loops then read neighbours there by tile-local position.
+struct TileCtl {
+  const int16_t* loc;     // per entry: col - tile start, or tile_rows + halo index
+  const int* halo_ptr;    // n_tiles + 1
+  const int* halo_rows;   // ascending per tile
+  int tile_rows;
+  int halo_cap;           // largest halo
+};
+
 struct StageArgsMix {
   Graph G;
   const InstConst* C;
@@ -67,6 +80,7 @@ struct StageArgsMix {
   int rk_stage;
   unsigned* err;
   int block;
+  const TileCtl* tiles = nullptr;  // row tiles of the shared-memory variants, or null
 };
 
 // Optional per-kernel event timing: when non-null, ev[2k], ev[2k+1] bracket
@@ -99,12 +113,14 @@ struct KernelTune {
   int batch[5] = {1, 1, 1, 1, 1};
   int grid[5] = {0, 0, 0, 0, 0};   // 0: a thread per row; k: k resident grids striding over the rows
   int cap_low = 0;
+  int tiled[5] = {0, 0, 0, 0, 0};  // 1: the shared-memory tile variant (grid: one block per tile)
 };
 
 void launch_stage_mix(const StageArgsMix& a, cudaStream_t s, const KernelEvents* kev, const KernelTune& t);
 void launch_kernel_mix(int kind, const StageArgsMix& a, const KernelTune& t, cudaStream_t s);
+bool kind_has_tiles(int kind);   // kernel kinds with a shared-memory tile variant
 void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, float* dlam, float* alpha,
-                   unsigned* err, const KernelTune& t, cudaStream_t s);
+                   unsigned* err, const KernelTune& t, const TileCtl* tiles, cudaStream_t s);
 void launch_refresh_z(const Graph& G, StateMix u, cudaStream_t s);
 void launch_mass_mix(const Graph& G, const float2* h, double* acc, cudaStream_t s);
 

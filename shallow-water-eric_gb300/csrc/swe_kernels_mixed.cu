@@ -151,18 +151,81 @@ __device__ __forceinline__ bool lambda_f(float hl, float hr, float vl, float vr,
 // instantiations may contract FMAs differently, so batch sizes agree to FP32
 // rounding.  The autotuner picks B per kernel.
 
+// Neighbour access of the entry loops: straight from HBM by column index
+// (NbGlobal), or from the block's shared-memory copy of its tile and halo
+// nodes by tile-local position (NbTile, rows of 3-component systems only).
+// aux is the per-node scalar the loop needs besides the node record (alpha
+// in k_low, the residual in k_fct and k_update); R is R^- (k_update).
+struct NbGlobal {
+  static constexpr bool kGlobal = true;
+  const int* col;
+  const float4* nq;
+  const float* aux;
+  const float* R;
+  __device__ __forceinline__ int index(int64_t e) const { return col[e]; }
+  __device__ __forceinline__ int self(int64_t r) const { return (int)r; }
+};
+struct NbTile {
+  static constexpr bool kGlobal = false;
+  const int16_t* loc;
+  const float4* nq;
+  const float* aux;
+  const float* R;
+  int64_t t0;
+  __device__ __forceinline__ int index(int64_t e) const { return loc[e]; }
+  __device__ __forceinline__ int self(int64_t r) const { return (int)(r - t0); }
+};
+
+// Shared-memory tile of one block: node records, aux and R^- of the tile's
+// rows (positions 0 .. T-1) and of its halo rows (T .. T+nh-1).
+struct TileSmem {
+  float4* nq;
+  float* aux;
+  float* R;
+};
+__device__ __forceinline__ TileSmem tile_smem(void* base, int cap) {
+  float4* nq = reinterpret_cast<float4*>(base);
+  float* aux = reinterpret_cast<float*>(nq + cap);
+  return TileSmem{nq, aux, aux + cap};
+}
+
+// Copy the tile's and the halo's node data into shared memory (coalesced for
+// the tile rows, ascending gathers for the halo); returns the tile start.
+template <bool AUX, bool RM>
+__device__ __forceinline__ int64_t stage_tile(const Graph& G, const TileCtl& tc, const StateMix& u,
+                                              const float* __restrict__ aux, const float* __restrict__ rminus,
+                                              const TileSmem& sm) {
+  const int T = tc.tile_rows;
+  const int64_t t0 = (int64_t)blockIdx.x * T;
+  const int h0 = tc.halo_ptr[blockIdx.x], nh = tc.halo_ptr[blockIdx.x + 1] - h0;
+  for (int i = threadIdx.x; i < T + nh; i += blockDim.x) {
+    const int64_t row = i < T ? t0 + i : (int64_t)tc.halo_rows[h0 + i - T];
+    if (row < G.n_rows) {
+      sm.nq[i] = u.nq[row];
+      if (AUX) sm.aux[i] = aux[row];
+      if (RM) sm.R[i] = rminus[row];
+    }
+  }
+  __syncthreads();
+  return t0;
+}
+
+__device__ __forceinline__ int64_t tile_end(const Graph& G, const TileCtl& tc, int64_t t0) {
+  return t0 + tc.tile_rows < G.n_rows ? t0 + tc.tile_rows : G.n_rows;
+}
+
 // k_node_mix: alpha_i (SOURCES/update.f90:758-781) from the FP32 depth.
-template <int B>
+template <int B, class Nb>
 __device__ __forceinline__ void node_row(int64_t r, Graph G, const InstConst* __restrict__ C,
                                                   const InstState* __restrict__ St, StateMix u,
-                                                  float* __restrict__ alpha_out) {
+                                                  float* __restrict__ alpha_out, const Nb& nb) {
   const int L = G.len[r];
   if (L == 0) return;
   const int b = G.slice_inst[r >> 5];
   if (St[b].done) return;
   const InstConst& c = C[b];
-  const float* hs = reinterpret_cast<const float*>(u.nq);
-  const float h = hs[4 * r];
+  const float* hs = reinterpret_cast<const float*>(nb.nq);
+  const float h = reinterpret_cast<const float*>(u.nq)[4 * r];
   float alpha = 1.0f;
   if (c.alpha_limit && !(h <= c.htinyf)) {
     const int64_t base = entry_base(G, r);
@@ -170,7 +233,7 @@ __device__ __forceinline__ void node_row(int64_t r, Graph G, const InstConst* __
     for (int k0 = 0; k0 < L; k0 += B) {
       int j[B];
 #pragma unroll
-      for (int q = 0; q < B; q++) j[q] = (k0 + q < L) ? G.col[base + 32 * (k0 + q)] : (int)r;
+      for (int q = 0; q < B; q++) j[q] = (k0 + q < L) ? nb.index(base + 32 * (k0 + q)) : nb.self(r);
       float hj[B];
 #pragma unroll
       for (int q = 0; q < B; q++) hj[q] = hs[4 * (int64_t)j[q]];
@@ -192,8 +255,21 @@ template <int B>
 __global__ void __launch_bounds__(256) k_node_mix(Graph G, const InstConst* __restrict__ C,
                                                   const InstState* __restrict__ St, StateMix u,
                                                   float* __restrict__ alpha_out) {
+  const NbGlobal nb{G.col, u.nq, nullptr, nullptr};
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < G.n_rows; r += (int64_t)gridDim.x * blockDim.x)
-    node_row<B>(r, G, C, St, u, alpha_out);
+    node_row<B>(r, G, C, St, u, alpha_out, nb);
+}
+
+template <int B>
+__global__ void __launch_bounds__(256) k_node_tile(Graph G, const InstConst* __restrict__ C,
+                                                   const InstState* __restrict__ St, StateMix u,
+                                                   float* __restrict__ alpha_out, TileCtl tc) {
+  extern __shared__ float4 tile_mem[];
+  const TileSmem sm = tile_smem(tile_mem, tc.tile_rows + tc.halo_cap);
+  const int64_t t0 = stage_tile<false, false>(G, tc, u, nullptr, nullptr, sm);
+  const int64_t t1 = tile_end(G, tc, t0);
+  const NbTile nb{tc.loc, sm.nq, nullptr, nullptr, t0};
+  for (int64_t r = t0 + threadIdx.x; r < t1; r += blockDim.x) node_row<B>(r, G, C, St, u, alpha_out, nb);
 }
 
 struct NodeF {   // FP32 view of one node used by the edge loop
@@ -223,19 +299,20 @@ __device__ __forceinline__ float sgn_pressure(float lambda_sgn, float g, float m
 // formed once and shared by mu_ij, lambda_max and the Galerkin flux.  The
 // diagonal entry only enters through terms that vanish identically
 // (u_i rat_ii - u_i rat_ii) and the Galerkin boundary term -c_ii.v_i.
-template <int B, bool LAMIN, int MINB>
+template <int B, bool LAMIN, int MINB, class Nb>
 __device__ __forceinline__ void low_row(int64_t r, Graph G, const InstConst* __restrict__ C,
                                                        const InstState* __restrict__ St, StateMix u,
                                                        const float* __restrict__ alpha, float2* __restrict__ dmu,
-                                                       WorkMix w, float* __restrict__ res, unsigned* __restrict__ err) {
+                                                       WorkMix w, float* __restrict__ res, unsigned* __restrict__ err,
+                                                       const Nb& nb) {
   const int L = G.len[r];
   if (L == 0) return;
   const int b = G.slice_inst[r >> 5];
   const InstState& st = St[b];
   if (st.done) return;
   const InstConst& c = C[b];
-  const int S = c.S;
-  const bool sgn = c.type_test == 13;
+  const int S = Nb::kGlobal ? c.S : 3;         // tiles hold 3-component systems only
+  const bool sgn = Nb::kGlobal && c.type_test == 13;
   const bool galerkin = c.visc == VISC_GALERKIN;   // every d_ij, mu_ij = 0 (update.f90:155-158)
   const float vis = galerkin ? 0.f : 1.f;
   const float g = c.gf, htiny = c.htinyf, dtf = st.dtf;
@@ -284,16 +361,16 @@ __device__ __forceinline__ void low_row(int64_t r, Graph G, const InstConst* __r
    for (int q = 0; q < B; q++) {
      if (k0 + q < L) {
        const int64_t e = base + 32 * (k0 + q);
-       jb[q] = G.col[e]; cxb[q] = G.cxf[e]; cyb[q] = G.cyf[e];
+       jb[q] = nb.index(e); cxb[q] = G.cxf[e]; cyb[q] = G.cyf[e];
        dlb[q] = LAMIN ? w.dlam[e] : 0.f;
      } else {
-       jb[q] = (int)r; cxb[q] = 0.f; cyb[q] = 0.f; dlb[q] = 0.f;
+       jb[q] = nb.self(r); cxb[q] = 0.f; cyb[q] = 0.f; dlb[q] = 0.f;
      }
    }
    float4 nqb[B];
    float alb[B];
 #pragma unroll
-   for (int q = 0; q < B; q++) { nqb[q] = u.nq[jb[q]]; alb[q] = alpha[jb[q]]; }
+   for (int q = 0; q < B; q++) { nqb[q] = nb.nq[jb[q]]; alb[q] = nb.aux[jb[q]]; }
 #pragma unroll
    for (int q = 0; q < B; q++) {
     if (k0 + q >= L) break;
@@ -358,7 +435,7 @@ __device__ __forceinline__ void low_row(int64_t r, Graph G, const InstConst* __r
     }
     rk1 -= topo * cxe; rk2_ -= topo * cye;
     g1 -= topo * cxe; g2 -= topo * cye;
-    if (S == 5) {
+    if (Nb::kGlobal && S == 5) {
       const float uj3 = u.q3[j], uj4 = u.q4[j];
       const float A3 = mu * (uj3 - ui3) - cvj_flux * uj3;
       const float A4 = mu * (uj4 - ui4) - cvj_flux * uj4;
@@ -430,8 +507,24 @@ __global__ void __launch_bounds__(256, MINB) k_low_mix(Graph G, const InstConst*
                                                        const InstState* __restrict__ St, StateMix u,
                                                        const float* __restrict__ alpha, float2* __restrict__ dmu,
                                                        WorkMix w, float* __restrict__ res, unsigned* __restrict__ err) {
+  const NbGlobal nb{G.col, u.nq, alpha, nullptr};
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < G.n_rows; r += (int64_t)gridDim.x * blockDim.x)
-    low_row<B, LAMIN, MINB>(r, G, C, St, u, alpha, dmu, w, res, err);
+    low_row<B, LAMIN, MINB>(r, G, C, St, u, alpha, dmu, w, res, err, nb);
+}
+
+template <int B, bool LAMIN, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_low_tile(Graph G, const InstConst* __restrict__ C,
+                                                        const InstState* __restrict__ St, StateMix u,
+                                                        const float* __restrict__ alpha, float2* __restrict__ dmu,
+                                                        WorkMix w, float* __restrict__ res, unsigned* __restrict__ err,
+                                                        TileCtl tc) {
+  extern __shared__ float4 tile_mem[];
+  const TileSmem sm = tile_smem(tile_mem, tc.tile_rows + tc.halo_cap);
+  const int64_t t0 = stage_tile<true, false>(G, tc, u, alpha, nullptr, sm);
+  const int64_t t1 = tile_end(G, tc, t0);
+  const NbTile nb{tc.loc, sm.nq, sm.aux, nullptr, t0};
+  for (int64_t r = t0 + threadIdx.x; r < t1; r += blockDim.x)
+    low_row<B, LAMIN, MINB>(r, G, C, St, u, alpha, dmu, w, res, err, nb);
 }
 
 // Limiter margin: (1 - 2^-18) Q^-.  Between the limiter and the depth update
@@ -446,10 +539,10 @@ constexpr float kLimiterShrink = 1.0f - 3.814697265625e-6f;
 // Q^- = -m h^L/dt, R^- = min(Q^-/P^-, 1), 0 where m h^L/dt <= htiny.  Also
 // stores R^-_i P_i (the limited negative part of the h-row, reused by the
 // update).
-template <int B>
+template <int B, class Nb>
 __device__ __forceinline__ void fct_row(int64_t r, Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St, StateMix u,
                           const float2* __restrict__ dmu, WorkMix w, const float* __restrict__ res,
-                          unsigned* __restrict__ err) {
+                          unsigned* __restrict__ err, const Nb& nb) {
   const int L = G.len[r];
   if (L == 0) return;
   const int b = G.slice_inst[r >> 5];
@@ -469,15 +562,15 @@ __device__ __forceinline__ void fct_row(int64_t r, Graph G, const InstConst* __r
     for (int q = 0; q < B; q++) {
       if (k0 + q < L) {
         const int64_t e = base + 32 * (k0 + q);
-        jb[q] = G.col[e]; const float2 v = dmu[e]; d0b[q] = v.x; m0b[q] = v.y;
+        jb[q] = nb.index(e); const float2 v = dmu[e]; d0b[q] = v.x; m0b[q] = v.y;
       } else {
-        jb[q] = (int)r; d0b[q] = 0.f; m0b[q] = 0.f;
+        jb[q] = nb.self(r); d0b[q] = 0.f; m0b[q] = 0.f;
       }
     }
     float4 njb[B];
     float rsb[B];
 #pragma unroll
-    for (int q = 0; q < B; q++) { njb[q] = u.nq[jb[q]]; rsb[q] = res[jb[q]]; }
+    for (int q = 0; q < B; q++) { njb[q] = nb.nq[jb[q]]; rsb[q] = nb.aux[jb[q]]; }
 #pragma unroll
     for (int q = 0; q < B; q++) {
       if (k0 + q >= L) break;
@@ -508,8 +601,22 @@ template <int B>
 __global__ void __launch_bounds__(256) k_fct_mix(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St,
                                                  StateMix u, const float2* __restrict__ dmu, WorkMix w,
                                                  const float* __restrict__ res, unsigned* __restrict__ err) {
+  const NbGlobal nb{G.col, u.nq, res, nullptr};
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < G.n_rows; r += (int64_t)gridDim.x * blockDim.x)
-    fct_row<B>(r, G, C, St, u, dmu, w, res, err);
+    fct_row<B>(r, G, C, St, u, dmu, w, res, err, nb);
+}
+
+template <int B>
+__global__ void __launch_bounds__(256) k_fct_tile(Graph G, const InstConst* __restrict__ C,
+                                                  const InstState* __restrict__ St, StateMix u,
+                                                  const float2* __restrict__ dmu, WorkMix w,
+                                                  const float* __restrict__ res, unsigned* __restrict__ err, TileCtl tc) {
+  extern __shared__ float4 tile_mem[];
+  const TileSmem sm = tile_smem(tile_mem, tc.tile_rows + tc.halo_cap);
+  const int64_t t0 = stage_tile<true, false>(G, tc, u, res, nullptr, sm);
+  const int64_t t1 = tile_end(G, tc, t0);
+  const NbTile nb{tc.loc, sm.nq, sm.aux, nullptr, t0};
+  for (int64_t r = t0 + threadIdx.x; r < t1; r += blockDim.x) fct_row<B>(r, G, C, St, u, dmu, w, res, err, nb);
 }
 
 // End of a stage for one row: non-finite check, the SSP-RK combination and
@@ -551,18 +658,18 @@ __device__ __forceinline__ void finish_mix(const Graph& G, const InstConst& c, i
 // k_update_mix: limited antidiffusion (update.f90:276-282, apply_viscosity
 // :684-718), RK combination and Dirichlet data (main.f90:77-90).  The h-row
 // sum is R^-_i P_i (from k_fct_mix) plus sum_{f_ij >= 0} R^-_j f_ij.
-template <int B>
+template <int B, class Nb>
 __device__ __forceinline__ void update_row(int64_t r, Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St,
                              StateMix u, const float2* __restrict__ dmu, WorkMix w,
                              const float* __restrict__ res, StateMix u0, StateMix out, int rk_stage,
-                             unsigned* __restrict__ err) {
+                             unsigned* __restrict__ err, const Nb& nb) {
   const int L = G.len[r];
   if (L == 0) return;
   const int b = G.slice_inst[r >> 5];
   const InstState& st = St[b];
   if (st.done) return;
   const InstConst& c = C[b];
-  const int S = c.S;
+  const int S = Nb::kGlobal ? c.S : 3;
   const float4 ni = u.nq[r];
   if (c.visc != VISC_FCT) {                     // 'galerkin' / 'viscous': u^L is the result
     const float2 qL = w.qL[r];
@@ -585,19 +692,18 @@ __device__ __forceinline__ void update_row(int64_t r, Graph G, const InstConst* 
    for (int q = 0; q < B; q++) {
      if (k0 + q < L) {
        const int64_t e = base + 32 * (k0 + q);
-       jb[q] = G.col[e]; const float2 v = dmu[e]; d0b[q] = v.x; m0b[q] = v.y;
+       jb[q] = nb.index(e); const float2 v = dmu[e]; d0b[q] = v.x; m0b[q] = v.y;
      } else {
-       jb[q] = (int)r; d0b[q] = 0.f; m0b[q] = 0.f;
+       jb[q] = nb.self(r); d0b[q] = 0.f; m0b[q] = 0.f;
      }
    }
    float4 njb[B];
    float rsb[B], Rjb[B];
 #pragma unroll
-   for (int q = 0; q < B; q++) { njb[q] = u.nq[jb[q]]; rsb[q] = res[jb[q]]; Rjb[q] = w.rminus[jb[q]]; }
+   for (int q = 0; q < B; q++) { njb[q] = nb.nq[jb[q]]; rsb[q] = nb.aux[jb[q]]; Rjb[q] = nb.R[jb[q]]; }
 #pragma unroll
    for (int q = 0; q < B; q++) {
     if (k0 + q >= L) break;
-    const int j = jb[q];
     const float4 nj = njb[q];
     const float d0 = d0b[q], m0 = m0b[q];
     const float rij = fmaxf(resi, rsb[q]);
@@ -611,10 +717,13 @@ __device__ __forceinline__ void update_row(int64_t r, Graph G, const InstConst* 
     const float dm = dmr * lf, dx = (ddr - dmr) * lf;
     x1 += dm * (nj.y - ni.y) + dx * (nj.y * R.rji - ni.y * R.rij);
     x2 += dm * (nj.z - ni.z) + dx * (nj.z * R.rji - ni.z * R.rij);
-    if (S == 5) {
-      const float uj3 = u.q3[j], uj4 = u.q4[j];
-      x3 += dm * (uj3 - ui3) + dx * (uj3 * R.rji - ui3 * R.rij);
-      x4 += dm * (uj4 - ui4) + dx * (uj4 * R.rji - ui4 * R.rij);
+    if constexpr (Nb::kGlobal) {
+      if (S == 5) {
+        const int j = jb[q];
+        const float uj3 = u.q3[j], uj4 = u.q4[j];
+        x3 += dm * (uj3 - ui3) + dx * (uj3 * R.rji - ui3 * R.rij);
+        x4 += dm * (uj4 - ui4) + dx * (uj4 * R.rji - ui4 * R.rij);
+      }
     }
    }
   }
@@ -635,8 +744,104 @@ __global__ void __launch_bounds__(256) k_update_mix(Graph G, const InstConst* __
                                                     StateMix u, const float2* __restrict__ dmu, WorkMix w,
                                                     const float* __restrict__ res, StateMix u0, StateMix out,
                                                     int rk_stage, unsigned* __restrict__ err) {
+  const NbGlobal nb{G.col, u.nq, res, w.rminus};
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < G.n_rows; r += (int64_t)gridDim.x * blockDim.x)
-    update_row<B>(r, G, C, St, u, dmu, w, res, u0, out, rk_stage, err);
+    update_row<B>(r, G, C, St, u, dmu, w, res, u0, out, rk_stage, err, nb);
+}
+
+template <int B>
+__global__ void __launch_bounds__(256) k_update_tile(Graph G, const InstConst* __restrict__ C,
+                                                     const InstState* __restrict__ St, StateMix u,
+                                                     const float2* __restrict__ dmu, WorkMix w,
+                                                     const float* __restrict__ res, StateMix u0, StateMix out,
+                                                     int rk_stage, unsigned* __restrict__ err, TileCtl tc) {
+  extern __shared__ float4 tile_mem[];
+  const TileSmem sm = tile_smem(tile_mem, tc.tile_rows + tc.halo_cap);
+  const int64_t t0 = stage_tile<true, true>(G, tc, u, res, w.rminus, sm);
+  const int64_t t1 = tile_end(G, tc, t0);
+  const NbTile nb{tc.loc, sm.nq, sm.aux, sm.R, t0};
+  for (int64_t r = t0 + threadIdx.x; r < t1; r += blockDim.x)
+    update_row<B>(r, G, C, St, u, dmu, w, res, u0, out, rk_stage, err, nb);
+}
+
+// k_dt_mix: FP32 lambda_max, max |d_ii|/m_i per instance (main.f90:166-174).
+// It walks the neighbours of the state that stage 1 starts from, so it also
+// stores |c_ij| lambda_max per entry (dlam, reused by stage 1's k_low_mix)
+// and alpha_i (alpha_out, stage 1's k_node_mix), when those are non-null.
+// One row of k_dt_mix; returns |d_ii| / m_i (0 for padding and finished rows).
+template <int B, class Nb>
+__device__ __forceinline__ float dt_row(int64_t r, const Graph& G, const InstConst* __restrict__ C,
+                                        const InstState* __restrict__ St, const StateMix& u, float* __restrict__ dlam,
+                                        float* __restrict__ alpha_out, unsigned* __restrict__ err, const Nb& nb) {
+  if (r >= G.n_rows || G.len[r] == 0) return 0.f;
+  const int b = G.slice_inst[r >> 5];
+  if (St[b].done) return 0.f;
+  const InstConst& c = C[b];
+  const float g = c.gf, htiny = c.htinyf;
+  const LamK lk = lam_k(g, htiny);
+  const int L = G.len[r];
+  const int64_t base = entry_base(G, r);
+  const NodeF ni = node_from(u.nq[r], htiny);
+  const float sqi = sqrtf(g * fabsf(ni.h));
+  float s = 0.f;
+  float num = 0.f, denom = 0.f;          // alpha_limit stencil (as k_node_mix)
+  bool bad = false;
+  for (int k0 = 0; k0 < L; k0 += B) {
+    int jb[B];
+    float cxb[B], cyb[B];
+#pragma unroll
+    for (int q = 0; q < B; q++) {
+      if (k0 + q < L) {
+        const int64_t e = base + 32 * (k0 + q);
+        jb[q] = nb.index(e); cxb[q] = G.cxf[e]; cyb[q] = G.cyf[e];
+      } else {
+        jb[q] = nb.self(r); cxb[q] = 1.f; cyb[q] = 0.f;
+      }
+    }
+    float4 njb[B];
+#pragma unroll
+    for (int q = 0; q < B; q++) njb[q] = nb.nq[jb[q]];
+#pragma unroll
+    for (int q = 0; q < B; q++) {
+      if (k0 + q >= L) break;
+      const NodeF nj = node_from(njb[q], htiny);
+      const float cxe = cxb[q], cye = cyb[q];
+      const float n2 = cxe * cxe + cye * cye;
+      const float inv = rsqrtf(n2);
+      float lam;
+      if (!lambda_f(ni.h, nj.h, dotc(cxe, cye, ni.v1, ni.v2) * inv, dotc(cxe, cye, nj.v1, nj.v2) * inv, ni.ovh,
+                    nj.ovh, sqi, sqrtf(g * fabsf(nj.h)), lk, &lam))
+        bad = true;
+      const float dl = (n2 * inv) * lam;
+      if (dlam) dlam[base + 32 * (k0 + q)] = dl;
+      s += dl;
+      num += nj.h - ni.h;
+      denom += fabsf(nj.h - ni.h);
+    }
+  }
+  if (alpha_out) {
+    float alpha = 1.0f;
+    if (c.alpha_limit && !(ni.h <= c.htinyf)) {
+      const float a = (denom <= fabsf(num)) ? 1.0f : fdiv(fabsf(num), denom);
+      const float a2 = a * a, a4 = a2 * a2;
+      alpha = a4 * a4;
+    }
+    alpha_out[r] = alpha;
+  }
+  if (bad) atomicOr(err, ERRB_DELTA);
+  return s * G.inv_lumpedf[r];
+}
+
+// Warp max of |d_ii| / m_i into the instance's maximum (the 32 rows of a warp
+// are one slice, so one instance).
+__device__ __forceinline__ void dt_reduce(float val, int64_t r, const Graph& G, InstState* __restrict__ St) {
+  for (int off = 16; off > 0; off >>= 1) val = fmaxf(val, __shfl_down_sync(0xffffffffu, val, off));
+  const int64_t r0 = r & ~(int64_t)31;
+  if ((threadIdx.x & 31) == 0 && r0 < G.n_rows) {
+    const int bw = G.slice_inst[r0 >> 5];
+    if (!St[bw].done && val > 0.f)
+      atomicMax(&St[bw].maxd_bits, (unsigned long long)__double_as_longlong((double)val));
+  }
 }
 
 // k_dt_mix: FP32 lambda_max, max |d_ii|/m_i per instance (main.f90:166-174).
@@ -647,76 +852,27 @@ template <int B>
 __global__ void __launch_bounds__(256) k_dt_mix(Graph G, const InstConst* __restrict__ C, InstState* __restrict__ St, StateMix u,
                          float* __restrict__ dlam, float* __restrict__ alpha_out, unsigned* __restrict__ err) {
   // grid-stride over block-sized row ranges: every lane of a warp runs the
-  // same iterations (the warp reduction below needs all 32)
+  // same iterations (the warp reduction needs all 32)
+  const NbGlobal nb{G.col, u.nq, nullptr, nullptr};
   for (int64_t rb = blockIdx.x * (int64_t)blockDim.x; rb < G.n_rows; rb += (int64_t)gridDim.x * blockDim.x) {
-  const int64_t r = rb + threadIdx.x;
-  float val = 0.f;
-  if (r < G.n_rows && G.len[r] > 0) {
-    const int b = G.slice_inst[r >> 5];
-    if (!St[b].done) {
-      const InstConst& c = C[b];
-      const float g = c.gf, htiny = c.htinyf;
-      const LamK lk = lam_k(g, htiny);
-      const int L = G.len[r];
-      const int64_t base = entry_base(G, r);
-      const NodeF ni = node_from(u.nq[r], htiny);
-      const float sqi = sqrtf(g * fabsf(ni.h));
-      float s = 0.f;
-      float num = 0.f, denom = 0.f;          // alpha_limit stencil (as k_node_mix)
-      bool bad = false;
-      for (int k0 = 0; k0 < L; k0 += B) {
-       int jb[B];
-       float cxb[B], cyb[B];
-#pragma unroll
-       for (int q = 0; q < B; q++) {
-         if (k0 + q < L) {
-           const int64_t e = base + 32 * (k0 + q);
-           jb[q] = G.col[e]; cxb[q] = G.cxf[e]; cyb[q] = G.cyf[e];
-         } else {
-           jb[q] = (int)r; cxb[q] = 1.f; cyb[q] = 0.f;
-         }
-       }
-       float4 njb[B];
-#pragma unroll
-       for (int q = 0; q < B; q++) njb[q] = u.nq[jb[q]];
-#pragma unroll
-       for (int q = 0; q < B; q++) {
-        if (k0 + q >= L) break;
-        const NodeF nj = node_from(njb[q], htiny);
-        const float cxe = cxb[q], cye = cyb[q];
-        const float n2 = cxe * cxe + cye * cye;
-        const float inv = rsqrtf(n2);
-        float lam;
-        if (!lambda_f(ni.h, nj.h, dotc(cxe, cye, ni.v1, ni.v2) * inv, dotc(cxe, cye, nj.v1, nj.v2) * inv, ni.ovh,
-                      nj.ovh, sqi, sqrtf(g * fabsf(nj.h)), lk, &lam))
-          bad = true;
-        const float dl = (n2 * inv) * lam;
-        if (dlam) dlam[base + 32 * (k0 + q)] = dl;
-        s += dl;
-        num += nj.h - ni.h;
-        denom += fabsf(nj.h - ni.h);
-       }
-      }
-      val = s * G.inv_lumpedf[r];
-      if (alpha_out) {
-        float alpha = 1.0f;
-        if (c.alpha_limit && !(ni.h <= c.htinyf)) {
-          const float a = (denom <= fabsf(num)) ? 1.0f : fdiv(fabsf(num), denom);
-          const float a2 = a * a, a4 = a2 * a2;
-          alpha = a4 * a4;
-        }
-        alpha_out[r] = alpha;
-      }
-      if (bad) atomicOr(err, ERRB_DELTA);
-    }
+    const int64_t r = rb + threadIdx.x;
+    dt_reduce(dt_row<B>(r, G, C, St, u, dlam, alpha_out, err, nb), r, G, St);
   }
-  for (int off = 16; off > 0; off >>= 1) val = fmaxf(val, __shfl_down_sync(0xffffffffu, val, off));
-  const int64_t r0 = r & ~(int64_t)31;
-  if ((threadIdx.x & 31) == 0 && r0 < G.n_rows) {
-    const int bw = G.slice_inst[r0 >> 5];
-    if (!St[bw].done && val > 0.f)
-      atomicMax(&St[bw].maxd_bits, (unsigned long long)__double_as_longlong((double)val));
-  }
+}
+
+template <int B>
+__global__ void __launch_bounds__(256) k_dt_tile(Graph G, const InstConst* __restrict__ C, InstState* __restrict__ St,
+                                                 StateMix u, float* __restrict__ dlam, float* __restrict__ alpha_out,
+                                                 unsigned* __restrict__ err, TileCtl tc) {
+  extern __shared__ float4 tile_mem[];
+  const TileSmem sm = tile_smem(tile_mem, tc.tile_rows + tc.halo_cap);
+  const int64_t t0 = stage_tile<false, false>(G, tc, u, nullptr, nullptr, sm);
+  const NbTile nb{tc.loc, sm.nq, nullptr, nullptr, t0};
+  // tile_rows is a multiple of 32: every lane of a warp runs the same iterations
+  for (int64_t rb = t0; rb < t0 + tc.tile_rows; rb += blockDim.x) {
+    const int64_t r = rb + threadIdx.x;
+    if (rb - t0 + (int64_t)threadIdx.x - (threadIdx.x & 31) >= tc.tile_rows) break;   // warp past the tile
+    dt_reduce(dt_row<B>(r, G, C, St, u, dlam, alpha_out, err, nb), r, G, St);
   }
 }
 
@@ -787,11 +943,38 @@ static unsigned row_grid(K kern, int64_t n, int block, int mode) {
     default: KERNEL<1><<<row_grid(KERNEL<1>, N, BS, MODE), BS, 0, s>>>(__VA_ARGS__); break;     \
   }
 
+// Tile variants: one block per tile, shared memory for the tile's and the
+// halo's node records, residuals and R^- (24 B per row)
+inline size_t tile_smem_bytes(const TileCtl& tc) { return (size_t)(tc.tile_rows + tc.halo_cap) * 24; }
+#define SWE_DISPATCH_TILE(b, KERNEL, BS, TC, NROWS, ...)                                                \
+  do {                                                                                                \
+    const TileCtl& tc_ = (TC);                                                                        \
+    const unsigned g_ = (unsigned)(((NROWS) + tc_.tile_rows - 1) / tc_.tile_rows);                    \
+    const size_t sm_ = tile_smem_bytes(tc_);                                                          \
+    switch (b) {                                                                                      \
+      case 8: KERNEL<8><<<g_, BS, sm_, s>>>(__VA_ARGS__); break;                                      \
+      case 4: KERNEL<4><<<g_, BS, sm_, s>>>(__VA_ARGS__); break;                                      \
+      case 2: KERNEL<2><<<g_, BS, sm_, s>>>(__VA_ARGS__); break;                                      \
+      default: KERNEL<1><<<g_, BS, sm_, s>>>(__VA_ARGS__); break;                                     \
+    }                                                                                                 \
+  } while (0)
+
 // k_low variants: entry batch 1 or 2, lambda_max computed or taken from
 // k_dt_mix (stage 1), registers capped at 85 or 64 (3 or 4 resident blocks
 // of 256 threads per SM; the compiler would take ~106 with no cap)
 template <bool LAMIN>
-static void launch_low(const StageArgsMix& a, int batch, int cap, int mode, int block, cudaStream_t s) {
+static void launch_low(const StageArgsMix& a, int batch, int cap, int mode, int block, bool tiled, cudaStream_t s) {
+  if (tiled && a.tiles) {
+    const TileCtl& tc = *a.tiles;
+    const unsigned g = (unsigned)((a.G.n_rows + tc.tile_rows - 1) / tc.tile_rows);
+    const size_t sm = tile_smem_bytes(tc);
+#define SWE_LOWT(BB, MB) \
+    k_low_tile<BB, LAMIN, MB><<<g, block, sm, s>>>(a.G, a.C, a.St, a.u, a.w.alpha, a.w.dmu, a.w, a.w.res, a.err, tc)
+    if (batch >= 2) { if (cap) SWE_LOWT(2, 4); else SWE_LOWT(2, 3); }
+    else { if (cap) SWE_LOWT(1, 4); else SWE_LOWT(1, 3); }
+#undef SWE_LOWT
+    return;
+  }
 #define SWE_LOW(BB, MB)                                                                                  \
   k_low_mix<BB, LAMIN, MB><<<row_grid(k_low_mix<BB, LAMIN, MB>, a.G.n_rows, block, mode), block, 0, s>>>( \
       a.G, a.C, a.St, a.u, a.w.alpha, a.w.dmu, a.w, a.w.res, a.err)
@@ -800,21 +983,37 @@ static void launch_low(const StageArgsMix& a, int batch, int cap, int mode, int 
 #undef SWE_LOW
 }
 
+bool kind_has_tiles(int kind) { return kind >= 0 && kind <= 4; }
+
 void launch_kernel_mix(int kind, const StageArgsMix& a, const KernelTune& t, cudaStream_t s) {
   const int64_t n = a.G.n_rows;
   switch (kind) {
-    case 1: SWE_DISPATCH_B(t.batch[1], k_node_mix, n, t.block[1], t.grid[1], a.G, a.C, a.St, a.u, a.w.alpha)
+    case 1: if (t.tiled[1] && a.tiles) {
+              SWE_DISPATCH_TILE(t.batch[1], k_node_tile, t.block[1], *a.tiles, n, a.G, a.C, a.St, a.u, a.w.alpha, *a.tiles);
+            } else {
+              SWE_DISPATCH_B(t.batch[1], k_node_mix, n, t.block[1], t.grid[1], a.G, a.C, a.St, a.u, a.w.alpha)
+            }
             break;
     case 2: if (a.rk_stage == 1 && a.w.dlam)   // stage 1 follows k_dt_mix on the same state
-              launch_low<true>(a, t.batch[2], t.cap_low, t.grid[2], t.block[2], s);
+              launch_low<true>(a, t.batch[2], t.cap_low, t.grid[2], t.block[2], t.tiled[2], s);
             else
-              launch_low<false>(a, t.batch[2], t.cap_low, t.grid[2], t.block[2], s);
+              launch_low<false>(a, t.batch[2], t.cap_low, t.grid[2], t.block[2], t.tiled[2], s);
             break;
-    case 3: SWE_DISPATCH_B(t.batch[3], k_fct_mix, n, t.block[3], t.grid[3], a.G, a.C, a.St, a.u, a.w.dmu, a.w,
-                           a.w.res, a.err)
+    case 3: if (t.tiled[3] && a.tiles) {
+              SWE_DISPATCH_TILE(t.batch[3], k_fct_tile, t.block[3], *a.tiles, n, a.G, a.C, a.St, a.u, a.w.dmu, a.w, a.w.res, a.err,
+                                *a.tiles);
+            } else {
+              SWE_DISPATCH_B(t.batch[3], k_fct_mix, n, t.block[3], t.grid[3], a.G, a.C, a.St, a.u, a.w.dmu, a.w,
+                             a.w.res, a.err)
+            }
             break;
-    case 4: SWE_DISPATCH_B(t.batch[4], k_update_mix, n, t.block[4], t.grid[4], a.G, a.C, a.St, a.u, a.w.dmu, a.w,
-                           a.w.res, a.u0, a.out, a.rk_stage, a.err)
+    case 4: if (t.tiled[4] && a.tiles) {
+              SWE_DISPATCH_TILE(t.batch[4], k_update_tile, t.block[4], *a.tiles, n, a.G, a.C, a.St, a.u, a.w.dmu, a.w, a.w.res,
+                                a.u0, a.out, a.rk_stage, a.err, *a.tiles);
+            } else {
+              SWE_DISPATCH_B(t.batch[4], k_update_mix, n, t.block[4], t.grid[4], a.G, a.C, a.St, a.u, a.w.dmu, a.w,
+                             a.w.res, a.u0, a.out, a.rk_stage, a.err)
+            }
             break;
     default: break;
   }
@@ -830,8 +1029,12 @@ void launch_stage_mix(const StageArgsMix& a, cudaStream_t s, const KernelEvents*
 }
 
 void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, float* dlam, float* alpha,
-                   unsigned* err, const KernelTune& t, cudaStream_t s) {
-  SWE_DISPATCH_B(t.batch[0], k_dt_mix, G.n_rows, t.block[0], t.grid[0], G, C, St, u, dlam, alpha, err)
+                   unsigned* err, const KernelTune& t, const TileCtl* tiles, cudaStream_t s) {
+  if (t.tiled[0] && tiles) {
+    SWE_DISPATCH_TILE(t.batch[0], k_dt_tile, t.block[0], *tiles, G.n_rows, G, C, St, u, dlam, alpha, err, *tiles);
+  } else {
+    SWE_DISPATCH_B(t.batch[0], k_dt_mix, G.n_rows, t.block[0], t.grid[0], G, C, St, u, dlam, alpha, err)
+  }
 }
 
 void launch_refresh_z(const Graph& G, StateMix u, cudaStream_t s) {

@@ -263,4 +263,47 @@ Layout build_layout(const std::vector<HostMesh>& meshes, const std::vector<std::
   return L;
 }
 
+bool build_row_tiles(const Layout& L, int tile, RowTiles& F) {
+  if (tile <= 0 || tile % 32) return false;
+  const int64_t n_tiles = (L.n_rows + tile - 1) / tile;
+  F.tile = tile;
+  F.loc.assign(L.n_entries, 0);
+  F.halo_ptr.assign(n_tiles + 1, 0);
+  std::vector<std::vector<int>> halo(n_tiles);
+  bool ok = true;
+#pragma omp parallel for schedule(dynamic, 64) reduction(&& : ok)
+  for (int64_t t = 0; t < n_tiles; t++) {
+    const int64_t r0 = t * tile, r1 = std::min<int64_t>(r0 + tile, L.n_rows);
+    std::vector<int>& h = halo[t];
+    for (int64_t r = r0; r < r1; r++) {
+      const int64_t base = L.slice_ptr[r >> 5] + (r & 31);
+      for (int k = 0; k < L.len[r]; k++) {
+        const int j = L.col[base + 32 * k];
+        if (j < r0 || j >= r1) h.push_back(j);
+      }
+    }
+    std::sort(h.begin(), h.end());
+    h.erase(std::unique(h.begin(), h.end()), h.end());
+    if (tile + (int64_t)h.size() > 32767) ok = false;
+    for (int64_t r = r0; r < r1; r++) {
+      const int64_t base = L.slice_ptr[r >> 5] + (r & 31);
+      for (int k = 0; k < L.len[r]; k++) {
+        const int j = L.col[base + 32 * k];
+        int pos = (int)(j - r0);
+        if (j < r0 || j >= r1) pos = tile + (int)(std::lower_bound(h.begin(), h.end(), j) - h.begin());
+        F.loc[base + 32 * k] = (int16_t)pos;
+      }
+    }
+  }
+  if (!ok) return false;
+  F.halo_cap = 0;
+  for (int64_t t = 0; t < n_tiles; t++) {
+    F.halo_ptr[t + 1] = F.halo_ptr[t] + (int)halo[t].size();
+    F.halo_cap = std::max(F.halo_cap, (int)halo[t].size());
+  }
+  F.halo_rows.resize(F.halo_ptr[n_tiles]);
+  for (int64_t t = 0; t < n_tiles; t++) std::copy(halo[t].begin(), halo[t].end(), F.halo_rows.begin() + F.halo_ptr[t]);
+  return true;
+}
+
 }  // namespace swe

@@ -77,4 +77,18 @@ struct Layout {
 
 Layout build_layout(const std::vector<HostMesh>& meshes, const std::vector<std::vector<double>>& baths);
 
+// Tiles of `tile` consecutive rows (a multiple of 32) for the shared-memory
+// kernel variants.  halo_rows[halo_ptr[t] .. halo_ptr[t+1]) lists, ascending,
+// the rows outside tile t that its entries reference; loc[e] is the column's
+// position in the tile's shared-memory arrays: col - tile start for rows of
+// the tile, tile + (index in the halo list) for halo rows, 0 for padding
+// entries.  Returns false when a tile would need more than 32767 positions.
+struct RowTiles {
+  int tile = 0;
+  int halo_cap = 0;
+  std::vector<int16_t> loc;
+  std::vector<int> halo_ptr, halo_rows;
+};
+bool build_row_tiles(const Layout& L, int tile, RowTiles& F);
+
 }  // namespace swe

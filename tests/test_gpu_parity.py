@@ -449,3 +449,49 @@ def test_autotuned_variants_agree(monkeypatch):
     assert _rel_l1(outs[1][0], outs[0][0], lump) <= 1e-6
     scale = np.abs(outs[0]).max(axis=1, keepdims=True) + 1e-300
     assert np.max(np.abs(outs[0] - outs[1]) / scale) <= 1e-5
+
+
+@pytest.mark.parametrize("tile", ["64", "256"])
+def test_tiled_kernels_match_global_gathers(golden, monkeypatch, tile):
+    """The shared-memory tile variants (node records of a tile of rows and of
+    its halo staged in shared memory, neighbours read by tile-local position)
+    against the kernels that gather from HBM by column index.  The autotuner
+    may pick other entry batches for the two, whose FMA contraction differs,
+    so they agree to FP32 rounding: one Euler stage on a Thacker state with
+    moving wet/dry fronts, and 20 RK3 steps (dt included) of the
+    well-conditioned bump basin (the Thacker film amplifies rounding)."""
+    case = _thacker(golden, "0.1", periods=1.0, cfl=0.3)
+    o = _oracle_for(case)
+    u = case.u0.copy(order="F")
+    t = 0.0
+    for _ in range(10):                     # wet/dry fronts moving
+        t = o.rk3_step(u, t)
+    _, dt = o.compute_dij(u)
+    p = replace(case.params, dt=dt, precision=1)
+    bump = C.bump_basin_case(n=60)
+    monkeypatch.setenv("SWE_TILE", tile)
+    eul, traj, dts = {}, {}, {}
+    for tiled in ("0", "1"):
+        monkeypatch.setenv("SWE_TILED", tiled)
+        upd = from_case(case, precision=1)
+        upd.set_params(p)
+        upd.upload(u)
+        upd.autotune()
+        assert ("/tiled" in upd.tuning) == (tiled == "1"), upd.tuning
+        eul[tiled] = upd.euler(u)
+        upd.close()
+        upd = from_case(bump, precision=1)
+        upd.upload(bump.u0)
+        upd.set_time(0.0, 1e30)
+        _, dts[tiled], _ = upd.rk3_steps(20)
+        assert ("/tiled" in upd.tuning) == (tiled == "1"), upd.tuning
+        traj[tiled] = upd.download()
+        lump = upd.lumped
+        upd.close()
+    scale = np.abs(eul["0"]).max(axis=1, keepdims=True) + 1e-300
+    assert np.max(np.abs(eul["1"] - eul["0"]) / scale) <= 1e-6
+    assert dts["1"] == pytest.approx(dts["0"], rel=1e-6)
+    assert traj["1"][0].min() >= 0.0
+    assert _rel_l1(traj["1"][0], traj["0"][0], lump) <= 1e-6
+    scale = np.abs(traj["0"]).max(axis=1, keepdims=True) + 1e-300
+    assert np.max(np.abs(traj["1"] - traj["0"]) / scale) <= 1e-5
