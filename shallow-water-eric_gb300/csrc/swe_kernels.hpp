@@ -68,7 +68,7 @@ struct TileCtl {
   const int* halo_ptr;    // n_tiles + 1
   const int* halo_rows;   // ascending per tile
   int tile_rows;
-  int halo_cap;           // largest halo
+  int halo_cap;           // largest halo, rounded so tile_rows + halo_cap is a multiple of 4
 };
 
 struct StageArgsMix {
@@ -103,9 +103,10 @@ void launch_mass_f64(const Graph& G, const double* h, double* acc, cudaStream_t 
 // Launch configuration of the mixed kernels, per kernel kind (0 dt, 1 node,
 // 2 low, 3 fct, 4 update): block size, entry batch (1, 2, 4 or 8; 1 or 2
 // for low), grid (one thread per row, or a resident grid striding over the
-// rows), and for low the tighter of two register caps (cap_low: 64 instead of
-// 85 registers).  Chosen by the
-// autotuner in swe_api.cu.  Every choice sums in the same entry order; the
+// rows, or one block per tile of rows with shared-memory neighbours), and for
+// low a register cap (cap_low 0, 1, 2: at least 3, 4 or 5 resident blocks of
+// 256 threads per SM, i.e. at most 85, 64 or 51 registers; the tightest
+// spills a little).  Chosen by the autotuner in swe_api.cu.  Every choice sums in the same entry order; the
 // variants are separate instantiations whose FMA contraction may differ, so
 // results agree to FP32 rounding.
 struct KernelTune {
@@ -113,7 +114,7 @@ struct KernelTune {
   int batch[5] = {1, 1, 1, 1, 1};
   int grid[5] = {0, 0, 0, 0, 0};   // 0: a thread per row; k: k resident grids striding over the rows
   int cap_low = 0;
-  int tiled[5] = {0, 0, 0, 0, 0};  // 1: the shared-memory tile variant (grid: one block per tile)
+  int tiled[5] = {0, 0, 0, 0, 0};  // shared-memory tile variant: 1 a block per tile, 2 resident blocks walking tiles
 };
 
 void launch_stage_mix(const StageArgsMix& a, cudaStream_t s, const KernelEvents* kev, const KernelTune& t);
