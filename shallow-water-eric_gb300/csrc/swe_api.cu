@@ -256,20 +256,17 @@ static int build_device(swe_ctx* c, const std::vector<std::vector<double>>& bath
     w.qL = c->buf.alloc<float2>(n, st);
     if (c->S == 5) { w.q3L = c->buf.alloc<float>(n, st); w.q4L = c->buf.alloc<float>(n, st); }
     // row tiles of the shared-memory kernel variants (SWE_TILE rows, default
-    // 256; 0 disables), while two buffers of the tile and its halo fit in 48 KB
+    // 256; 0 disables), while the tile and its halo fit in 48 KB
     const char* ft = getenv("SWE_TILE");
     const int tile = ft ? atoi(ft) : 256;
     RowTiles F;
-    if (c->S == 3 && tile > 0 && build_row_tiles(L, tile, F)) {
-      const int halo_cap = (F.halo_cap + 3) & ~3;
-      if ((size_t)(F.tile + halo_cap) * 48 <= 48 * 1024) {
-        c->tiles.loc = upload_vec(c, F.loc, st);
-        c->tiles.halo_ptr = upload_vec(c, F.halo_ptr, st);
-        c->tiles.halo_rows = upload_vec(c, F.halo_rows, st);
-        c->tiles.tile_rows = F.tile;
-        c->tiles.halo_cap = halo_cap;
-        c->tiles_ok = true;
-      }
+    if (c->S == 3 && tile > 0 && build_row_tiles(L, tile, F) && (size_t)(F.tile + F.halo_cap) * 24 <= 48 * 1024) {
+      c->tiles.loc = upload_vec(c, F.loc, st);
+      c->tiles.halo_ptr = upload_vec(c, F.halo_ptr, st);
+      c->tiles.halo_rows = upload_vec(c, F.halo_rows, st);
+      c->tiles.tile_rows = F.tile;
+      c->tiles.halo_cap = F.halo_cap;
+      c->tiles_ok = true;
     }
   }
   if (st != cudaSuccess) return fail(c, SWE_ERR_CUDA, std::string("device allocation: ") + cudaGetErrorString(st));
@@ -913,10 +910,9 @@ static int autotune(swe_ctx* c) {
   for (int kind = 0; kind < 5; kind++) {
     float best = 1e30f;
     int bb = t.block[kind], bt = t.batch[kind], bc = t.cap_low, bg = t.grid[kind], btl = t.tiled[kind];
-    // grid modes: a thread per row, resident grid, shared-memory tiles (a
-    // block per tile, or resident blocks walking the tiles)
+    // grid modes: a thread per row, resident grid, shared-memory tiles
     const bool tiles = a_low.tiles && kind_has_tiles(kind) && !(tenv && tenv[0] == '0');
-    const int gm0 = (tiles && tenv && tenv[0] == '1') ? 2 : 0, n_modes = tiles ? 4 : 2;
+    const int gm0 = (tiles && tenv && tenv[0] == '1') ? 2 : 0, n_modes = tiles ? 3 : 2;
     for (int ib = 0; ib < 3; ib++)
       for (int it = 0; it < 4; it++)
         for (int cap = 0; cap < (kind == 2 ? 3 : 1); cap++)
@@ -926,7 +922,7 @@ static int autotune(swe_ctx* c) {
             v.block[kind] = blocks[ib];
             v.batch[kind] = batches[it];
             v.grid[kind] = gm == 1;
-            v.tiled[kind] = gm >= 2 ? gm - 1 : 0;
+            v.tiled[kind] = gm == 2;
             if (kind == 2) v.cap_low = cap;
             float tmin = 1e30f;
             for (int rep = 0; rep < 3; rep++) {
@@ -940,7 +936,7 @@ static int autotune(swe_ctx* c) {
               tmin = std::min(tmin, ms);
             }
             if (tmin < best) {
-              best = tmin; bb = blocks[ib]; bt = batches[it]; bg = gm == 1; btl = gm >= 2 ? gm - 1 : 0;
+              best = tmin; bb = blocks[ib]; bt = batches[it]; bg = gm == 1; btl = gm == 2;
               if (kind == 2) bc = cap;
             }
           }
@@ -952,7 +948,7 @@ static int autotune(swe_ctx* c) {
     char buf[96];
     snprintf(buf, sizeof buf, "%s%s:block%d/batch%d%s%s", kind ? " " : "", names[kind], bb, bt,
              kind == 2 ? (bc == 2 ? "/regs51" : bc ? "/regs64" : "/regs85") : "",
-             bg ? "/resident" : (btl == 2 ? "/tiled/resident" : btl ? "/tiled" : ""));
+             bg ? "/resident" : (btl ? "/tiled" : ""));
     desc += buf;
   }
   cudaEventDestroy(e0);

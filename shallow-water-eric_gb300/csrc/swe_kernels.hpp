@@ -68,7 +68,7 @@ struct TileCtl {
   const int* halo_ptr;    // n_tiles + 1
   const int* halo_rows;   // ascending per tile
   int tile_rows;
-  int halo_cap;           // largest halo, rounded so tile_rows + halo_cap is a multiple of 4
+  int halo_cap;           // largest halo
 };
 
 struct StageArgsMix {
@@ -114,7 +114,7 @@ struct KernelTune {
   int batch[5] = {1, 1, 1, 1, 1};
   int grid[5] = {0, 0, 0, 0, 0};   // 0: a thread per row; k: k resident grids striding over the rows
   int cap_low = 0;
-  int tiled[5] = {0, 0, 0, 0, 0};  // shared-memory tile variant: 1 a block per tile, 2 resident blocks walking tiles
+  int tiled[5] = {0, 0, 0, 0, 0};  // 1: the shared-memory tile variant (grid: one block per tile)
 };
 
 void launch_stage_mix(const StageArgsMix& a, cudaStream_t s, const KernelEvents* kev, const KernelTune& t);

@@ -176,93 +176,42 @@ struct NbTile {
   __device__ __forceinline__ int self(int64_t r) const { return (int)(r - t0); }
 };
 
-// Shared-memory tile buffer: node records, aux and R^- of the tile's rows
-// (positions 0 .. T-1) and of its halo rows (T .. T+nh-1); cap = T + halo_cap
-// is a multiple of 4, so consecutive buffers keep 16-byte alignment.
+// Shared-memory tile of one block: node records, aux and R^- of the tile's
+// rows (positions 0 .. T-1) and of its halo rows (T .. T+nh-1).
 struct TileSmem {
   float4* nq;
   float* aux;
   float* R;
 };
-__device__ __forceinline__ TileSmem tile_smem(float4* base, int cap, int k) {
-  float4* nq = base + (size_t)k * (cap + cap / 2);      // 24 bytes per position
+__device__ __forceinline__ TileSmem tile_smem(void* base, int cap) {
+  float4* nq = reinterpret_cast<float4*>(base);
   float* aux = reinterpret_cast<float*>(nq + cap);
   return TileSmem{nq, aux, aux + cap};
 }
 
-__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
-
-// Start the asynchronous copy of tile t's and its halo's node data into a
-// buffer (the tile rows are contiguous; the halo rows ascend).
+// Copy the tile's and the halo's node data into shared memory (coalesced for
+// the tile rows, ascending gathers for the halo); returns the tile start.
 template <bool AUX, bool RM>
-__device__ __forceinline__ void tile_fetch(const Graph& G, const TileCtl& tc, const StateMix& u,
-                                           const float* __restrict__ aux, const float* __restrict__ rminus,
-                                           const TileSmem& sm, int64_t t) {
+__device__ __forceinline__ int64_t stage_tile(const Graph& G, const TileCtl& tc, const StateMix& u,
+                                              const float* __restrict__ aux, const float* __restrict__ rminus,
+                                              const TileSmem& sm) {
   const int T = tc.tile_rows;
-  const int64_t t0 = t * T;
-  const int h0 = tc.halo_ptr[t], nh = tc.halo_ptr[t + 1] - h0;
+  const int64_t t0 = (int64_t)blockIdx.x * T;
+  const int h0 = tc.halo_ptr[blockIdx.x], nh = tc.halo_ptr[blockIdx.x + 1] - h0;
   for (int i = threadIdx.x; i < T + nh; i += blockDim.x) {
     const int64_t row = i < T ? t0 + i : (int64_t)tc.halo_rows[h0 + i - T];
     if (row < G.n_rows) {
-      cp_async16(&sm.nq[i], &u.nq[row]);
-      if (AUX) cp_async4(&sm.aux[i], &aux[row]);
-      if (RM) cp_async4(&sm.R[i], &rminus[row]);
+      sm.nq[i] = u.nq[row];
+      if (AUX) sm.aux[i] = aux[row];
+      if (RM) sm.R[i] = rminus[row];
     }
   }
+  __syncthreads();
+  return t0;
 }
 
-// Tiles of a block: with a block per tile (gridDim.x = number of tiles), one
-// synchronous copy of the tile's node data; with a resident grid, the blocks
-// walk the tiles blockIdx.x, blockIdx.x + gridDim.x, ... with two buffers,
-// tile k+1's asynchronous copy in flight while the block computes tile k.
-// body(nb, t0, t1) processes rows [t0, t1) reading neighbours through nb.
-template <bool AUX, bool RM, class Body>
-__device__ __forceinline__ void tile_loop(const Graph& G, const TileCtl& tc, const StateMix& u,
-                                          const float* __restrict__ aux, const float* __restrict__ rminus,
-                                          float4* smem, Body&& body) {
-  const int cap = tc.tile_rows + tc.halo_cap;
-  const int64_t n_tiles = (G.n_rows + tc.tile_rows - 1) / tc.tile_rows;
-  const TileSmem buf[2] = {tile_smem(smem, cap, 0), tile_smem(smem, cap, 1)};
-  if ((int64_t)gridDim.x >= n_tiles) {
-    const int T = tc.tile_rows;
-    const int64_t t = blockIdx.x, t0 = t * T;
-    if (t >= n_tiles) return;
-    const int h0 = tc.halo_ptr[t], nh = tc.halo_ptr[t + 1] - h0;
-    for (int i = threadIdx.x; i < T + nh; i += blockDim.x) {
-      const int64_t row = i < T ? t0 + i : (int64_t)tc.halo_rows[h0 + i - T];
-      if (row < G.n_rows) {
-        buf[0].nq[i] = u.nq[row];
-        if (AUX) buf[0].aux[i] = aux[row];
-        if (RM) buf[0].R[i] = rminus[row];
-      }
-    }
-    __syncthreads();
-    const int64_t t1 = t0 + T < G.n_rows ? t0 + T : G.n_rows;
-    body(NbTile{tc.loc, buf[0].nq, buf[0].aux, buf[0].R, t0}, t0, t1);
-    return;
-  }
-  int k = 0;
-  if ((int64_t)blockIdx.x < n_tiles) tile_fetch<AUX, RM>(G, tc, u, aux, rminus, buf[0], blockIdx.x);
-  cp_async_commit();
-  for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x, k ^= 1) {
-    if (t + gridDim.x < n_tiles) tile_fetch<AUX, RM>(G, tc, u, aux, rminus, buf[k ^ 1], t + gridDim.x);
-    cp_async_commit();
-    cp_async_wait_prev();          // this thread's copies of tile t have landed
-    __syncthreads();               // and every thread's
-    const int64_t t0 = t * tc.tile_rows;
-    const int64_t t1 = t0 + tc.tile_rows < G.n_rows ? t0 + tc.tile_rows : G.n_rows;
-    body(NbTile{tc.loc, buf[k].nq, buf[k].aux, buf[k].R, t0}, t0, t1);
-    __syncthreads();               // buf[k] is refilled next iteration
-  }
+__device__ __forceinline__ int64_t tile_end(const Graph& G, const TileCtl& tc, int64_t t0) {
+  return t0 + tc.tile_rows < G.n_rows ? t0 + tc.tile_rows : G.n_rows;
 }
 
 // k_node_mix: alpha_i (SOURCES/update.f90:758-781) from the FP32 depth.
@@ -316,9 +265,11 @@ __global__ void __launch_bounds__(256) k_node_tile(Graph G, const InstConst* __r
                                                    const InstState* __restrict__ St, StateMix u,
                                                    float* __restrict__ alpha_out, TileCtl tc) {
   extern __shared__ float4 tile_mem[];
-  tile_loop<false, false>(G, tc, u, nullptr, nullptr, tile_mem, [&](const NbTile& nb, int64_t t0, int64_t t1) {
-    for (int64_t r = t0 + threadIdx.x; r < t1; r += blockDim.x) node_row<B>(r, G, C, St, u, alpha_out, nb);
-  });
+  const TileSmem sm = tile_smem(tile_mem, tc.tile_rows + tc.halo_cap);
+  const int64_t t0 = stage_tile<false, false>(G, tc, u, nullptr, nullptr, sm);
+  const int64_t t1 = tile_end(G, tc, t0);
+  const NbTile nb{tc.loc, sm.nq, nullptr, nullptr, t0};
+  for (int64_t r = t0 + threadIdx.x; r < t1; r += blockDim.x) node_row<B>(r, G, C, St, u, alpha_out, nb);
 }
 
 struct NodeF {   // FP32 view of one node used by the edge loop
@@ -568,10 +519,12 @@ __global__ void __launch_bounds__(256, MINB) k_low_tile(Graph G, const InstConst
                                                         WorkMix w, float* __restrict__ res, unsigned* __restrict__ err,
                                                         TileCtl tc) {
   extern __shared__ float4 tile_mem[];
-  tile_loop<true, false>(G, tc, u, alpha, nullptr, tile_mem, [&](const NbTile& nb, int64_t t0, int64_t t1) {
-    for (int64_t r = t0 + threadIdx.x; r < t1; r += blockDim.x)
-      low_row<B, LAMIN, MINB>(r, G, C, St, u, alpha, dmu, w, res, err, nb);
-  });
+  const TileSmem sm = tile_smem(tile_mem, tc.tile_rows + tc.halo_cap);
+  const int64_t t0 = stage_tile<true, false>(G, tc, u, alpha, nullptr, sm);
+  const int64_t t1 = tile_end(G, tc, t0);
+  const NbTile nb{tc.loc, sm.nq, sm.aux, nullptr, t0};
+  for (int64_t r = t0 + threadIdx.x; r < t1; r += blockDim.x)
+    low_row<B, LAMIN, MINB>(r, G, C, St, u, alpha, dmu, w, res, err, nb);
 }
 
 // Limiter margin: (1 - 2^-18) Q^-.  Between the limiter and the depth update
@@ -659,9 +612,11 @@ __global__ void __launch_bounds__(256) k_fct_tile(Graph G, const InstConst* __re
                                                   const float2* __restrict__ dmu, WorkMix w,
                                                   const float* __restrict__ res, unsigned* __restrict__ err, TileCtl tc) {
   extern __shared__ float4 tile_mem[];
-  tile_loop<true, false>(G, tc, u, res, nullptr, tile_mem, [&](const NbTile& nb, int64_t t0, int64_t t1) {
-    for (int64_t r = t0 + threadIdx.x; r < t1; r += blockDim.x) fct_row<B>(r, G, C, St, u, dmu, w, res, err, nb);
-  });
+  const TileSmem sm = tile_smem(tile_mem, tc.tile_rows + tc.halo_cap);
+  const int64_t t0 = stage_tile<true, false>(G, tc, u, res, nullptr, sm);
+  const int64_t t1 = tile_end(G, tc, t0);
+  const NbTile nb{tc.loc, sm.nq, sm.aux, nullptr, t0};
+  for (int64_t r = t0 + threadIdx.x; r < t1; r += blockDim.x) fct_row<B>(r, G, C, St, u, dmu, w, res, err, nb);
 }
 
 // End of a stage for one row: non-finite check, the SSP-RK combination and
@@ -801,10 +756,12 @@ __global__ void __launch_bounds__(256) k_update_tile(Graph G, const InstConst* _
                                                      const float* __restrict__ res, StateMix u0, StateMix out,
                                                      int rk_stage, unsigned* __restrict__ err, TileCtl tc) {
   extern __shared__ float4 tile_mem[];
-  tile_loop<true, true>(G, tc, u, res, w.rminus, tile_mem, [&](const NbTile& nb, int64_t t0, int64_t t1) {
-    for (int64_t r = t0 + threadIdx.x; r < t1; r += blockDim.x)
-      update_row<B>(r, G, C, St, u, dmu, w, res, u0, out, rk_stage, err, nb);
-  });
+  const TileSmem sm = tile_smem(tile_mem, tc.tile_rows + tc.halo_cap);
+  const int64_t t0 = stage_tile<true, true>(G, tc, u, res, w.rminus, sm);
+  const int64_t t1 = tile_end(G, tc, t0);
+  const NbTile nb{tc.loc, sm.nq, sm.aux, sm.R, t0};
+  for (int64_t r = t0 + threadIdx.x; r < t1; r += blockDim.x)
+    update_row<B>(r, G, C, St, u, dmu, w, res, u0, out, rk_stage, err, nb);
 }
 
 // k_dt_mix: FP32 lambda_max, max |d_ii|/m_i per instance (main.f90:166-174).
@@ -908,15 +865,15 @@ __global__ void __launch_bounds__(256) k_dt_tile(Graph G, const InstConst* __res
                                                  StateMix u, float* __restrict__ dlam, float* __restrict__ alpha_out,
                                                  unsigned* __restrict__ err, TileCtl tc) {
   extern __shared__ float4 tile_mem[];
-  tile_loop<false, false>(G, tc, u, nullptr, nullptr, tile_mem, [&](const NbTile& nb, int64_t t0, int64_t) {
-    // tile_rows is a multiple of 32: every lane of a warp runs the same
-    // iterations (warps past the tile's end skip them together)
-    for (int64_t rb = t0; rb < t0 + tc.tile_rows; rb += blockDim.x) {
-      if (rb - t0 + (int64_t)(threadIdx.x & ~31u) >= tc.tile_rows) break;
-      const int64_t r = rb + threadIdx.x;
-      dt_reduce(dt_row<B>(r, G, C, St, u, dlam, alpha_out, err, nb), r, G, St);
-    }
-  });
+  const TileSmem sm = tile_smem(tile_mem, tc.tile_rows + tc.halo_cap);
+  const int64_t t0 = stage_tile<false, false>(G, tc, u, nullptr, nullptr, sm);
+  const NbTile nb{tc.loc, sm.nq, nullptr, nullptr, t0};
+  // tile_rows is a multiple of 32: every lane of a warp runs the same iterations
+  for (int64_t rb = t0; rb < t0 + tc.tile_rows; rb += blockDim.x) {
+    const int64_t r = rb + threadIdx.x;
+    if (rb - t0 + (int64_t)threadIdx.x - (threadIdx.x & 31) >= tc.tile_rows) break;   // warp past the tile
+    dt_reduce(dt_row<B>(r, G, C, St, u, dlam, alpha_out, err, nb), r, G, St);
+  }
 }
 
 // Copy the bathymetry into the packed node records after a bathymetry change
@@ -988,40 +945,17 @@ static unsigned row_grid(K kern, int64_t n, int block, int mode) {
 
 // Tile variants: one block per tile, shared memory for the tile's and the
 // halo's node records, residuals and R^- (24 B per row)
-// one buffer of 24 bytes per position with a block per tile, two when resident
-inline size_t tile_smem_bytes(const TileCtl& tc, int mode) {
-  return (size_t)(tc.tile_rows + tc.halo_cap) * (mode >= 2 ? 48 : 24);
-}
-
-// Grid of a tile kernel: a block per tile (mode 1), or a resident grid whose
-// blocks walk the tiles with the next tile's copy in flight (mode 2).
-template <typename K>
-static unsigned tile_grid(K kern, int64_t n_tiles, int block, size_t smem, int mode) {
-  if (mode < 2) return (unsigned)n_tiles;
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  }
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem) != cudaSuccess || per_sm <= 0) {
-    cudaGetLastError();
-    return (unsigned)n_tiles;
-  }
-  const int64_t g = (int64_t)per_sm * sms;
-  return (unsigned)(g < n_tiles ? g : n_tiles);
-}
-#define SWE_DISPATCH_TILE(b, KERNEL, BS, MODE, TC, NROWS, ...)                                          \
+inline size_t tile_smem_bytes(const TileCtl& tc) { return (size_t)(tc.tile_rows + tc.halo_cap) * 24; }
+#define SWE_DISPATCH_TILE(b, KERNEL, BS, TC, NROWS, ...)                                                \
   do {                                                                                                \
     const TileCtl& tc_ = (TC);                                                                        \
-    const int64_t nt_ = ((NROWS) + tc_.tile_rows - 1) / tc_.tile_rows;                                \
-    const size_t sm_ = tile_smem_bytes(tc_, MODE);                                                    \
+    const unsigned g_ = (unsigned)(((NROWS) + tc_.tile_rows - 1) / tc_.tile_rows);                    \
+    const size_t sm_ = tile_smem_bytes(tc_);                                                          \
     switch (b) {                                                                                      \
-      case 8: KERNEL<8><<<tile_grid(KERNEL<8>, nt_, BS, sm_, MODE), BS, sm_, s>>>(__VA_ARGS__); break; \
-      case 4: KERNEL<4><<<tile_grid(KERNEL<4>, nt_, BS, sm_, MODE), BS, sm_, s>>>(__VA_ARGS__); break; \
-      case 2: KERNEL<2><<<tile_grid(KERNEL<2>, nt_, BS, sm_, MODE), BS, sm_, s>>>(__VA_ARGS__); break; \
-      default: KERNEL<1><<<tile_grid(KERNEL<1>, nt_, BS, sm_, MODE), BS, sm_, s>>>(__VA_ARGS__); break; \
+      case 8: KERNEL<8><<<g_, BS, sm_, s>>>(__VA_ARGS__); break;                                      \
+      case 4: KERNEL<4><<<g_, BS, sm_, s>>>(__VA_ARGS__); break;                                      \
+      case 2: KERNEL<2><<<g_, BS, sm_, s>>>(__VA_ARGS__); break;                                      \
+      default: KERNEL<1><<<g_, BS, sm_, s>>>(__VA_ARGS__); break;                                     \
     }                                                                                                 \
   } while (0)
 
@@ -1029,14 +963,13 @@ static unsigned tile_grid(K kern, int64_t n_tiles, int block, size_t smem, int m
 // k_dt_mix (stage 1), registers capped at 85, 64 or 51 (3, 4 or 5 resident
 // blocks of 256 threads per SM; the compiler would take ~106 with no cap)
 template <bool LAMIN>
-static void launch_low(const StageArgsMix& a, int batch, int cap, int mode, int block, int tiled, cudaStream_t s) {
+static void launch_low(const StageArgsMix& a, int batch, int cap, int mode, int block, bool tiled, cudaStream_t s) {
   if (tiled && a.tiles) {
     const TileCtl& tc = *a.tiles;
-    const int64_t nt = (a.G.n_rows + tc.tile_rows - 1) / tc.tile_rows;
-    const size_t sm = tile_smem_bytes(tc, tiled);
-#define SWE_LOWT(BB, MB)                                                                              \
-    k_low_tile<BB, LAMIN, MB><<<tile_grid(k_low_tile<BB, LAMIN, MB>, nt, block, sm, tiled), block, sm, s>>>( \
-        a.G, a.C, a.St, a.u, a.w.alpha, a.w.dmu, a.w, a.w.res, a.err, tc)
+    const unsigned g = (unsigned)((a.G.n_rows + tc.tile_rows - 1) / tc.tile_rows);
+    const size_t sm = tile_smem_bytes(tc);
+#define SWE_LOWT(BB, MB) \
+    k_low_tile<BB, LAMIN, MB><<<g, block, sm, s>>>(a.G, a.C, a.St, a.u, a.w.alpha, a.w.dmu, a.w, a.w.res, a.err, tc)
     if (batch >= 2) { if (cap == 2) SWE_LOWT(2, 5); else if (cap) SWE_LOWT(2, 4); else SWE_LOWT(2, 3); }
     else { if (cap == 2) SWE_LOWT(1, 5); else if (cap) SWE_LOWT(1, 4); else SWE_LOWT(1, 3); }
 #undef SWE_LOWT
@@ -1056,7 +989,7 @@ void launch_kernel_mix(int kind, const StageArgsMix& a, const KernelTune& t, cud
   const int64_t n = a.G.n_rows;
   switch (kind) {
     case 1: if (t.tiled[1] && a.tiles) {
-              SWE_DISPATCH_TILE(t.batch[1], k_node_tile, t.block[1], t.tiled[1], *a.tiles, n, a.G, a.C, a.St, a.u, a.w.alpha, *a.tiles);
+              SWE_DISPATCH_TILE(t.batch[1], k_node_tile, t.block[1], *a.tiles, n, a.G, a.C, a.St, a.u, a.w.alpha, *a.tiles);
             } else {
               SWE_DISPATCH_B(t.batch[1], k_node_mix, n, t.block[1], t.grid[1], a.G, a.C, a.St, a.u, a.w.alpha)
             }
@@ -1067,7 +1000,7 @@ void launch_kernel_mix(int kind, const StageArgsMix& a, const KernelTune& t, cud
               launch_low<false>(a, t.batch[2], t.cap_low, t.grid[2], t.block[2], t.tiled[2], s);
             break;
     case 3: if (t.tiled[3] && a.tiles) {
-              SWE_DISPATCH_TILE(t.batch[3], k_fct_tile, t.block[3], t.tiled[3], *a.tiles, n, a.G, a.C, a.St, a.u, a.w.dmu, a.w, a.w.res, a.err,
+              SWE_DISPATCH_TILE(t.batch[3], k_fct_tile, t.block[3], *a.tiles, n, a.G, a.C, a.St, a.u, a.w.dmu, a.w, a.w.res, a.err,
                                 *a.tiles);
             } else {
               SWE_DISPATCH_B(t.batch[3], k_fct_mix, n, t.block[3], t.grid[3], a.G, a.C, a.St, a.u, a.w.dmu, a.w,
@@ -1075,7 +1008,7 @@ void launch_kernel_mix(int kind, const StageArgsMix& a, const KernelTune& t, cud
             }
             break;
     case 4: if (t.tiled[4] && a.tiles) {
-              SWE_DISPATCH_TILE(t.batch[4], k_update_tile, t.block[4], t.tiled[4], *a.tiles, n, a.G, a.C, a.St, a.u, a.w.dmu, a.w, a.w.res,
+              SWE_DISPATCH_TILE(t.batch[4], k_update_tile, t.block[4], *a.tiles, n, a.G, a.C, a.St, a.u, a.w.dmu, a.w, a.w.res,
                                 a.u0, a.out, a.rk_stage, a.err, *a.tiles);
             } else {
               SWE_DISPATCH_B(t.batch[4], k_update_mix, n, t.block[4], t.grid[4], a.G, a.C, a.St, a.u, a.w.dmu, a.w,
@@ -1098,7 +1031,7 @@ void launch_stage_mix(const StageArgsMix& a, cudaStream_t s, const KernelEvents*
 void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, float* dlam, float* alpha,
                    unsigned* err, const KernelTune& t, const TileCtl* tiles, cudaStream_t s) {
   if (t.tiled[0] && tiles) {
-    SWE_DISPATCH_TILE(t.batch[0], k_dt_tile, t.block[0], t.tiled[0], *tiles, G.n_rows, G, C, St, u, dlam, alpha, err, *tiles);
+    SWE_DISPATCH_TILE(t.batch[0], k_dt_tile, t.block[0], *tiles, G.n_rows, G, C, St, u, dlam, alpha, err, *tiles);
   } else {
     SWE_DISPATCH_B(t.batch[0], k_dt_mix, G.n_rows, t.block[0], t.grid[0], G, C, St, u, dlam, alpha, err)
   }
