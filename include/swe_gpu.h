@@ -195,11 +195,14 @@ double swe_last_device_ms(const swe_ctx* ctx);
 enum { SWE_NKERNELS = 5 };
 int swe_profile_kernels(swe_ctx* ctx, int nsteps, double* ms_out);
 
-/* Autotuner: times every block-size / entry-batch variant of the mixed
- * kernels on the current state and keeps the fastest per kernel (variants
- * agree to FP32 rounding).  swe_rk3_steps runs it on its first call unless the
- * environment sets SWE_AUTOTUNE=0.  swe_tuning names the chosen
- * configuration. */
+/* Autotuner: times every block-size / entry-batch / grid variant of the
+ * mixed kernels (including the shared-memory row-tile variants) on the
+ * current state and keeps the fastest per kernel (variants agree to FP32
+ * rounding).  swe_rk3_steps runs it on its first call unless the environment
+ * sets SWE_AUTOTUNE=0.  swe_tuning names the chosen configuration; setting
+ * SWE_TUNE to that description (the text after "autotuned ") makes a later
+ * context launch exactly those variants without timing (a malformed value
+ * -> SWE_ERR_ARG). */
 int swe_autotune(swe_ctx* ctx);
 const char* swe_tuning(const swe_ctx* ctx);
 

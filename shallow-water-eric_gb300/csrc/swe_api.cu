@@ -880,8 +880,65 @@ SWE_API int swe_set_time(swe_ctx* c, const double* time, const double* t_final) 
 // size, entry batch) variant on the current state and keep the fastest.  The
 // variants agree to FP32 rounding, and every timed kernel is idempotent on its
 // inputs (it only rewrites its own outputs), so the state is unchanged.
+// Launch configuration from the autotuner's own description ("dt:block256/
+// batch4/resident node:... low:block128/batch2/regs64/tiled ..."), so that a
+// profiling run can reproduce the variants a timed run chose.  Kinds not
+// named keep their defaults; false on a malformed string.
+static bool parse_tuning(const char* spec, bool tiles, KernelTune& t) {
+  const char* names[5] = {"dt", "node", "low", "fct", "update"};
+  std::string str(spec);
+  size_t pos = 0;
+  while (pos < str.size()) {
+    size_t end = str.find(' ', pos);
+    if (end == std::string::npos) end = str.size();
+    const std::string tok = str.substr(pos, end - pos);
+    pos = end + 1;
+    if (tok.empty()) continue;
+    const size_t colon = tok.find(':');
+    if (colon == std::string::npos) return false;
+    int kind = -1;
+    for (int k = 0; k < 5; k++)
+      if (tok.compare(0, colon, names[k]) == 0) kind = k;
+    if (kind < 0) return false;
+    int block = 0, batch = 0, cap = 0, grid = 0, tiled = 0;
+    size_t p = colon + 1;
+    while (p < tok.size()) {
+      size_t q = tok.find('/', p);
+      if (q == std::string::npos) q = tok.size();
+      const std::string f = tok.substr(p, q - p);
+      p = q + 1;
+      if (f.compare(0, 5, "block") == 0) block = atoi(f.c_str() + 5);
+      else if (f.compare(0, 5, "batch") == 0) batch = atoi(f.c_str() + 5);
+      else if (f == "regs85") cap = 0;
+      else if (f == "regs64") cap = 1;
+      else if (f == "regs51") cap = 2;
+      else if (f == "resident") grid = 1;
+      else if (f == "tiled") tiled = 1;
+      else return false;
+    }
+    if (!(block == 64 || block == 128 || block == 256) || !(batch == 1 || batch == 2 || batch == 4 || batch == 8))
+      return false;
+    if ((kind == 2 && batch > 2) || (tiled && !tiles)) return false;
+    t.block[kind] = block;
+    t.batch[kind] = batch;
+    t.grid[kind] = grid;
+    t.tiled[kind] = tiled;
+    if (kind == 2) t.cap_low = cap;
+  }
+  return true;
+}
+
 static int autotune(swe_ctx* c) {
   if (c->precision != SWE_PREC_MIXED) { c->tuned = true; return SWE_OK; }
+  if (const char* spec = getenv("SWE_TUNE")) {   // a fixed configuration instead of timing
+    KernelTune t;
+    if (!parse_tuning(spec, c->tiles_ok, t)) return fail(c, SWE_ERR_ARG, std::string("bad SWE_TUNE: ") + spec);
+    c->tune = t;
+    c->tuned = true;
+    c->tuning = std::string("thread-per-row SELL-32; fixed ") + spec;
+    if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; c->graph_steps = 0; }
+    return SWE_OK;
+  }
   int rc;
   std::vector<InstState> saved;
   if ((rc = save_state(c, saved))) return rc;

@@ -495,3 +495,31 @@ def test_tiled_kernels_match_global_gathers(golden, monkeypatch, tile):
     assert _rel_l1(traj["1"][0], traj["0"][0], lump) <= 1e-6
     scale = np.abs(traj["0"]).max(axis=1, keepdims=True) + 1e-300
     assert np.max(np.abs(traj["1"] - traj["0"]) / scale) <= 1e-5
+
+
+def test_fixed_tuning_reproduces_autotuned_variants(monkeypatch):
+    """SWE_TUNE takes the autotuner's own description and launches exactly
+    those variants (profiling runs pin the timed run's choice with it)."""
+    case = C.bump_basin_case(n=60)
+    monkeypatch.delenv("SWE_TUNE", raising=False)
+    upd = from_case(case, precision=1)
+    upd.upload(case.u0)
+    upd.set_time(0.0, 1e30)
+    upd.rk3_steps(10)
+    ref = upd.download()
+    spec = upd.tuning.split("autotuned ", 1)[1]
+    upd.close()
+    monkeypatch.setenv("SWE_TUNE", spec)
+    upd = from_case(case, precision=1)
+    upd.upload(case.u0)
+    upd.set_time(0.0, 1e30)
+    upd.rk3_steps(10)
+    assert upd.tuning.endswith("fixed " + spec)
+    np.testing.assert_array_equal(upd.download(), ref)
+    upd.close()
+    monkeypatch.setenv("SWE_TUNE", "low:block100/batch2")
+    upd = from_case(case, precision=1)
+    upd.upload(case.u0)
+    with pytest.raises(L.SweError, match="SWE_TUNE"):
+        upd.rk3_steps(1)
+    upd.close()
