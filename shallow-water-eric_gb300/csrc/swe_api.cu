@@ -38,6 +38,12 @@ struct DevBuf {
 struct swe_ctx {
   int dev = 0;
   cudaStream_t stream = nullptr;
+  // state transfers: chunks copied on their own streams (several copy engines)
+  // and permuted on `stream` as each lands
+  static constexpr int kMaxCopyChunks = 8;
+  cudaStream_t copy_stream[kMaxCopyChunks] = {};
+  cudaEvent_t copy_ev[kMaxCopyChunks] = {}, copy_go = nullptr;
+  int copy_chunks = 0;
   int n_inst = 0, S = 3, precision = 0;
   std::vector<HostMesh> meshes;
   std::vector<swe_params> params;
@@ -73,6 +79,7 @@ struct swe_ctx {
   // graph of `graph_steps` time steps
   cudaGraphExec_t gexec = nullptr;
   int graph_steps = 0;
+  cudaGraphExec_t gexec1 = nullptr;      // one time step (the remainder of a call)
   int block = 128;
   KernelTune tune;
   bool tuned = false;
@@ -323,21 +330,53 @@ __global__ void k_gather_out_mix(double* __restrict__ stage, const int* __restri
   }
 }
 
+// Node ranges of the transfer chunks: k of `chunks` equal parts of [b, e).
+static inline int64_t chunk_at(int64_t b, int64_t e, int k, int chunks) { return b + (e - b) * k / chunks; }
+
+// Copy streams and events on first use (SWE_COPY_CHUNKS, default 4, 1..8).
+static int copy_setup(swe_ctx* c) {
+  if (c->copy_chunks) return SWE_OK;
+  const char* env = getenv("SWE_COPY_CHUNKS");
+  int k = env ? atoi(env) : 4;
+  k = std::max(1, std::min(k, (int)swe_ctx::kMaxCopyChunks));
+  for (int i = 0; i < k; i++) {
+    CK(cudaStreamCreateWithFlags(&c->copy_stream[i], cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&c->copy_ev[i], cudaEventDisableTiming));
+  }
+  CK(cudaEventCreateWithFlags(&c->copy_go, cudaEventDisableTiming));
+  c->copy_chunks = k;
+  return SWE_OK;
+}
+
 static int to_device(swe_ctx* c, const double* un, bool device_src, int64_t node_begin, int64_t node_end) {
   const int64_t nn = node_end - node_begin;
   if (nn <= 0) return SWE_OK;
-  const size_t bytes = (size_t)c->S * nn * sizeof(double);
-  CK(cudaMemcpyAsync(c->d_stage + (size_t)c->S * node_begin, un, bytes,
-                     device_src ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream));
-  const unsigned nb = (unsigned)((nn + 255) / 256);
-  if (c->precision == SWE_PREC_FP64)
-    k_scatter_in<<<nb, 256, 0, c->stream>>>(c->d_stage + (size_t)c->S * node_begin, c->d_row_of_node + node_begin,
-                                             nn, c->S, c->A);
-  else
-    k_scatter_in_mix<<<nb, 256, 0, c->stream>>>(c->d_stage + (size_t)c->S * node_begin,
-                                                 c->d_row_of_node + node_begin, nn, c->S, c->mA, c->G.slice_inst,
-                                                 c->d_C, c->G.bathf);
-  CK(cudaGetLastError());
+  int rc = copy_setup(c);
+  if (rc) return rc;
+  const int K = nn >= 1024 ? c->copy_chunks : 1;
+  // chunk k: copy on copy_stream[k] (after the work already on `stream`),
+  // then its permutation into the rows on `stream` once it has landed
+  CK(cudaEventRecord(c->copy_go, c->stream));
+  for (int k = 0; k < K; k++) {
+    const int64_t b = chunk_at(node_begin, node_end, k, K), e = chunk_at(node_begin, node_end, k + 1, K);
+    CK(cudaStreamWaitEvent(c->copy_stream[k], c->copy_go, 0));
+    CK(cudaMemcpyAsync(c->d_stage + (size_t)c->S * b, un + (size_t)c->S * (b - node_begin),
+                       (size_t)c->S * (e - b) * sizeof(double),
+                       device_src ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->copy_stream[k]));
+    CK(cudaEventRecord(c->copy_ev[k], c->copy_stream[k]));
+  }
+  for (int k = 0; k < K; k++) {
+    const int64_t b = chunk_at(node_begin, node_end, k, K), e = chunk_at(node_begin, node_end, k + 1, K);
+    CK(cudaStreamWaitEvent(c->stream, c->copy_ev[k], 0));
+    const unsigned nb = (unsigned)((e - b + 255) / 256);
+    if (nb == 0) continue;
+    if (c->precision == SWE_PREC_FP64)
+      k_scatter_in<<<nb, 256, 0, c->stream>>>(c->d_stage + (size_t)c->S * b, c->d_row_of_node + b, e - b, c->S, c->A);
+    else
+      k_scatter_in_mix<<<nb, 256, 0, c->stream>>>(c->d_stage + (size_t)c->S * b, c->d_row_of_node + b, e - b, c->S,
+                                                   c->mA, c->G.slice_inst, c->d_C, c->G.bathf);
+    CK(cudaGetLastError());
+  }
   return SWE_OK;
 }
 
@@ -345,14 +384,31 @@ static int from_device_state(swe_ctx* c, double* un, bool device_dst, int64_t no
                              const StateF64* sf, const StateMix* sm, bool low_mix = false) {
   const int64_t nn = node_end - node_begin;
   if (nn <= 0) return SWE_OK;
-  const unsigned nb = (unsigned)((nn + 255) / 256);
-  double* stg = c->d_stage + (size_t)c->S * node_begin;
-  if (sf) k_gather_out<<<nb, 256, 0, c->stream>>>(stg, c->d_row_of_node + node_begin, nn, c->S, *sf);
-  else k_gather_out_mix<<<nb, 256, 0, c->stream>>>(stg, c->d_row_of_node + node_begin, nn, c->S,
-                                                    sm ? *sm : c->mA, c->wm, low_mix ? 1 : 0);
-  CK(cudaGetLastError());
-  CK(cudaMemcpyAsync(un, stg, (size_t)c->S * nn * sizeof(double),
-                     device_dst ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream));
+  int rc = copy_setup(c);
+  if (rc) return rc;
+  const int K = nn >= 1024 ? c->copy_chunks : 1;
+  // chunk k: gathered into reference order on `stream`, then copied out on
+  // copy_stream[k] while the next chunk is gathered; `stream` waits for every
+  // copy, so the caller's synchronisation on it covers the transfer
+  for (int k = 0; k < K; k++) {
+    const int64_t b = chunk_at(node_begin, node_end, k, K), e = chunk_at(node_begin, node_end, k + 1, K);
+    const unsigned nb = (unsigned)((e - b + 255) / 256);
+    double* stg = c->d_stage + (size_t)c->S * b;
+    if (nb) {
+      if (sf) k_gather_out<<<nb, 256, 0, c->stream>>>(stg, c->d_row_of_node + b, e - b, c->S, *sf);
+      else k_gather_out_mix<<<nb, 256, 0, c->stream>>>(stg, c->d_row_of_node + b, e - b, c->S, sm ? *sm : c->mA,
+                                                        c->wm, low_mix ? 1 : 0);
+      CK(cudaGetLastError());
+    }
+    CK(cudaEventRecord(c->copy_ev[k], c->stream));
+    CK(cudaStreamWaitEvent(c->copy_stream[k], c->copy_ev[k], 0));
+    CK(cudaMemcpyAsync(un + (size_t)c->S * (b - node_begin), stg, (size_t)c->S * (e - b) * sizeof(double),
+                       device_dst ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->copy_stream[k]));
+  }
+  for (int k = 0; k < K; k++) {
+    CK(cudaEventRecord(c->copy_ev[k], c->copy_stream[k]));
+    CK(cudaStreamWaitEvent(c->stream, c->copy_ev[k], 0));
+  }
   return SWE_OK;
 }
 
@@ -435,18 +491,32 @@ static void enqueue_step(swe_ctx* c, const KernelEvents* kev = nullptr, double* 
   launch_step_end(c->d_St, c->n_inst, s);
 }
 
-static int build_graph(swe_ctx* c, int steps) {
-  if (c->gexec && c->graph_steps == steps) return SWE_OK;
-  if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
+static int capture_steps(swe_ctx* c, int steps, cudaGraphExec_t* exec) {
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   for (int k = 0; k < steps; k++) enqueue_step(c);
   CK(cudaStreamEndCapture(c->stream, &g));
-  cudaError_t e = cudaGraphInstantiate(&c->gexec, g, 0);
+  cudaError_t e = cudaGraphInstantiate(exec, g, 0);
   cudaGraphDestroy(g);
   CK(e);
+  return SWE_OK;
+}
+
+static int build_graph(swe_ctx* c, int steps) {
+  if (c->gexec && c->graph_steps == steps) return SWE_OK;
+  if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
+  int rc = capture_steps(c, steps, &c->gexec);
+  if (rc) return rc;
   c->graph_steps = steps;
   return SWE_OK;
+}
+
+// Captured steps depend on the launch configuration; drop them when it
+// changes (parameter, bathymetry and Dirichlet updates rewrite device arrays
+// in place and keep them valid).
+static void drop_graphs(swe_ctx* c) {
+  if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; c->graph_steps = 0; }
+  if (c->gexec1) { cudaGraphExecDestroy(c->gexec1); c->gexec1 = nullptr; }
 }
 
 // ============================== C ABI ======================================
@@ -512,10 +582,16 @@ SWE_API int swe_create_batch(swe_ctx** ctx, int n_inst, const int* np, const int
 
 SWE_API void swe_destroy(swe_ctx* c) {
   if (!c) return;
-  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  drop_graphs(c);
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->t0) cudaEventDestroy(c->t0);
   if (c->t1) cudaEventDestroy(c->t1);
+  for (int k = 0; k < c->copy_chunks; k++) {
+    cudaStreamSynchronize(c->copy_stream[k]);
+    cudaStreamDestroy(c->copy_stream[k]);
+    cudaEventDestroy(c->copy_ev[k]);
+  }
+  if (c->copy_go) cudaEventDestroy(c->copy_go);
   c->buf.release();
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -936,7 +1012,7 @@ static int autotune(swe_ctx* c) {
     c->tune = t;
     c->tuned = true;
     c->tuning = std::string("thread-per-row SELL-32; fixed ") + spec;
-    if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; c->graph_steps = 0; }
+    drop_graphs(c);
     return SWE_OK;
   }
   int rc;
@@ -1016,7 +1092,7 @@ static int autotune(swe_ctx* c) {
   c->tune = t;
   c->tuned = true;
   c->tuning = "thread-per-row SELL-32; autotuned " + desc;
-  if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; c->graph_steps = 0; }
+  drop_graphs(c);
   return SWE_OK;
 }
 
@@ -1033,10 +1109,7 @@ SWE_API int swe_rk3_steps(swe_ctx* c, int nsteps, double* time_out, double* dt_o
     if (env && env[0] == '0') c->tuned = true;
     else if ((rc = autotune(c))) return rc;
   }
-  std::vector<InstState> hs;
-  if ((rc = save_state(c, hs))) return rc;
-  for (auto& s : hs) { s.steps = 0; s.maxd_bits = 0ull; }
-  if ((rc = restore_done(c, hs))) return rc;
+  launch_reset_counters(c->d_St, c->n_inst, c->stream);
   const int chunk = nsteps >= 8 ? 8 : 1;
   long long launches = 0;
   if (!c->t0) { CK(cudaEventCreate(&c->t0)); CK(cudaEventCreate(&c->t1)); }
@@ -1051,18 +1124,19 @@ SWE_API int swe_rk3_steps(swe_ctx* c, int nsteps, double* time_out, double* dt_o
     }
   }
   const int rem = chunk > 1 ? nsteps % chunk : nsteps;
+  if (rem && !c->gexec1 && (rc = capture_steps(c, 1, &c->gexec1))) return rc;
   for (int k = 0; k < rem; k++) {
-    enqueue_step(c);
+    CK(cudaGraphLaunch(c->gexec1, c->stream));
     launches += per_step;
   }
   CK(cudaEventRecord(c->t1, c->stream));
   CK(cudaGetLastError());
   c->last_launches = launches;
   c->euler_done = false;
+  // the instances' state and the error word in one synchronisation
+  std::vector<InstState> out(c->n_inst);
+  CK(cudaMemcpyAsync(out.data(), c->d_St, sizeof(InstState) * c->n_inst, cudaMemcpyDeviceToHost, c->stream));
   rc = read_errors(c);
-  std::vector<InstState> out;
-  int rc2 = save_state(c, out);
-  if (rc2) return rc2;
   for (int b = 0; b < c->n_inst; b++) {
     if (time_out) time_out[b] = out[b].time;
     if (dt_out) dt_out[b] = out[b].dt;

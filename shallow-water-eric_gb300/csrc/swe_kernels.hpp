@@ -94,6 +94,7 @@ void launch_dt_f64(const Graph& G, const InstConst* C, InstState* St, const Stat
                    double* dii_out, unsigned* err, int block, cudaStream_t s);
 void launch_step_begin(const InstConst* C, InstState* St, int n_inst, cudaStream_t s);
 void launch_step_end(InstState* St, int n_inst, cudaStream_t s);
+void launch_reset_counters(InstState* St, int n_inst, cudaStream_t s);
 void launch_fct_positivity_f64(const Graph& G, const InstConst* C, const double* unext, const double* mat,
                                const double* matii, double* rtmp, double* lij, cudaStream_t s);
 void launch_fct_generic_f64(const Graph& G, double* unext, const double* maxn, const double* minn, const double* dg,

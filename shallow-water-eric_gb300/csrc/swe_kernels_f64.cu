@@ -676,6 +676,15 @@ __global__ void k_step_begin(const InstConst* __restrict__ C, InstState* __restr
   s.maxd_bits = 0ull;
 }
 
+// Start of a swe_rk3_steps call: step counters and the lambda_max maximum
+// restart (the instances' time, dt and done flags carry over)
+__global__ void k_reset_counters(InstState* __restrict__ St, int n_inst) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n_inst) return;
+  St[b].steps = 0;
+  St[b].maxd_bits = 0ull;
+}
+
 // End of a time step: time = to + dt (main.f90:91)
 __global__ void k_step_end(InstState* __restrict__ St, int n_inst) {
   int b = blockIdx.x * blockDim.x + threadIdx.x;
@@ -814,6 +823,9 @@ void launch_step_begin(const InstConst* C, InstState* St, int n_inst, cudaStream
 
 void launch_step_end(InstState* St, int n_inst, cudaStream_t s) {
   k_step_end<<<nblk(n_inst, 128), 128, 0, s>>>(St, n_inst);
+}
+void launch_reset_counters(InstState* St, int n_inst, cudaStream_t s) {
+  k_reset_counters<<<nblk(n_inst, 128), 128, 0, s>>>(St, n_inst);
 }
 
 void launch_fct_positivity_f64(const Graph& G, const InstConst* C, const double* unext, const double* mat,
