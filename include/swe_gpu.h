@@ -232,6 +232,34 @@ const char* swe_tuning(const swe_ctx* ctx);
 int swe_fct_positivity_noalloc(int np, const int* d_ia, const int* d_ja, const double* d_unext,
                                const double* d_mat, double htiny, double* d_lij, void* stream);
 
+/* ---- movie frames and VTK output (the frame block of the time loop,
+ * SOURCES/main.f90:119-143, and vtk_2d, SFEMaNS/FEMSUB/sub_plot.f90:1036-1095)
+ *
+ * swe_write_vtk_2d writes one P1 scalar field as the legacy-VTK text that
+ * vtk_2d writes, byte for byte (P1 branch): title is the file name vtk_2d
+ * puts on its second line, jj (3, me) is 1-based like mesh%jj, rr (2, np)
+ * like mesh%rr.  Host only; SWE_ERR_ARG if the file cannot be written.
+ *
+ * swe_frame_fields computes on the device the two fields of a movie frame
+ * from the current state of instance inst, in the reference node order:
+ *   hpz = h + bath, or -1e-7 hmax0 + bath where h <= 1e-4 hmax0  (hpz_k.vtk)
+ *   h   = h,        or 0                  where h <= 1e-4 hmax0  (h_k.vtk)
+ * with hmax0 = MAXVAL of the initial depth (main.f90:32), and copies them to
+ * the host arrays (np doubles each).
+ *
+ * swe_frame_async does the same into one of two page-locked buffers and
+ * returns at once; a worker thread writes hpz_path and h_path with
+ * swe_write_vtk_2d while the caller keeps stepping (at most two frames in
+ * flight: a third call waits for a free buffer).  The title line carries
+ * the file's name blank-padded to 200 characters, as main.f90 passes its
+ * CHARACTER(LEN=200) header to vtk_2d.  swe_frames_wait returns
+ * once every queued frame is on disk, with the first write error if any. */
+int swe_write_vtk_2d(const char* path, const char* title, int np, int me, const int* jj, const double* rr,
+                     const double* field);
+int swe_frame_fields(swe_ctx* ctx, int inst, double hmax0, double* hpz, double* h);
+int swe_frame_async(swe_ctx* ctx, int inst, double hmax0, const char* hpz_path, const char* h_path);
+int swe_frames_wait(swe_ctx* ctx);
+
 #ifdef __cplusplus
 }
 #endif

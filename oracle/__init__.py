@@ -223,3 +223,49 @@ class Oracle:
     @property
     def last_dt(self):
         return lib().orc_last_dt(self.h)
+
+
+def frame_fields(h, bath, hmax0):
+    """Movie-frame fields of the time loop (SOURCES/main.f90:125-143):
+    hpz = h + bath, or -1e-7 hmax0 + bath where h <= 1e-4 hmax0 (hpz_k.vtk);
+    h, or 0 there (h_k.vtk).  Each product and sum is one FP64 rounding."""
+    h = np.asarray(h, np.float64)
+    bath = np.asarray(bath, np.float64)
+    dry = h <= 1.e-4 * hmax0
+    hpz = np.where(dry, (-1.e-7 * hmax0) + bath, h + bath)
+    return hpz, np.where(dry, 0.0, h)
+
+
+def fortran_e13_7(x):
+    """Fortran E13.7 edit descriptor as gfortran writes it (the number format
+    of vtk_2d, SFEMaNS/FEMSUB/sub_plot.f90:1059,1093): 0.dddddddE+xx,
+    -.dddddddE+xx when negative (no room for the leading zero)."""
+    import math
+    if math.isnan(x):
+        return "NaN".rjust(13)
+    if math.isinf(x):
+        return ("Infinity" if x > 0 else "-Infinity").rjust(13)
+    neg = math.copysign(1.0, x) < 0
+    if x == 0:
+        digits, e = "0000000", 0
+    else:
+        m, ex = f"{abs(x):.6E}".split("E")
+        digits, e = m.replace(".", ""), int(ex) + 1
+    exp = f"E{'-' if e < 0 else '+'}{abs(e):02d}" if abs(e) <= 99 else f"{'-' if e < 0 else '+'}{abs(e):03d}"
+    return ("-." if neg else "0.") + digits + exp
+
+
+def vtk_2d_text(title, jj, rr, field):
+    """The text vtk_2d writes (SFEMaNS/FEMSUB/sub_plot.f90:1036-1095, P1
+    branch) for a mesh jj (3, me) 1-based, rr (2, np) and a P1 field."""
+    np_, me = rr.shape[1], jj.shape[1]
+    out = ["# vtk DataFile Version 3.0", f"vtk {title}", "ASCII", "DATASET UNSTRUCTURED_GRID",
+           f"POINTS {np_:7d} float"]
+    out += [f"{fortran_e13_7(rr[0, i])}  {fortran_e13_7(rr[1, i])}   0.0 " for i in range(np_)]
+    out.append(f"CELLS {me:7d}{4 * me:8d}")
+    out += [f"3 {jj[0, k] - 1:8d} {jj[1, k] - 1:8d} {jj[2, k] - 1:8d}" for k in range(me)]
+    out.append(f"CELL_TYPES {me:7d}")
+    out += ["5"] * me
+    out += [f"POINT_DATA {np_:7d}", "SCALARS scalars float 1", "LOOKUP_TABLE default"]
+    out += [fortran_e13_7(v) for v in field]
+    return "\n".join(out) + "\n"

@@ -7,8 +7,12 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <condition_variable>
 #include <cstring>
+#include <deque>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/swe_gpu.h"
@@ -80,6 +84,25 @@ struct swe_ctx {
   cudaGraphExec_t gexec = nullptr;
   int graph_steps = 0;
   cudaGraphExec_t gexec1 = nullptr;      // one time step (the remainder of a call)
+  // movie frames (swe_frame_async): device fields and page-locked host copies
+  // in two slots, written to files by a worker thread
+  struct FrameJob {
+    int slot, inst;
+    std::string paths[2];
+  };
+  double* d_frame = nullptr;             // 2 slots x (hpz, h) x frame_np
+  double* h_frame = nullptr;             // same, page-locked
+  int64_t frame_np = 0;
+  cudaEvent_t frame_ev[2] = {};
+  bool frame_busy[2] = {false, false};
+  std::vector<std::vector<int>> jj1;     // 1-based element lists per instance (writer input)
+  std::deque<FrameJob> frame_queue;
+  std::thread frame_worker;
+  std::mutex frame_mu;
+  std::condition_variable frame_cv;
+  bool frame_stop = false;
+  int frame_err = 0;
+  std::string frame_errmsg;
   int block = 128;
   KernelTune tune;
   bool tuned = false;
@@ -412,6 +435,28 @@ static int from_device_state(swe_ctx* c, double* un, bool device_dst, int64_t no
   return SWE_OK;
 }
 
+// Movie frame fields of the time loop (main.f90:125-143) in reference node
+// order: hpz = h + z, or -1e-7 hmax0 + z where h <= 1e-4 hmax0; h, or 0
+// there.  Explicit roundings: the reference forms each product and sum once.
+__global__ void k_frame_fields(const int* __restrict__ row_of_node, int64_t n_nodes, int fp64, StateF64 a,
+                               StateMix m, const double* __restrict__ bath, double hmax0, double* __restrict__ hpz,
+                               double* __restrict__ hout) {
+  const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (n >= n_nodes) return;
+  const int64_t r = row_of_node[n];
+  const double h = fp64 ? a.h[r] : df_to_double(m.h[r]);
+  const double z = bath[r];
+  if (h <= __dmul_rn(1.e-4, hmax0)) {
+    hpz[n] = __dadd_rn(__dmul_rn(-1.e-7, hmax0), z);
+    hout[n] = 0.0;
+  } else {
+    hpz[n] = __dadd_rn(h, z);
+    hout[n] = h;
+  }
+}
+
+static int frames_wait(swe_ctx* c);
+
 static int read_errors(swe_ctx* c) {
   unsigned e = 0;
   CK(cudaMemcpyAsync(&e, c->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
@@ -582,6 +627,18 @@ SWE_API int swe_create_batch(swe_ctx** ctx, int n_inst, const int* np, const int
 
 SWE_API void swe_destroy(swe_ctx* c) {
   if (!c) return;
+  if (c->d_frame) {                                   // finish the frames in flight, stop the writer
+    frames_wait(c);
+    {
+      std::lock_guard<std::mutex> lk(c->frame_mu);
+      c->frame_stop = true;
+      c->frame_cv.notify_all();
+    }
+    if (c->frame_worker.joinable()) c->frame_worker.join();
+    for (int k = 0; k < 2; k++) if (c->frame_ev[k]) cudaEventDestroy(c->frame_ev[k]);
+    cudaFreeHost(c->h_frame);
+    cudaFree(c->d_frame);
+  }
   drop_graphs(c);
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->t0) cudaEventDestroy(c->t0);
@@ -1099,6 +1156,131 @@ static int autotune(swe_ctx* c) {
 SWE_API int swe_autotune(swe_ctx* c) {
   if (!c) return SWE_ERR_ARG;
   return autotune(c);
+}
+
+// ---- movie frames (main.f90:119-143, sub_plot.f90:1036-1095) ----
+static int frame_setup(swe_ctx* c) {
+  if (c->d_frame) return SWE_OK;
+  int64_t npmax = 0;
+  for (const HostMesh& m : c->meshes) npmax = std::max<int64_t>(npmax, m.np);
+  CK(cudaMalloc(&c->d_frame, sizeof(double) * 4 * npmax));
+  CK(cudaMallocHost(&c->h_frame, sizeof(double) * 4 * npmax));
+  for (int k = 0; k < 2; k++) CK(cudaEventCreateWithFlags(&c->frame_ev[k], cudaEventDisableTiming));
+  c->frame_np = npmax;
+  c->jj1.resize(c->n_inst);
+  for (int b = 0; b < c->n_inst; b++) {
+    c->jj1[b] = c->meshes[b].jj;
+    for (int& v : c->jj1[b]) v += 1;
+  }
+  const int dev = c->dev;
+  c->frame_worker = std::thread([c, dev]() {
+    cudaSetDevice(dev);
+    for (;;) {
+      swe_ctx::FrameJob job;
+      {
+        std::unique_lock<std::mutex> lk(c->frame_mu);
+        c->frame_cv.wait(lk, [c] { return c->frame_stop || !c->frame_queue.empty(); });
+        if (c->frame_queue.empty()) return;
+        job = c->frame_queue.front();
+      }
+      const cudaError_t e = cudaEventSynchronize(c->frame_ev[job.slot]);
+      int rc = e == cudaSuccess ? SWE_OK : SWE_ERR_CUDA;
+      const HostMesh& m = c->meshes[job.inst];
+      const double* f = c->h_frame + (size_t)job.slot * 2 * c->frame_np;
+      for (int k = 0; k < 2 && rc == SWE_OK; k++) {
+        const std::string& path = job.paths[k];
+        // title: the file's name in main.f90's CHARACTER(LEN=200) header, blank-padded
+        const size_t cut = path.find_last_of('/');
+        std::string title = cut == std::string::npos ? path : path.substr(cut + 1);
+        if (title.size() < 200) title.resize(200, ' ');
+        rc = swe_write_vtk_2d(path.c_str(), title.c_str(), m.np, m.me, c->jj1[job.inst].data(), m.rr.data(),
+                              f + (size_t)k * c->frame_np);
+      }
+      std::lock_guard<std::mutex> lk(c->frame_mu);
+      if (rc && !c->frame_err) {
+        c->frame_err = rc;
+        c->frame_errmsg = rc == SWE_ERR_CUDA ? std::string("frame copy: ") + cudaGetErrorString(e)
+                                             : "cannot write " + job.paths[0] + " or " + job.paths[1];
+      }
+      c->frame_busy[job.slot] = false;
+      c->frame_queue.pop_front();
+      c->frame_cv.notify_all();
+    }
+  });
+  return SWE_OK;
+}
+
+// Fields of slot k computed on the stream and copied to its page-locked
+// buffer on a copy stream (event frame_ev[k] marks the copy's end).
+static int frame_enqueue(swe_ctx* c, int inst, double hmax0, int k) {
+  const int64_t n0 = c->node_off[inst], nn = c->node_off[inst + 1] - n0;
+  double* d = c->d_frame + (size_t)k * 2 * c->frame_np;
+  double* h = c->h_frame + (size_t)k * 2 * c->frame_np;
+  k_frame_fields<<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(
+      c->d_row_of_node + n0, nn, c->precision == SWE_PREC_FP64 ? 1 : 0, c->A, c->mA, c->G.bath, hmax0, d,
+      d + c->frame_np);
+  CK(cudaGetLastError());
+  int rc = copy_setup(c);
+  if (rc) return rc;
+  CK(cudaEventRecord(c->frame_ev[k], c->stream));
+  CK(cudaStreamWaitEvent(c->copy_stream[0], c->frame_ev[k], 0));
+  CK(cudaMemcpyAsync(h, d, sizeof(double) * nn, cudaMemcpyDeviceToHost, c->copy_stream[0]));
+  CK(cudaMemcpyAsync(h + c->frame_np, d + c->frame_np, sizeof(double) * nn, cudaMemcpyDeviceToHost,
+                     c->copy_stream[0]));
+  CK(cudaEventRecord(c->frame_ev[k], c->copy_stream[0]));
+  return SWE_OK;
+}
+
+static int frames_wait(swe_ctx* c) {
+  if (!c->d_frame) return SWE_OK;
+  std::unique_lock<std::mutex> lk(c->frame_mu);
+  c->frame_cv.wait(lk, [c] { return c->frame_queue.empty(); });
+  if (c->frame_err) {
+    const int rc = c->frame_err;
+    c->frame_err = 0;
+    return fail(c, rc, c->frame_errmsg);
+  }
+  return SWE_OK;
+}
+
+SWE_API int swe_frame_fields(swe_ctx* c, int inst, double hmax0, double* hpz, double* h) {
+  if (!c || inst < 0 || inst >= c->n_inst || !hpz || !h) return fail(c, SWE_ERR_ARG, "bad arguments");
+  int rc = frame_setup(c);
+  if (rc) return rc;
+  if ((rc = frames_wait(c))) return rc;              // both slots free
+  if ((rc = frame_enqueue(c, inst, hmax0, 0))) return rc;
+  CK(cudaEventSynchronize(c->frame_ev[0]));
+  const int64_t nn = c->node_off[inst + 1] - c->node_off[inst];
+  std::memcpy(hpz, c->h_frame, sizeof(double) * nn);
+  std::memcpy(h, c->h_frame + c->frame_np, sizeof(double) * nn);
+  return SWE_OK;
+}
+
+SWE_API int swe_frame_async(swe_ctx* c, int inst, double hmax0, const char* hpz_path, const char* h_path) {
+  if (!c || inst < 0 || inst >= c->n_inst || !hpz_path || !h_path) return fail(c, SWE_ERR_ARG, "bad arguments");
+  int rc = frame_setup(c);
+  if (rc) return rc;
+  int k;
+  {
+    std::unique_lock<std::mutex> lk(c->frame_mu);    // a free slot (at most two frames in flight)
+    c->frame_cv.wait(lk, [c] { return !c->frame_busy[0] || !c->frame_busy[1]; });
+    k = c->frame_busy[0] ? 1 : 0;
+    c->frame_busy[k] = true;
+  }
+  if ((rc = frame_enqueue(c, inst, hmax0, k))) {
+    std::lock_guard<std::mutex> lk(c->frame_mu);
+    c->frame_busy[k] = false;
+    return rc;
+  }
+  std::lock_guard<std::mutex> lk(c->frame_mu);
+  c->frame_queue.push_back(swe_ctx::FrameJob{k, inst, {hpz_path, h_path}});
+  c->frame_cv.notify_all();
+  return SWE_OK;
+}
+
+SWE_API int swe_frames_wait(swe_ctx* c) {
+  if (!c) return SWE_ERR_ARG;
+  return frames_wait(c);
 }
 
 SWE_API int swe_rk3_steps(swe_ctx* c, int nsteps, double* time_out, double* dt_out, int* steps_done) {

@@ -32,6 +32,7 @@ UNITS = {
     "swe_setup_gpu.cu": ["-fmad=false"],
     "swe_diag.cu": ["-fmad=false"],
     "swe_setup.cpp": None,   # host C++
+    "swe_io.cpp": None,      # host C++
 }
 
 

@@ -167,6 +167,25 @@ class Update:
                                       ctypes.byref(l1), ctypes.byref(l2)))
         return l1.value, l2.value
 
+    # ---- movie frames (main.f90:119-143) -------------------------------------
+    def frame_fields(self, hmax0, inst=0):
+        """(hpz, h) of a movie frame from the device state: h + bath and h,
+        with -1e-7 hmax0 + bath and 0 where h <= 1e-4 hmax0."""
+        n = int(self.node_off[inst + 1] - self.node_off[inst])
+        hpz = np.zeros(n); h = np.zeros(n)
+        self._check(self._L.swe_frame_fields(self.h, inst, float(hmax0), _L.dp(hpz), _L.dp(h)))
+        return hpz, h
+
+    def frame_async(self, hpz_path, h_path, hmax0, inst=0):
+        """Queue a movie frame: its fields are computed and copied on the
+        GPU now and written as VTK files by a worker thread (hpz_k.vtk,
+        h_k.vtk of the reference's time loop)."""
+        self._check(self._L.swe_frame_async(self.h, inst, float(hmax0), str(hpz_path).encode(),
+                                            str(h_path).encode()))
+
+    def frames_wait(self):
+        self._check(self._L.swe_frames_wait(self.h))
+
     # ---- device-resident time loop ----------------------------------------
     def upload(self, un):
         """un: (S, sum np) concatenation of the instances' states, or a list."""
@@ -246,3 +265,20 @@ def from_case(case, precision=None):
     for comp, js, vals in case.dirichlet:
         upd.set_dirichlet(comp, js, vals)
     return upd
+
+
+def write_vtk_2d(path, jj, rr, field, title=None):
+    """vtk_2d (SFEMaNS/FEMSUB/sub_plot.f90:1036-1095): one P1 scalar field as
+    legacy-VTK text, byte for byte the reference's.  jj (3, me) 1-based,
+    rr (2, np); title defaults to the file's name."""
+    from pathlib import Path
+    L = _L.load()
+    jj = np.asfortranarray(jj, np.int32)
+    rr = np.asfortranarray(rr, np.float64)
+    f = np.ascontiguousarray(field, np.float64)
+    if rr.shape[1] != f.size or jj.shape[0] != 3:
+        raise ValueError("rr (2, np), jj (3, me) and a field of np values are required")
+    rc = L.swe_write_vtk_2d(str(path).encode(), (title or Path(path).name).encode(), rr.shape[1], jj.shape[1],
+                            _L.ip(jj.ravel(order="F")), _L.dp(rr.ravel(order="F")), _L.dp(f))
+    if rc:
+        raise _L.SweError(rc, f"cannot write {path}")

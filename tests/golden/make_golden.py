@@ -12,6 +12,9 @@ Fixtures written (all small, numpy .npz):
                                written by an older revision without +htiny).
   pin_lis.npz                  it_max and relative L1 errors recorded in
                                PARABOLOID/lis_{h}_type2_lim (older revision).
+  ref_{bath,h_1,hpz_1}.vtk.gz  SOURCES/BACKUP/*.vtk, the reference's own vtk_2d
+                               output on cav_0.2 (gzip of the files as shipped):
+                               pins the VTK text byte for byte.
   oracle_*.npz                 FP64 oracle trajectories (regression vectors
                                for the oracle itself and GPU parity vectors).
 """
@@ -63,6 +66,12 @@ def main():
         l1.append(float(re.findall(r"[-+0-9.E]+", txt[3])[-1]))
     np.savez(HERE / "pin_lis.npz", h=np.array([0.2, 0.1, 0.05, 0.025, 0.0125]), it_max=np.array(it_max),
              l1=np.array(l1), cfl=0.3)
+
+    import gzip
+    for name in ("bath", "h_1", "hpz_1"):
+        data = (REF / "SOURCES/BACKUP" / f"{name}.vtk").read_bytes()
+        with gzip.GzipFile(HERE / f"ref_{name}.vtk.gz", "wb", mtime=0) as f:
+            f.write(data)
 
     # oracle trajectories
     m = dict(np.load(HERE / "mesh_cav_0.2.npz"))

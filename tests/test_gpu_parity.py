@@ -555,3 +555,50 @@ def test_fixed_tuning_reproduces_autotuned_variants(monkeypatch):
     with pytest.raises(L.SweError, match="SWE_TUNE"):
         upd.rk3_steps(1)
     upd.close()
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_frame_fields_match_oracle(golden, prec):
+    """Movie-frame fields computed on the device (main.f90:125-143) equal the
+    oracle's restatement on the downloaded state, bit for bit, with wet and
+    dry nodes on both sides of 1e-4 hmax0."""
+    case = _thacker(golden, "0.1", periods=1.0, cfl=0.3)
+    upd = from_case(case, precision=prec)
+    upd.upload(case.u0)
+    upd.set_time(0.0, 1e30)
+    upd.rk3_steps(12)
+    hmax0 = float(case.u0[0].max())
+    hpz, h = upd.frame_fields(hmax0)
+    u = upd.download()
+    e_hpz, e_h = oracle.frame_fields(u[0], case.bath, hmax0)
+    dry = u[0] <= 1e-4 * hmax0
+    assert dry.any() and (~dry).any()
+    np.testing.assert_array_equal(hpz, e_hpz)
+    np.testing.assert_array_equal(h, e_h)
+    upd.close()
+
+
+def test_async_frames_write_the_reference_text(golden, tmp_path):
+    """Frames queued with swe_frame_async between steps (three in a row, so
+    one waits for a free buffer) are written by the worker thread as the
+    text vtk_2d writes for the state at the time of the call."""
+    case = _thacker(golden, "0.1", periods=1.0, cfl=0.3)
+    upd = from_case(case, precision=1)
+    upd.upload(case.u0)
+    upd.set_time(0.0, 1e30)
+    hmax0 = float(case.u0[0].max())
+    expect = {}
+    for k in range(1, 4):
+        upd.rk3_steps(3)
+        paths = (tmp_path / f"hpz_{k}.vtk", tmp_path / f"h_{k}.vtk")
+        upd.frame_async(paths[0], paths[1], hmax0)
+        fields = oracle.frame_fields(upd.download()[0], case.bath, hmax0)
+        for p, f in zip(paths, fields):
+            expect[p] = oracle.vtk_2d_text(p.name.ljust(200), case.mesh["jj"], case.mesh["rr"], f)
+    upd.frames_wait()
+    for p, text in expect.items():
+        assert p.read_text() == text, p.name
+    upd.frame_async(tmp_path / "missing" / "a.vtk", tmp_path / "missing" / "b.vtk", hmax0)
+    with pytest.raises(L.SweError, match="cannot write"):
+        upd.frames_wait()
+    upd.close()
