@@ -561,8 +561,9 @@ def test_fixed_tuning_reproduces_autotuned_variants(monkeypatch):
 def test_frame_fields_match_oracle(golden, prec):
     """Movie-frame fields computed on the device (main.f90:125-143) equal the
     oracle's restatement on the downloaded state, bit for bit, with wet and
-    dry nodes on both sides of 1e-4 hmax0."""
-    case = _thacker(golden, "0.1", periods=1.0, cfl=0.3)
+    dry nodes on both sides of 1e-4 hmax0 (the Thacker case without the
+    htiny film, whose dry box holds h = 0)."""
+    case = _thacker(golden, "0.1", periods=1.0, cfl=0.3, film=False)
     upd = from_case(case, precision=prec)
     upd.upload(case.u0)
     upd.set_time(0.0, 1e30)
@@ -582,7 +583,7 @@ def test_async_frames_write_the_reference_text(golden, tmp_path):
     """Frames queued with swe_frame_async between steps (three in a row, so
     one waits for a free buffer) are written by the worker thread as the
     text vtk_2d writes for the state at the time of the call."""
-    case = _thacker(golden, "0.1", periods=1.0, cfl=0.3)
+    case = _thacker(golden, "0.1", periods=1.0, cfl=0.3, film=False)
     upd = from_case(case, precision=1)
     upd.upload(case.u0)
     upd.set_time(0.0, 1e30)
