@@ -260,6 +260,23 @@ int swe_frame_fields(swe_ctx* ctx, int inst, double hmax0, double* hpz, double* 
 int swe_frame_async(swe_ctx* ctx, int inst, double hmax0, const char* hpz_path, const char* h_path);
 int swe_frames_wait(swe_ctx* ctx);
 
+/* ---- gauges (the Malpasset gauge block of the time loop,
+ * SOURCES/main.f90:102-117, located as in condlim.f90:273-283)
+ *
+ * swe_gauges_set places n point gauges (rr (2, n), instance inst[g]): each
+ * lies in the first element where the reference's `inside` holds
+ * (SFEMaNS/FEMSUB_OBJET/post_interp.f90:492-524) and carries its
+ * FE_interpolation weights (:206-255); elem_out (optional) gets the 1-based
+ * element numbers.  A gauge in no element -> SWE_ERR_ARG.  From then on every
+ * time step ends with one more kernel, which appends a row per gauge to a
+ * device ring of 4096 steps: (time, SUM(h(jj(:,m)) ff),
+ * SUM((h + bath)(jj(:,m)) ff)); NaN for an instance that did not step.  n = 0
+ * removes the gauges.  swe_gauges_read copies the rows recorded since the
+ * previous read, oldest first, as out(3, n, rows) (at most max_rows); lost
+ * (optional) counts rows overwritten before they were read. */
+int swe_gauges_set(swe_ctx* ctx, int n, const int* inst, const double* rr, int* elem_out);
+int swe_gauges_read(swe_ctx* ctx, int max_rows, double* out, int* rows, long long* lost);
+
 #ifdef __cplusplus
 }
 #endif

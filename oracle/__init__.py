@@ -269,3 +269,52 @@ def vtk_2d_text(title, jj, rr, field):
     out += [f"POINT_DATA {np_:7d}", "SCALARS scalars float 1", "LOOKUP_TABLE default"]
     out += [fortran_e13_7(v) for v in field]
     return "\n".join(out) + "\n"
+
+
+def _pd_scal(a, b):
+    return a[0] * b[0] + a[1] * b[1]
+
+
+def _pd_vect(y):
+    return (-y[1], y[0])
+
+
+def _sub(a, b):
+    return (a[0] - b[0], a[1] - b[1])
+
+
+def gauge_element(jj, rr, r):
+    """First element (1-based) where inside(mesh, m, r) holds
+    (SFEMaNS/FEMSUB_OBJET/post_interp.f90:492-524, the search of
+    SOURCES/condlim.f90:273-278), or 0.  jj (3, me) 1-based, rr (2, np)."""
+    r = (float(r[0]), float(r[1]))
+    for m in range(jj.shape[1]):
+        p = [(float(rr[0, jj[v, m] - 1]), float(rr[1, jj[v, m] - 1])) for v in range(3)]
+        s1 = _pd_scal(_pd_vect(_sub(p[2], p[1])), _sub(r, p[1]))
+        s2 = _pd_scal(_pd_vect(_sub(p[0], p[2])), _sub(r, p[2]))
+        s3 = _pd_scal(_pd_vect(_sub(p[1], p[0])), _sub(r, p[0]))
+        if not (min(s1, s2, s3) < -1.e-12):
+            return m + 1
+    return 0
+
+
+def gauge_weights(jj, rr, m, r):
+    """FE_interpolation(mesh, m, r) for P1 (post_interp.f90:206-255), m
+    1-based."""
+    r = (float(r[0]), float(r[1]))
+    p = [(float(rr[0, jj[v, m - 1] - 1]), float(rr[1, jj[v, m - 1] - 1])) for v in range(3)]
+    n2, n3 = _pd_vect(_sub(p[0], p[2])), _pd_vect(_sub(p[1], p[0]))
+    x = 1.0 - _pd_scal(n2, _sub(p[1], r)) / _pd_scal(n2, _sub(p[1], p[2]))
+    y = 1.0 - _pd_scal(n3, _sub(p[2], r)) / _pd_scal(n3, _sub(p[2], p[0]))
+    return ((1.0 - x) - y, x, y)
+
+
+def gauge_values(jj, m, ff, h, bath):
+    """The two sums the Malpasset gauges write (SOURCES/main.f90:112-115):
+    SUM(h(jj(:,m)) * ff) and SUM((h + bath)(jj(:,m)) * ff), in order."""
+    nodes = [int(jj[v, m - 1]) - 1 for v in range(3)]
+    sh = se = 0.0
+    for v, n in enumerate(nodes):
+        sh = h[n] * ff[v] if v == 0 else sh + h[n] * ff[v]
+        se = (h[n] + bath[n]) * ff[v] if v == 0 else se + (h[n] + bath[n]) * ff[v]
+    return sh, se

@@ -103,6 +103,17 @@ struct swe_ctx {
   bool frame_stop = false;
   int frame_err = 0;
   std::string frame_errmsg;
+  // gauges (main.f90:102-117): per gauge its instance, the device rows of its
+  // element's three nodes and the P1 weights there; a device ring of
+  // (time, h, h + bath) rows appended by k_gauges at the end of every step
+  int n_gauges = 0;
+  int* d_gauge_inst = nullptr;
+  int* d_gauge_rows = nullptr;           // 3 per gauge
+  double* d_gauge_w = nullptr;           // 3 per gauge
+  double* d_gauge_rec = nullptr;         // kGaugeRing x n_gauges x 3
+  unsigned long long* d_gauge_count = nullptr;
+  unsigned long long gauge_read = 0;     // rows handed to the caller so far
+  static constexpr int kGaugeRing = 4096;
   int block = 128;
   KernelTune tune;
   bool tuned = false;
@@ -435,6 +446,38 @@ static int from_device_state(swe_ctx* c, double* un, bool device_dst, int64_t no
   return SWE_OK;
 }
 
+// Gauges after a step (main.f90:102-117): SUM(h(jj(:,m)) * ff) and
+// SUM((h + bath)(jj(:,m)) * ff) in the reference's order, with the time
+// reached.  One block; the row index is the step count before this step.
+// Gauges of an instance that did not step (done) record NaN.
+__global__ void k_gauges(int n, const int* __restrict__ ginst, const int* __restrict__ grows,
+                         const double* __restrict__ gw, const InstState* __restrict__ St, int fp64, StateF64 a,
+                         StateMix m, const double* __restrict__ bath, double* __restrict__ rec,
+                         unsigned long long* __restrict__ count, int ring) {
+  const unsigned long long k = *count;
+  for (int g = threadIdx.x; g < n; g += blockDim.x) {
+    double* row = rec + ((size_t)(k % (unsigned long long)ring) * n + g) * 3;
+    const InstState& st = St[ginst[g]];
+    if (st.done) {
+      row[0] = row[1] = row[2] = __longlong_as_double(0x7ff8000000000000ll);
+      continue;
+    }
+    double sh = 0.0, se = 0.0;
+    for (int v = 0; v < 3; v++) {
+      const int r = grows[3 * g + v];
+      const double h = fp64 ? a.h[r] : df_to_double(m.h[r]);
+      const double w = gw[3 * g + v];
+      sh = v ? __dadd_rn(sh, __dmul_rn(h, w)) : __dmul_rn(h, w);
+      se = v ? __dadd_rn(se, __dmul_rn(__dadd_rn(h, bath[r]), w)) : __dmul_rn(__dadd_rn(h, bath[r]), w);
+    }
+    row[0] = st.time;
+    row[1] = sh;
+    row[2] = se;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *count = k + 1;
+}
+
 // Movie frame fields of the time loop (main.f90:125-143) in reference node
 // order: hpz = h + z, or -1e-7 hmax0 + z where h <= 1e-4 hmax0; h, or 0
 // there.  Explicit roundings: the reference forms each product and sum once.
@@ -456,6 +499,7 @@ __global__ void k_frame_fields(const int* __restrict__ row_of_node, int64_t n_no
 }
 
 static int frames_wait(swe_ctx* c);
+static void free_gauges(swe_ctx* c);
 
 static int read_errors(swe_ctx* c) {
   unsigned e = 0;
@@ -534,6 +578,10 @@ static void enqueue_step(swe_ctx* c, const KernelEvents* kev = nullptr, double* 
     harvest(1, 4);
   }
   launch_step_end(c->d_St, c->n_inst, s);
+  if (c->n_gauges)
+    k_gauges<<<1, 256, 0, s>>>(c->n_gauges, c->d_gauge_inst, c->d_gauge_rows, c->d_gauge_w, c->d_St,
+                               c->precision == SWE_PREC_FP64 ? 1 : 0, c->A, c->mA, c->G.bath, c->d_gauge_rec,
+                               c->d_gauge_count, swe_ctx::kGaugeRing);
 }
 
 static int capture_steps(swe_ctx* c, int steps, cudaGraphExec_t* exec) {
@@ -627,6 +675,7 @@ SWE_API int swe_create_batch(swe_ctx** ctx, int n_inst, const int* np, const int
 
 SWE_API void swe_destroy(swe_ctx* c) {
   if (!c) return;
+  free_gauges(c);
   if (c->d_frame) {                                   // finish the frames in flight, stop the writer
     frames_wait(c);
     {
@@ -1283,6 +1332,83 @@ SWE_API int swe_frames_wait(swe_ctx* c) {
   return frames_wait(c);
 }
 
+// ---- gauges (main.f90:102-117, condlim.f90:273-283) ----
+static void free_gauges(swe_ctx* c) {
+  cudaFree(c->d_gauge_inst); cudaFree(c->d_gauge_rows); cudaFree(c->d_gauge_w);
+  cudaFree(c->d_gauge_rec); cudaFree(c->d_gauge_count);
+  c->d_gauge_inst = c->d_gauge_rows = nullptr;
+  c->d_gauge_w = c->d_gauge_rec = nullptr;
+  c->d_gauge_count = nullptr;
+  c->n_gauges = 0;
+  c->gauge_read = 0;
+}
+
+SWE_API int swe_gauges_set(swe_ctx* c, int n, const int* inst, const double* rr, int* elem_out) {
+  if (!c || n < 0 || n > 1024 || (n && (!inst || !rr))) return fail(c, SWE_ERR_ARG, "bad arguments");
+  std::vector<int> gi(n), rows(3 * (size_t)n), elems(n);
+  std::vector<double> w(3 * (size_t)n);
+  for (int g = 0; g < n; g++) {
+    if (inst[g] < 0 || inst[g] >= c->n_inst) return fail(c, SWE_ERR_ARG, "bad gauge instance");
+    const HostMesh& m = c->meshes[inst[g]];
+    const int e = gauge_element(m, rr + 2 * (size_t)g);
+    if (e < 0) return fail(c, SWE_ERR_ARG, "gauge " + std::to_string(g) + " lies in no element");
+    gauge_weights(m, e, rr + 2 * (size_t)g, &w[3 * (size_t)g]);
+    gi[g] = inst[g];
+    elems[g] = e + 1;
+    for (int v = 0; v < 3; v++)
+      rows[3 * (size_t)g + v] = c->L.new_of_old[inst[g]][m.jj[3 * (size_t)e + v]];
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  free_gauges(c);
+  drop_graphs(c);                                    // steps now end with k_gauges (or no longer do)
+  if (elem_out) std::copy(elems.begin(), elems.end(), elem_out);
+  if (n == 0) return SWE_OK;
+  // owned by the gauges (freed by free_gauges), not by the context's buffer list
+  auto put = [](auto** d, const auto& v, cudaError_t& e) {
+    if (e != cudaSuccess) return;
+    e = cudaMalloc(d, v.size() * sizeof(v[0]));
+    if (e == cudaSuccess) e = cudaMemcpy(*d, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice);
+  };
+  cudaError_t st = cudaSuccess;
+  put(&c->d_gauge_inst, gi, st);
+  put(&c->d_gauge_rows, rows, st);
+  put(&c->d_gauge_w, w, st);
+  if (st == cudaSuccess) st = cudaMalloc(&c->d_gauge_rec, sizeof(double) * 3 * n * (size_t)swe_ctx::kGaugeRing);
+  if (st == cudaSuccess) st = cudaMalloc(&c->d_gauge_count, sizeof(unsigned long long));
+  if (st == cudaSuccess) st = cudaMemset(c->d_gauge_count, 0, sizeof(unsigned long long));
+  if (st != cudaSuccess) { free_gauges(c); return cuda_check(c, st, "gauges"); }
+  c->n_gauges = n;
+  return SWE_OK;
+}
+
+SWE_API int swe_gauges_read(swe_ctx* c, int max_rows, double* out, int* rows, long long* lost) {
+  if (!c || max_rows < 0 || !rows || (max_rows && !out)) return fail(c, SWE_ERR_ARG, "bad arguments");
+  *rows = 0;
+  if (lost) *lost = 0;
+  if (!c->n_gauges) return SWE_OK;
+  unsigned long long count = 0;
+  CK(cudaMemcpyAsync(&count, c->d_gauge_count, sizeof count, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  const unsigned long long ring = swe_ctx::kGaugeRing;
+  unsigned long long first = c->gauge_read;
+  if (count - first > ring) {                        // overwritten before this read
+    if (lost) *lost = (long long)(count - ring - first);
+    first = count - ring;
+  }
+  const unsigned long long take = std::min<unsigned long long>(count - first, (unsigned long long)max_rows);
+  const size_t row_bytes = sizeof(double) * 3 * c->n_gauges;
+  for (unsigned long long k = 0; k < take;) {         // at most two contiguous pieces of the ring
+    const unsigned long long slot = (first + k) % ring, len = std::min(take - k, ring - slot);
+    CK(cudaMemcpyAsync(out + (size_t)k * 3 * c->n_gauges, c->d_gauge_rec + (size_t)slot * 3 * c->n_gauges,
+                       row_bytes * len, cudaMemcpyDeviceToHost, c->stream));
+    k += len;
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  c->gauge_read = first + take;
+  *rows = (int)take;
+  return SWE_OK;
+}
+
 SWE_API int swe_rk3_steps(swe_ctx* c, int nsteps, double* time_out, double* dt_out, int* steps_done) {
   if (!c || nsteps < 0) return fail(c, SWE_ERR_ARG, "bad arguments");
   int rc;
@@ -1298,7 +1424,8 @@ SWE_API int swe_rk3_steps(swe_ctx* c, int nsteps, double* time_out, double* dt_o
   if (nsteps >= chunk && chunk > 1 && (rc = build_graph(c, chunk))) return rc;
   CK(cudaEventRecord(c->t0, c->stream));
   // the mixed stage 1 takes alpha from k_dt_mix: one k_node launch fewer
-  const long long per_step = 3LL * kLaunchesPerStage + kLaunchesPerStepExtra - (c->precision == SWE_PREC_MIXED ? 1 : 0);
+  const long long per_step = 3LL * kLaunchesPerStage + kLaunchesPerStepExtra -
+                             (c->precision == SWE_PREC_MIXED ? 1 : 0) + (c->n_gauges ? 1 : 0);
   if (nsteps >= chunk && chunk > 1) {
     for (int k = 0; k + chunk <= nsteps; k += chunk) {
       CK(cudaGraphLaunch(c->gexec, c->stream));

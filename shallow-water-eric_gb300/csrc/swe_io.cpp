@@ -11,6 +11,7 @@
 #include <string>
 
 #include "../../include/swe_gpu.h"
+#include "swe_setup.hpp"
 
 #define SWE_API extern "C" __attribute__((visibility("default")))
 
@@ -97,3 +98,45 @@ SWE_API int swe_write_vtk_2d(const char* path, const char* title, int np, int me
   const int closed = std::fclose(f);
   return (wrote == s.size() && closed == 0) ? SWE_OK : SWE_ERR_ARG;
 }
+
+// ---- gauge location (post_interp.f90: pd_scal :133-141, pd_vect :144-153,
+// inside :492-524, FE_interpolation :206-255), FP64 without contraction ----
+namespace {
+struct V2 {
+  double x, y;
+};
+inline V2 node(const swe::HostMesh& m, int e, int v) {
+  const int n = m.jj[3 * (size_t)e + v];
+  return V2{m.rr[2 * (size_t)n], m.rr[2 * (size_t)n + 1]};
+}
+inline V2 sub(V2 a, V2 b) { return V2{a.x - b.x, a.y - b.y}; }
+inline V2 pd_vect(V2 y) { return V2{-y.y, y.x}; }
+inline double pd_scal(V2 a, V2 b) { return a.x * b.x + a.y * b.y; }
+}  // namespace
+
+namespace swe {
+
+int gauge_element(const HostMesh& m, const double* rp) {
+  const V2 r{rp[0], rp[1]};
+  for (int e = 0; e < m.me; e++) {
+    const V2 r1 = node(m, e, 0), r2 = node(m, e, 1), r3 = node(m, e, 2);
+    const double s1 = pd_scal(pd_vect(sub(r3, r2)), sub(r, r2));
+    const double s2 = pd_scal(pd_vect(sub(r1, r3)), sub(r, r3));
+    const double s3 = pd_scal(pd_vect(sub(r2, r1)), sub(r, r1));
+    if (!(std::fmin(std::fmin(s1, s2), s3) < -1.e-12)) return e;
+  }
+  return -1;
+}
+
+void gauge_weights(const HostMesh& m, int e, const double* rp, double* ff) {
+  const V2 r{rp[0], rp[1]};
+  const V2 r1 = node(m, e, 0), r2 = node(m, e, 1), r3 = node(m, e, 2);
+  const V2 n2 = pd_vect(sub(r1, r3)), n3 = pd_vect(sub(r2, r1));
+  const double x = 1.0 - pd_scal(n2, sub(r2, r)) / pd_scal(n2, sub(r2, r3));
+  const double y = 1.0 - pd_scal(n3, sub(r3, r)) / pd_scal(n3, sub(r3, r1));
+  ff[0] = (1.0 - x) - y;
+  ff[1] = x;
+  ff[2] = y;
+}
+
+}  // namespace swe

@@ -19,6 +19,13 @@ struct HostMesh {
   std::vector<int> diag;                 // CSR position of (i, i)
 };
 
+// Gauge location (condlim.f90:273-283): the first element m (0-based) for
+// which inside(mesh, m, r) holds (SFEMaNS/FEMSUB_OBJET/post_interp.f90:
+// 492-524), or -1; and the P1 weights FE_interpolation(mesh, m, r)
+// (post_interp.f90:206-255) of the point in that element.
+int gauge_element(const HostMesh& m, const double* r);
+void gauge_weights(const HostMesh& m, int e, const double* r, double* ff);
+
 // Builds ia/ja/mass/lumped/diag/cx/cy on the current CUDA device
 // (swe_setup_gpu.cu) and copies them into m.  Returns "" or an error message.
 std::string construct_matrices_device(HostMesh& m);

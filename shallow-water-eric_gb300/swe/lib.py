@@ -37,7 +37,8 @@ EXPORTS = [
     "swe_fct_positivity", "swe_fct_generic", "swe_gauss_points", "swe_norms", "swe_upload", "swe_download", "swe_upload_device", "swe_download_device",
     "swe_set_time", "swe_rk3_steps", "swe_mass", "swe_last_launch_count", "swe_tuning",
     "swe_last_device_ms", "swe_profile_kernels", "swe_fct_positivity_noalloc", "swe_autotune",
-    "swe_write_vtk_2d", "swe_frame_fields", "swe_frame_async", "swe_frames_wait",
+    "swe_write_vtk_2d", "swe_frame_fields", "swe_frame_async", "swe_frames_wait", "swe_gauges_set",
+    "swe_gauges_read",
 ]
 NOALLOC_MAX_NODES = 1 << 20   # SWE_NOALLOC_MAX_NODES
 KERNEL_KINDS = ("dt", "node", "low", "fct", "update")
@@ -103,6 +104,8 @@ def load(build: bool = True):
         "swe_frame_fields": ([vp, ctypes.c_int, ctypes.c_double, dp, dp], ctypes.c_int),
         "swe_frame_async": ([vp, ctypes.c_int, ctypes.c_double, ctypes.c_char_p, ctypes.c_char_p], ctypes.c_int),
         "swe_frames_wait": ([vp], ctypes.c_int),
+        "swe_gauges_set": ([vp, ctypes.c_int, ip, dp, ip], ctypes.c_int),
+        "swe_gauges_read": ([vp, ctypes.c_int, dp, ip, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -186,6 +186,29 @@ class Update:
     def frames_wait(self):
         self._check(self._L.swe_frames_wait(self.h))
 
+    # ---- gauges (main.f90:102-117) -------------------------------------------
+    def set_gauges(self, rr, inst=None):
+        """Point gauges at rr (2, n) (instances inst, default 0); returns their
+        1-based elements.  Every later time step records (time, h, h + bath)
+        interpolated at each gauge on the device."""
+        pts = np.asfortranarray(np.asarray(rr, np.float64).reshape(2, -1))
+        n = pts.shape[1]
+        gi = np.zeros(n, np.int32) if inst is None else np.ascontiguousarray(inst, np.int32)
+        elems = np.zeros(n, np.int32)
+        self._check(self._L.swe_gauges_set(self.h, n, _L.ip(gi), _L.dp(pts.ravel(order="F")), _L.ip(elems)))
+        self._n_gauges = n
+        return elems
+
+    def read_gauges(self, max_rows=4096):
+        """Rows recorded since the last read: (times (rows, n), h (rows, n),
+        h + bath (rows, n), lost)."""
+        n = getattr(self, "_n_gauges", 0)
+        out = np.zeros(3 * max(n, 1) * max_rows)
+        rows = ctypes.c_int(); lost = ctypes.c_longlong()
+        self._check(self._L.swe_gauges_read(self.h, max_rows, _L.dp(out), ctypes.byref(rows), ctypes.byref(lost)))
+        a = out[:3 * n * rows.value].reshape(rows.value, n, 3)
+        return a[:, :, 0], a[:, :, 1], a[:, :, 2], lost.value
+
     # ---- device-resident time loop ----------------------------------------
     def upload(self, un):
         """un: (S, sum np) concatenation of the instances' states, or a list."""

@@ -603,3 +603,47 @@ def test_async_frames_write_the_reference_text(golden, tmp_path):
     with pytest.raises(L.SweError, match="cannot write"):
         upd.frames_wait()
     upd.close()
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_gauges_record_every_step(prec):
+    """Gauges (main.f90:102-117) placed as the reference does (first element
+    where `inside` holds, FE_interpolation weights) and recorded on the
+    device after every step, inside the captured step graphs: each row equals
+    the oracle's interpolation of the state downloaded after that step, bit
+    for bit, and the ring keeps the last 4096 steps."""
+    case = C.dam_break_case(n=41)
+    jj, rr = case.mesh["jj"], case.mesh["rr"]
+    rng = np.random.default_rng(3)
+    pts = np.column_stack([rng.uniform(0.05, 0.95, (2, 5)), rr[:, 100], 0.5 * (rr[:, 0] + rr[:, 1])])
+    upd = from_case(case, precision=prec)
+    elems = upd.set_gauges(pts)
+    want = [oracle.gauge_element(jj, rr, pts[:, g]) for g in range(pts.shape[1])]
+    np.testing.assert_array_equal(elems, want)
+    ff = [oracle.gauge_weights(jj, rr, want[g], pts[:, g]) for g in range(pts.shape[1])]
+    upd.upload(case.u0)
+    upd.set_time(0.0, 1e30)
+    times, states = [], []
+    for _ in range(5):
+        t, _, _ = upd.rk3_steps(1)
+        times.append(t[0]); states.append(upd.download()[0])
+    t_rec, h_rec, e_rec, lost = upd.read_gauges()
+    assert h_rec.shape == (5, pts.shape[1]) and lost == 0
+    for k in range(5):
+        assert np.all(t_rec[k] == times[k])
+        for g in range(pts.shape[1]):
+            sh, se = oracle.gauge_values(jj, want[g], ff[g], states[k], case.bath)
+            assert (h_rec[k, g], e_rec[k, g]) == (sh, se), (k, g)
+    upd.rk3_steps(4101)                      # graphs of 8 steps plus single steps
+    t_rec, h_rec, e_rec, lost = upd.read_gauges()
+    assert h_rec.shape[0] == 4096 and lost == 5
+    assert np.all(np.diff(t_rec[:, 0]) > 0)
+    u = upd.download()[0]
+    for g in range(pts.shape[1]):
+        assert (h_rec[-1, g], e_rec[-1, g]) == oracle.gauge_values(jj, want[g], ff[g], u, case.bath)
+    with pytest.raises(L.SweError, match="no element"):
+        upd.set_gauges(np.array([[5.0], [5.0]]))
+    upd.set_gauges(np.zeros((2, 0)))
+    upd.rk3_steps(2)
+    assert upd.read_gauges()[1].shape[0] == 0
+    upd.close()
