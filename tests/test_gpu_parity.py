@@ -260,6 +260,38 @@ def test_batch_equals_single_instances():
         assert np.max(np.abs(got[b] - u) / scale) < 1e-12, b
 
 
+def test_batch_tiled_mixed_equals_single_instances(monkeypatch):
+    """Mixed path with every kernel in its shared-memory tile variant and
+    64-row tiles, so that tiles straddle instances (row offsets are padded to
+    32 only): a batch of three instances against each instance alone.  The
+    two may run other entry batches (FMA contraction), and the dam breaks'
+    shocks amplify that FP32 rounding: relative L1 of h <= 1e-6, every
+    component within 5e-5 of its maximum."""
+    monkeypatch.setenv("SWE_TILED", "1")
+    monkeypatch.setenv("SWE_TILE", "64")
+    cases = C.batch_instances(n_inst=3, nmin=200, nmax=2000, seed=11, precision=1)
+    upd = Update(batch=[(c.mesh, c.bath, c.params) for c in cases])
+    for b, c in enumerate(cases):
+        for comp, js, vals in c.dirichlet:
+            upd.set_dirichlet(comp, js, vals, inst=b)
+    upd.upload([c.u0 for c in cases])
+    upd.set_time(0.0, 1e30)
+    upd.rk3_steps(12)
+    assert "/tiled" in upd.tuning
+    got = upd.download_split()
+    upd.close()
+    for b, c in enumerate(cases):
+        one = from_case(c)
+        one.upload(c.u0)
+        one.set_time(0.0, 1e30)
+        one.rk3_steps(12)
+        ref = one.download()
+        one.close()
+        assert np.sum(np.abs(got[b][0] - ref[0])) <= 1e-6 * np.sum(np.abs(ref[0])), b
+        scale = np.abs(ref).max(axis=1, keepdims=True) + 1e-300
+        assert np.max(np.abs(got[b] - ref) / scale) < 5e-5, b
+
+
 def test_negative_depth_is_reported_not_trapped():
     case = C.dam_break_case(n=11)
     upd = from_case(case)
