@@ -808,6 +808,7 @@ int orc_set_params(void* h, const Params* p) {
   Oracle& o = *static_cast<Oracle*>(h);
   if (p->syst_size != 3 && p->syst_size != 5) return ORC_ERR_ARG;
   o.P = *p;
+  if (o.P.type_test == 9) o.P.htiny = 1.e-3;   // what every euler call sees in the Malpasset loop (main.f90:67-68)
   return ORC_OK;
 }
 
@@ -966,12 +967,16 @@ static void bdy(Oracle& o, double* uu) {
 }
 
 // One pass of the time loop body (SOURCES/main.f90:61-91): COMPUTE_DT (unless
-// fixed_dt > 0), then the three SSP-RK stages with bdy after each.
+// fixed_dt > 0, or the Malpasset case's fixed dt and htiny), then the three
+// SSP-RK stages with bdy after each.
 int orc_rk3_step(void* h, double* un, double* time, double fixed_dt) {
   Oracle& o = *static_cast<Oracle*>(h);
   const size_t NS = (size_t)o.np * o.P.syst_size;
   int rc;
-  if (fixed_dt > 0) o.P.dt = fixed_dt;
+  if (o.P.type_test == 9) {            // Malpasset: htiny = 1e-3, dt = 2.5e-2 (main.f90:67-69)
+    o.P.htiny = 1.e-3;
+    o.P.dt = 2.5e-2;
+  } else if (fixed_dt > 0) o.P.dt = fixed_dt;
   else if ((rc = orc_compute_dij(h, un, nullptr, &o.P.dt))) return rc;
   std::vector<double> uo(un, un + NS), ui(NS);
   if ((rc = orc_euler(h, uo.data(), un, nullptr))) return rc;

@@ -145,6 +145,9 @@ static int cuda_check(swe_ctx* c, cudaError_t e, const char* where) {
 static InstConst make_const(const swe_params& p) {
   InstConst k{};
   k.g = p.gravity; k.htiny = p.htiny; k.cfl = p.cfl; k.mannings = p.mannings; k.lambda_sgn = p.lambda_sgn;
+  // Malpasset (type 9): the time loop sets htiny = 1e-3 before every step
+  // (main.f90:67-68), so every euler call of that case sees it
+  if (p.type_test == 9) k.htiny = 1.e-3;
   k.max_water_h = p.max_water_h;
   k.rescale_floor = 1.e-10 * p.gravity * (p.max_water_h * p.max_water_h);   // update.f90:866
   k.type_test = p.type_test; k.S = p.syst_size; k.visc = p.viscosity_type; k.viscous_type = p.viscous_type;

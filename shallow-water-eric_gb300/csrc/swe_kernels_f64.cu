@@ -664,7 +664,8 @@ __global__ void k_dt_f64(Graph G, const InstConst* __restrict__ C, InstState* __
   }
 }
 
-// Start of a time step: DO WHILE(time < Tfinal) and dt = CFL/max (main.f90:61, 173)
+// Start of a time step: DO WHILE(time < Tfinal) and dt = CFL/max (main.f90:61,
+// 173), or the fixed dt = 2.5e-2 of the Malpasset case (type 9, main.f90:67-69)
 __global__ void k_step_begin(const InstConst* __restrict__ C, InstState* __restrict__ St, int n_inst) {
   int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= n_inst) return;
@@ -672,7 +673,7 @@ __global__ void k_step_begin(const InstConst* __restrict__ C, InstState* __restr
   if (s.done) return;
   if (!(s.time < s.t_final)) { s.done = 1; return; }
   double mx = __longlong_as_double((long long)s.maxd_bits);
-  inst_set_dt(s, C[b].cfl * 1 / mx);
+  inst_set_dt(s, C[b].type_test == 9 ? 2.5e-2 : C[b].cfl * 1 / mx);
   s.maxd_bits = 0ull;
 }
 

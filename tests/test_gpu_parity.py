@@ -679,3 +679,27 @@ def test_gauges_record_every_step(prec):
     upd.rk3_steps(2)
     assert upd.read_gauges()[1].shape[0] == 0
     upd.close()
+
+
+def test_malpasset_time_loop_fixed_dt_and_htiny():
+    """Type 9 (Malpasset) runs the time loop with dt = 2.5e-2 and htiny =
+    1e-3 instead of COMPUTE_DT (main.f90:67-69), with Manning friction; the
+    FP64 path equals the oracle bit for bit.  The reference's Malpasset mesh
+    is missing, so a dam break on a 100 m lattice stands in."""
+    mesh = M.lattice_mesh(21, 21, 0.0, 100.0, 0.0, 100.0)
+    x = mesh["rr"][0]
+    u0 = np.asfortranarray(np.vstack([np.where(x < 50.0, 2.0, 0.5), np.zeros_like(x), np.zeros_like(x)]))
+    p = C.Params(gravity=9.81, cfl=0.25, max_water_h=2.0, htiny=1e-6, mannings=0.03, type_test=9)
+    case = C.Case(name="type9", mesh=mesh, bath=np.zeros_like(x), params=p, u0=u0, dirichlet=[], tfinal=1e30)
+    o = _oracle_for(case)
+    u = u0.copy(order="F")
+    t = 0.0
+    for _ in range(10):
+        t = o.rk3_step(u, t)
+    upd = from_case(case)
+    upd.upload(u0)
+    upd.set_time(0.0, 1e30)
+    tg, dtg, n = upd.rk3_steps(10)
+    assert n == 10 and dtg[0] == 2.5e-2 and tg[0] == pytest.approx(0.25, rel=1e-14)
+    np.testing.assert_array_equal(upd.download(), u)
+    upd.close()
