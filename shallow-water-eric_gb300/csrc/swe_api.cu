@@ -284,6 +284,7 @@ static int build_device(swe_ctx* c, const std::vector<std::vector<double>>& bath
     WorkF64& w = c->w;
     w.ovh = c->buf.alloc<double>(n, st); w.v1 = c->buf.alloc<double>(n, st); w.v2 = c->buf.alloc<double>(n, st);
     w.ent = c->buf.alloc<double>(n, st); w.alpha = c->buf.alloc<double>(n, st);
+    w.sqgh = c->buf.alloc<double>(n, st);
     w.dL = c->buf.alloc<double>(ne, st); w.muL = c->buf.alloc<double>(ne, st); w.fct = c->buf.alloc<double>(ne, st);
     w.dLii = c->buf.alloc<double>(n, st); w.muLii = c->buf.alloc<double>(n, st);
     w.res = c->buf.alloc<double>(n, st); w.rminus = c->buf.alloc<double>(n, st);
@@ -553,21 +554,29 @@ static void enqueue_step(swe_ctx* c, const KernelEvents* kev = nullptr, double* 
       acc[k] += ms;
     }
   };
+  // FP64: k_node's per-node arrays of the step's state serve k_dt (1/h,
+  // sqrt(g |h|)) and stage 1 (which then skips k_node); k_dt keeps every d_ij
+  // (in the f_ij array, free until stage 1's k_fct) for stage 1's k_low
+  if (c->precision == SWE_PREC_FP64) {
+    StageArgs a0{c->G, c->d_C, c->d_St, c->A, c->A, c->B, c->w, 1, nullptr, c->d_err, c->block};
+    if (kev) cudaEventRecord(kev->ev[2], s);
+    launch_node_f64(a0, s);
+    if (kev) cudaEventRecord(kev->ev[3], s);
+  }
   if (kev) cudaEventRecord(kev->ev[0], s);
-  // FP64: k_dt keeps every d_ij (in the f_ij array, free until stage 1's
-  // k_fct) for stage 1's k_low
   if (c->precision == SWE_PREC_FP64)
-    launch_dt_f64(c->G, c->d_C, c->d_St, c->A, c->w.fct, nullptr, c->d_err, c->block, s);
+    launch_dt_f64(c->G, c->d_C, c->d_St, c->A, c->w.fct, nullptr, c->d_err, c->block, s, &c->w);
   else launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->wm.dlam, c->wm.alpha, c->d_err, c->tune,
                    c->tiles_ok ? &c->tiles : nullptr, s);
   if (kev) cudaEventRecord(kev->ev[1], s);
-  harvest(0, 0);
+  harvest(0, 0);                                   // waits for k_dt, the later of the two
+  if (c->precision == SWE_PREC_FP64) harvest(1, 1);
   launch_step_begin(c->d_C, c->d_St, c->n_inst, s);
   for (int stage = 1; stage <= 3; stage++) {
     if (c->precision == SWE_PREC_FP64) {
       StageArgs a{c->G, c->d_C, c->d_St, c->A, c->A, c->B, c->w, stage, nullptr, c->d_err, c->block};
       a.entropy = has_entropy(c);
-      if (stage == 1) a.dij_in = c->w.fct;
+      if (stage == 1) { a.dij_in = c->w.fct; a.skip_node = 1; }
       if (stage == 2) { a.u = c->B; a.out = c->Cs; }
       if (stage == 3) { a.u = c->Cs; a.out = c->A; }
       launch_stage_f64(a, s, kev);

@@ -132,57 +132,80 @@ template <typename T> __device__ __forceinline__ T one_over_h(T h, T htiny) {
   return T(2) * h / (h * h + mh * mh);
 }
 
-// phi (SOURCES/condlim.f90:960-981)
+// Per-call constants of compute_lambda_vacc, formed once per thread with the
+// reference's own expressions (so every use sees the value the reference
+// forms at that point).
 template <typename T>
-__device__ __forceinline__ T phi_fn(T h, T ul, T hl, T ur, T hr, T g, T htiny) {
+struct LamConstF64 {
+  T x0;              // (2 sqrt2 - 1)^2
+  T a, two_a;        // 1/(2 sqrt2), 2 a
+  T sixteen_g;       // 16 g
+  T two_sqrt_g;      // 2 sqrt(g)
+  T sqrt_2_over_g;   // sqrt(2/g)
+  T g_half;          // g/2
+};
+template <typename T>
+__device__ __forceinline__ LamConstF64<T> lam_const_f64(T g, T sqrt2) {
+  LamConstF64<T> k;
+  const T t0 = T(2) * sqrt2 - T(1);
+  k.x0 = t0 * t0;
+  k.a = T(1) / (T(2) * sqrt2);
+  k.two_a = T(2) * k.a;
+  k.sixteen_g = T(16) * g;
+  k.two_sqrt_g = T(2) * sqrt(g);
+  k.sqrt_2_over_g = sqrt(T(2) / g);
+  k.g_half = g / T(2);
+  return k;
+}
+
+// phi (SOURCES/condlim.f90:960-981).  The node terms one_over_h(hl),
+// one_over_h(hr) and sqrt(g hl), sqrt(g hr) are the nodes' per-node values
+// (ovhl, ovhr; sqghl = sqrt(g |hl|) equals sqrt(g hl) for hl > 0, and is
+// recomputed otherwise), so each is formed once per node instead of per
+// entry and per call; one_over_h(h) and sqrt(g h) are formed once per call.
+template <typename T>
+__device__ __forceinline__ T phi_fn(T h, T ul, T hl, T ur, T hr, T g, T htiny, T ovhl, T ovhr, T sqghl, T sqghr,
+                                    T g_half) {
+  const bool shock_l = h > hl, shock_r = h > hr;
+  const T ovh = (shock_l || shock_r) ? one_over_h(h, htiny) : T(0);
+  const T sgh = (!shock_l || !shock_r) ? sqrt(g * h) : T(0);
   T fl, fr;
-  if (h > hl) {
-    T ovh = one_over_h(h, htiny), ovhl = one_over_h(hl, htiny);
-    fl = (h - hl) * sqrt((g / T(2)) * (ovh + ovhl));
-  } else {
-    fl = T(2) * (sqrt(g * h) - sqrt(g * hl));
-  }
-  if (h > hr) {
-    T ovh = one_over_h(h, htiny), ovhr = one_over_h(hr, htiny);
-    fr = (h - hr) * sqrt((g / T(2)) * (ovh + ovhr));
-  } else {
-    fr = T(2) * (sqrt(g * h) - sqrt(g * hr));
-  }
+  if (shock_l) fl = (h - hl) * sqrt(g_half * (ovh + ovhl));
+  else fl = T(2) * (sgh - (hl > T(0) ? sqghl : sqrt(g * hl)));
+  if (shock_r) fr = (h - hr) * sqrt(g_half * (ovh + ovhr));
+  else fr = T(2) * (sgh - (hr > T(0) ? sqghr : sqrt(g * hr)));
   return fl + fr + ur - ul;
 }
 
-// compute_lambda_vacc (SOURCES/condlim.f90:879-957) with ovhl/ovhr passed in
-// (they equal the node's one_over_h bit for bit).  Returns false where the
-// reference STOPs (Delta < 0).
+// compute_lambda_vacc (SOURCES/condlim.f90:879-957) with the node values
+// ovhl/ovhr (one_over_h) and sqghl/sqghr (sqrt(g |h|), the reference's
+// sql/sqr) passed in; they equal what the reference forms bit for bit.
+// Returns false where the reference STOPs (Delta < 0).
 template <typename T>
-__device__ __forceinline__ bool lambda_vacc(T hl, T qxl, T qyl, T ovhl, T hr, T qxr, T qyr, T ovhr,
-                                            T nx, T ny, T g, T htiny, T sqrt2, T* lambda) {
+__device__ __forceinline__ bool lambda_vacc(T hl, T qxl, T qyl, T ovhl, T sqghl, T hr, T qxr, T qyr, T ovhr, T sqghr,
+                                            T nx, T ny, T g, T htiny, const LamConstF64<T>& k, T* lambda) {
   T vl = (qxl * nx + qyl * ny) * ovhl;
   T vr = (qxr * nx + qyr * ny) * ovhr;
-  T sql = sqrt(g * tabs(hl));
-  T sqr = sqrt(g * tabs(hr));
-  T t0 = T(2) * sqrt2 - T(1);
-  T x0 = t0 * t0;
+  const T sql = sqghl, sqr = sqghr;
   T hmin, hmax;
   if (hl <= hr) { hmin = hl; hmax = hr; } else { hmin = hr; hmax = hl; }
   T ht;
   bool ok = true;
-  T fh = phi_fn(x0 * hmin, vl, hl, vr, hr, g, htiny);
+  T fh = phi_fn(k.x0 * hmin, vl, hl, vr, hr, g, htiny, ovhl, ovhr, sql, sqr, k.g_half);
   if (T(0) <= fh) {
     T s = tmax(vl - vr + T(2) * sql + T(2) * sqr, T(0));
-    ht = tmin(x0 * hmin, s * s / (T(16) * g));
+    ht = tmin(k.x0 * hmin, s * s / k.sixteen_g);
   } else {
-    fh = phi_fn(x0 * hmax, vl, hl, vr, hr, g, htiny);
+    fh = phi_fn(k.x0 * hmax, vl, hl, vr, hr, g, htiny, ovhl, ovhr, sql, sqr, k.g_half);
     T sqrmin = sqrt(hmin), sqrmax = sqrt(hmax);
     if (T(0) <= fh) {
-      T a = T(1) / (T(2) * sqrt2);
-      T c = -(hmin * a) - sqrmin * sqrmax + sqrmin * (vr - vl) / (T(2) * sqrt(g));
-      T Delta = hmin - T(4) * a * c;
+      T c = -(hmin * k.a) - sqrmin * sqrmax + sqrmin * (vr - vl) / k.two_sqrt_g;
+      T Delta = hmin - T(4) * k.a * c;
       if (Delta < T(0)) { ok = false; Delta = T(0); }
-      T s = (-sqrmin + sqrt(Delta)) / (T(2) * a);
-      ht = tmin(x0 * hmax, s * s);
+      T s = (-sqrmin + sqrt(Delta)) / k.two_a;
+      ht = tmin(k.x0 * hmax, s * s);
     } else {
-      ht = sqrmin * sqrmax * (T(1) + sqrt(T(2) / g) * (vl - vr) / (sqrmin + sqrmax));
+      ht = sqrmin * sqrmax * (T(1) + k.sqrt_2_over_g * (vl - vr) / (sqrmin + sqrmax));
     }
   }
   T lbdl = vl - sql * sqrt((T(1) + tmax((ht - hl) * ovhl / T(2), T(0))) * (T(1) + tmax((ht - hl) * ovhl, T(0))));

@@ -27,6 +27,7 @@ struct StateMix {
 // Work arrays of one stage
 struct WorkF64 {
   double *ovh, *v1, *v2, *ent, *alpha;   // per row
+  double* sqgh;                          // per row: sqrt(g |h|)
   double *dL, *muL, *fct;                // per off-diagonal entry
   double *dLii, *muLii;                  // per row: the diagonal of dL, muL
   double *res, *rminus;                  // per row
@@ -56,6 +57,7 @@ struct StageArgs {
   int block;
   int entropy = 0;   // some instance uses 'entropy_visc': launch k_entropy
   const double* dij_in = nullptr;   // stage 1: d_ij of k_dt on the same state (bit-identical)
+  int skip_node = 0;                // stage 1: k_node already ran on this state (before k_dt)
 };
 
 // Tiles of rows for the shared-memory variants of the entry loops: a block
@@ -91,7 +93,8 @@ struct KernelEvents {
 
 void launch_stage_f64(const StageArgs& a, cudaStream_t s, const KernelEvents* kev = nullptr);
 void launch_dt_f64(const Graph& G, const InstConst* C, InstState* St, const StateF64& u, double* d_out,
-                   double* dii_out, unsigned* err, int block, cudaStream_t s);
+                   double* dii_out, unsigned* err, int block, cudaStream_t s, const WorkF64* node = nullptr);
+void launch_node_f64(const StageArgs& a, cudaStream_t s);   // per-node arrays of the state a.u
 void launch_step_begin(const InstConst* C, InstState* St, int n_inst, cudaStream_t s);
 void launch_step_end(InstState* St, int n_inst, cudaStream_t s);
 void launch_reset_counters(InstState* St, int n_inst, cudaStream_t s);

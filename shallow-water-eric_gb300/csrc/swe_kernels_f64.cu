@@ -24,6 +24,7 @@ struct NodeF64 {        // per-row arrays of the FP64 path
   double* v2;
   double* ent;
   double* alpha;
+  double* sqgh;         // sqrt(g |h|), the sql / sqr of compute_lambda_vacc
 };
 
 // ---------------------------------------------------------------------------
@@ -47,6 +48,7 @@ __global__ void k_node_f64(Graph G, const InstConst* __restrict__ C, const InstS
   nd.ovh[r] = o;
   nd.v1[r] = v1;
   nd.v2[r] = v2;
+  nd.sqgh[r] = sqrt(c.g * tabs(h));
   double E = c.g * (h * h);
   E = E + v1 * qx;
   E = E + v2 * qy;
@@ -273,7 +275,7 @@ __global__ void k_low_f64(Graph G, const InstConst* __restrict__ C, const InstSt
   const InstConst& c = C[b];
   const int S = c.S;
   const double g = c.g, htiny = c.htiny, dt = st.dt;
-  const double sqrt2 = sqrt(2.0);
+  const LamConstF64<double> lk = lam_const_f64(g, sqrt(2.0));
   const int64_t base = entry_base(G, r);
   const int dp = G.dpos[r];
   double ui[5];
@@ -299,7 +301,8 @@ __global__ void k_low_f64(Graph G, const InstConst* __restrict__ C, const InstSt
         const double norm = sqrt(cxe * cxe + cye * cye);
         const double nx = cxe / norm, ny = cye / norm;
         double lam;
-        if (!lambda_vacc(ui[0], ui[1], ui[2], ovhi, u.h[j], u.q1[j], u.q2[j], nd.ovh[j], nx, ny, g, htiny, sqrt2,
+        if (!lambda_vacc(ui[0], ui[1], ui[2], ovhi, nd.sqgh[r], u.h[j], u.q1[j], u.q2[j], nd.ovh[j], nd.sqgh[j], nx,
+                         ny, g, htiny, lk,
                          &lam))
           delta_bad = true;
         d = norm * lam;
@@ -611,8 +614,8 @@ __global__ void k_entropy_f64(Graph G, const InstConst* __restrict__ C, const In
 // receives every d_ij.
 // ---------------------------------------------------------------------------
 __global__ void k_dt_f64(Graph G, const InstConst* __restrict__ C, InstState* __restrict__ St, StateF64 u,
-                         const double* __restrict__ ovh, double* __restrict__ d_out, double* __restrict__ dii_out,
-                         unsigned* __restrict__ err) {
+                         const double* __restrict__ ovh, const double* __restrict__ sqgh, double* __restrict__ d_out,
+                         double* __restrict__ dii_out, unsigned* __restrict__ err) {
   int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   double val = 0.0;
   int b = -1;
@@ -622,9 +625,10 @@ __global__ void k_dt_f64(Graph G, const InstConst* __restrict__ C, InstState* __
       const InstConst& c = C[b];
       const int L = G.len[r];
       const int64_t base = entry_base(G, r);
-      const double sqrt2 = sqrt(2.0);
+      const LamConstF64<double> lk = lam_const_f64(c.g, sqrt(2.0));
       const double hi = u.h[r], q1 = u.q1[r], q2 = u.q2[r];
       const double ovhi = ovh ? ovh[r] : one_over_h(hi, c.htiny);
+      const double sqgi = sqgh ? sqgh[r] : sqrt(c.g * tabs(hi));
       double s = 0.0;
       bool bad = false;
       for (int k = 0; k < L; k++) {
@@ -636,9 +640,10 @@ __global__ void k_dt_f64(Graph G, const InstConst* __restrict__ C, InstState* __
           const double norm = sqrt(cxe * cxe + cye * cye);
           const double hj = u.h[j];
           const double ovhj = ovh ? ovh[j] : one_over_h(hj, c.htiny);
+          const double sqgj = sqgh ? sqgh[j] : sqrt(c.g * tabs(hj));
           double lam;
-          if (!lambda_vacc(hi, q1, q2, ovhi, hj, u.q1[j], u.q2[j], ovhj, cxe / norm, cye / norm, c.g, c.htiny, sqrt2,
-                           &lam))
+          if (!lambda_vacc(hi, q1, q2, ovhi, sqgi, hj, u.q1[j], u.q2[j], ovhj, sqgj, cxe / norm, cye / norm, c.g,
+                           c.htiny, lk, &lam))
             bad = true;
           d = norm * lam;
         }
@@ -793,11 +798,16 @@ static inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) 
 #define EV_BEGIN(k) if (kev) cudaEventRecord(kev->ev[2 * (k)], s)
 #define EV_END(k) if (kev) cudaEventRecord(kev->ev[2 * (k) + 1], s)
 
+void launch_node_f64(const StageArgs& a, cudaStream_t s) {
+  NodeF64 nd{a.w.ovh, a.w.v1, a.w.v2, a.w.ent, a.w.alpha, a.w.sqgh};
+  k_node_f64<<<nblk(a.G.n_rows, a.block), a.block, 0, s>>>(a.G, a.C, a.St, a.u, nd);
+}
+
 void launch_stage_f64(const StageArgs& a, cudaStream_t s, const KernelEvents* kev) {
   const int bs = a.block;
-  NodeF64 nd{a.w.ovh, a.w.v1, a.w.v2, a.w.ent, a.w.alpha};
+  NodeF64 nd{a.w.ovh, a.w.v1, a.w.v2, a.w.ent, a.w.alpha, a.w.sqgh};
   EV_BEGIN(1);
-  k_node_f64<<<nblk(a.G.n_rows, bs), bs, 0, s>>>(a.G, a.C, a.St, a.u, nd);
+  if (!a.skip_node) k_node_f64<<<nblk(a.G.n_rows, bs), bs, 0, s>>>(a.G, a.C, a.St, a.u, nd);
   EV_END(1); EV_BEGIN(2);
   k_low_f64<<<nblk(a.G.n_rows, bs), bs, 0, s>>>(a.G, a.C, a.St, a.u, nd, a.w.dL, a.w.muL, a.w.dLii, a.w.muLii,
                                                 a.w.uL, a.w.res, a.dij_in, a.err);
@@ -814,8 +824,9 @@ void launch_stage_f64(const StageArgs& a, cudaStream_t s, const KernelEvents* ke
 }
 
 void launch_dt_f64(const Graph& G, const InstConst* C, InstState* St, const StateF64& u, double* d_out,
-                   double* dii_out, unsigned* err, int block, cudaStream_t s) {
-  k_dt_f64<<<nblk(G.n_rows, block), block, 0, s>>>(G, C, St, u, nullptr, d_out, dii_out, err);
+                   double* dii_out, unsigned* err, int block, cudaStream_t s, const WorkF64* node) {
+  k_dt_f64<<<nblk(G.n_rows, block), block, 0, s>>>(G, C, St, u, node ? node->ovh : nullptr,
+                                                   node ? node->sqgh : nullptr, d_out, dii_out, err);
 }
 
 void launch_step_begin(const InstConst* C, InstState* St, int n_inst, cudaStream_t s) {
