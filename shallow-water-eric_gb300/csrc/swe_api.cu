@@ -234,6 +234,20 @@ static int build_device(swe_ctx* c, const std::vector<std::vector<double>>& bath
   if (c->precision == SWE_PREC_FP64) {
     G.cx = upload_vec(c, L.cx, st);
     G.cy = upload_vec(c, L.cy, st);
+    {   // compute_dij's norm = SQRT(c.c) and normal c/norm per entry (update.f90:309-312),
+        // the same IEEE operations as a kernel would do per use
+      std::vector<double> nrm(L.n_entries), nx(L.n_entries), ny(L.n_entries);
+      for (int64_t e = 0; e < L.n_entries; e++) {
+        const double cx = L.cx[e], cy = L.cy[e];
+        const double cc = cx * cx + cy * cy;
+        nrm[e] = std::sqrt(cc);
+        nx[e] = cx / nrm[e];                       // padding entries (never read): 0/0
+        ny[e] = cy / nrm[e];
+      }
+      G.cnorm = upload_vec(c, nrm, st);
+      G.cnx = upload_vec(c, nx, st);
+      G.cny = upload_vec(c, ny, st);
+    }
     G.cxii = upload_vec(c, L.cxii, st);
     G.cyii = upload_vec(c, L.cyii, st);
   } else {

@@ -58,6 +58,9 @@ struct Graph {
   const float* __restrict__ cyf;
   const float* __restrict__ cxiif;
   const float* __restrict__ cyiif;
+  const double* __restrict__ cnorm;       // FP64 path, per entry: |c_ij| and c_ij/|c_ij|
+  const double* __restrict__ cnx;         // (compute_dij's norm and normal, formed once)
+  const double* __restrict__ cny;
   const double* __restrict__ lumped;
   const double* __restrict__ inv_lumped;
   const float* __restrict__ lumpedf;      // FP32 copies (mixed path)

@@ -298,8 +298,7 @@ __global__ void k_low_f64(Graph G, const InstConst* __restrict__ C, const InstSt
       if (dij_in) {                            // stage 1: k_dt computed this d_ij on this state
         d = dij_in[e];
       } else {
-        const double norm = sqrt(cxe * cxe + cye * cye);
-        const double nx = cxe / norm, ny = cye / norm;
+        const double norm = G.cnorm[e], nx = G.cnx[e], ny = G.cny[e];   // sqrt(c.c), c/norm
         double lam;
         if (!lambda_vacc(ui[0], ui[1], ui[2], ovhi, nd.sqgh[r], u.h[j], u.q1[j], u.q2[j], nd.ovh[j], nd.sqgh[j], nx,
                          ny, g, htiny, lk,
@@ -637,12 +636,12 @@ __global__ void k_dt_f64(Graph G, const InstConst* __restrict__ C, InstState* __
         {
           const int j = G.col[e];
           const double cxe = G.cx[e], cye = G.cy[e];
-          const double norm = sqrt(cxe * cxe + cye * cye);
+          const double norm = G.cnorm[e];                                  // sqrt(c.c)
           const double hj = u.h[j];
           const double ovhj = ovh ? ovh[j] : one_over_h(hj, c.htiny);
           const double sqgj = sqgh ? sqgh[j] : sqrt(c.g * tabs(hj));
           double lam;
-          if (!lambda_vacc(hi, q1, q2, ovhi, sqgi, hj, u.q1[j], u.q2[j], ovhj, sqgj, cxe / norm, cye / norm, c.g,
+          if (!lambda_vacc(hi, q1, q2, ovhi, sqgi, hj, u.q1[j], u.q2[j], ovhj, sqgj, G.cnx[e], G.cny[e], c.g,
                            c.htiny, lk, &lam))
             bad = true;
           d = norm * lam;
