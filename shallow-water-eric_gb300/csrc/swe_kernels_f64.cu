@@ -181,9 +181,12 @@ __device__ __forceinline__ void smb_rows_f64(const Graph& G, const InstConst& c,
     const double zmax = tmax(zi, zj);
     const double Hij = tmax(0.0, ui[0] + zi - zmax);
     const double Hji = tmax(0.0, uj[0] + zj - zmax);
+    // H*/h, formed once for the three rows (each tests h against its own bound)
+    const double qij = (ui[0] <= 0.0) ? 0.0 : Hij / ui[0];
+    const double qji = (uj[0] <= 0.0) ? 0.0 : Hji / uj[0];
     if (want_round) {   // smb_2_roundoff (htiny tests)
-      const double ratij = (ui[0] <= htiny) ? 0.0 : Hij / ui[0];
-      const double ratji = (uj[0] <= htiny) ? 0.0 : Hji / uj[0];
+      const double ratij = (ui[0] <= htiny) ? 0.0 : (ui[0] > 0.0 ? qij : Hij / ui[0]);   // h > htiny >= 0: qij
+      const double ratji = (uj[0] <= htiny) ? 0.0 : (uj[0] > 0.0 ? qji : Hji / uj[0]);
       double xx = 0.0;
       xx = xx - cxe * (v1j);
       xx = xx - cye * (v2j);
@@ -203,8 +206,8 @@ __device__ __forceinline__ void smb_rows_f64(const Graph& G, const InstConst& c,
       rk[2] = rk[2] - g * ui[0] * (uj[0] + zj - ui[0] - zi) * cye;
     }
     if (want_plain) {   // smb_2 (h <= 0 tests)
-      const double ratij = (ui[0] <= 0.0) ? 0.0 : Hij / ui[0];
-      const double ratji = (uj[0] <= 0.0) ? 0.0 : Hji / uj[0];
+      const double ratij = qij;
+      const double ratji = qji;
       for (int q = 0; q < S; q++) {
         double x2 = 0.0;
         x2 = x2 - cxe * (v1j * uj[q]);
@@ -215,8 +218,8 @@ __device__ __forceinline__ void smb_rows_f64(const Graph& G, const InstConst& c,
       rk2[2] = rk2[2] - g * ui[0] * (uj[0] + zj - ui[0] - zi) * cye;
     }
     if (want_t1) {      // smb_1 (htiny tests, flux vv = velocity u_k)
-      const double ratij = (ui[0] <= htiny) ? 0.0 : Hij / ui[0];
-      const double ratji = (uj[0] <= htiny) ? 0.0 : Hji / uj[0];
+      const double ratij = (ui[0] <= htiny) ? 0.0 : (ui[0] > 0.0 ? qij : Hij / ui[0]);   // h > htiny >= 0: qij
+      const double ratji = (uj[0] <= htiny) ? 0.0 : (uj[0] > 0.0 ? qji : Hji / uj[0]);
       for (int q = 0; q < S; q++) {
         double xx = 0.0;
         xx = xx - cxe * ((v1j * uj[q]) * ratji + (v1i * ui[q]) * ratij);
