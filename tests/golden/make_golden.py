@@ -15,6 +15,9 @@ Fixtures written (all small, numpy .npz):
   ref_{bath,h_1,hpz_1}.vtk.gz  SOURCES/BACKUP/*.vtk, the reference's own vtk_2d
                                output on cav_0.2 (gzip of the files as shipped):
                                pins the VTK text byte for byte.
+  ref_data_{sources,paraboloid,backup}.txt
+                               SOURCES/data, PARABOLOID/data, SOURCES/BACKUP/data
+                               as shipped: inputs for the data-file reader.
   oracle_*.npz                 FP64 oracle trajectories (regression vectors
                                for the oracle itself and GPU parity vectors).
 """
@@ -67,6 +70,9 @@ def main():
     np.savez(HERE / "pin_lis.npz", h=np.array([0.2, 0.1, 0.05, 0.025, 0.0125]), it_max=np.array(it_max),
              l1=np.array(l1), cfl=0.3)
 
+    for tag, rel in (("sources", "SOURCES/data"), ("paraboloid", "PARABOLOID/data"),
+                     ("backup", "SOURCES/BACKUP/data")):
+        (HERE / f"ref_data_{tag}.txt").write_bytes((REF / rel).read_bytes())
     import gzip
     for name in ("bath", "h_1", "hpz_1"):
         data = (REF / "SOURCES/BACKUP" / f"{name}.vtk").read_bytes()
