@@ -169,6 +169,10 @@ int swe_download_device(swe_ctx* ctx, double* d_un);
 /* Set every instance's time and final time (arrays of n_inst, NULL time =
  * keep). */
 int swe_set_time(swe_ctx* ctx, const double* time, const double* t_final);
+/* The instances' time, t_final and last dt (n_inst each; any may be null):
+ * with swe_download, what a checkpoint needs to resume with swe_upload and
+ * swe_set_time. */
+int swe_get_time(swe_ctx* ctx, double* time, double* t_final, double* dt);
 
 /* Advance nsteps iterations of the reference time loop (SOURCES/main.f90:
  * 61-91) on the device: per instance, while time < t_final: dt =

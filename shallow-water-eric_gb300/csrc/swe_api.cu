@@ -15,6 +15,8 @@
 #include <thread>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/swe_gpu.h"
 #include "swe_kernels.hpp"
 #include "swe_setup.hpp"
@@ -124,6 +126,14 @@ struct swe_ctx {
   int euler_inst = -1;
   std::string err;
   std::string tuning = "thread-per-row SELL-32, block 128";
+};
+
+// NVTX range over an API call (host timeline in nsys / ncu; no cost without a tool)
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
 };
 
 static int fail(swe_ctx* c, int code, const std::string& msg) {
@@ -642,6 +652,7 @@ static void drop_graphs(swe_ctx* c) {
 
 static int create_common(swe_ctx** out, int n_inst, const int* np, const int* me, const int* jj, const double* rr,
                          const double* bath, const swe_params* params) {
+  NvtxRange nvtx("swe_create");
   if (!out) return SWE_ERR_ARG;
   *out = nullptr;
   if (n_inst <= 0 || !np || !me || !jj || !rr || !bath || !params) return SWE_ERR_ARG;
@@ -872,6 +883,7 @@ SWE_API int swe_compute_dij(swe_ctx* c, int inst, const double* un, double* dij,
 }
 
 SWE_API int swe_euler(swe_ctx* c, int inst, const double* un, double* unext) {
+  NvtxRange nvtx("swe_euler");
   if (!c || inst < 0 || inst >= c->n_inst || !un || !unext) return fail(c, SWE_ERR_ARG, "bad arguments");
   if (!(c->params[inst].dt > 0)) return fail(c, SWE_ERR_ARG, "params.dt must be > 0 for swe_euler");
   int rc = to_device(c, un, false, c->node_off[inst], c->node_off[inst + 1]);
@@ -1036,6 +1048,7 @@ SWE_API int swe_norms(swe_ctx* c, int inst, int field, const double* f_anal, dou
 }
 
 SWE_API int swe_upload(swe_ctx* c, const double* un) {
+  NvtxRange nvtx("swe_upload");
   if (!c || !un) return fail(c, SWE_ERR_ARG, "bad arguments");
   int rc = to_device(c, un, false, 0, c->node_off[c->n_inst]);
   if (rc) return rc;
@@ -1044,6 +1057,7 @@ SWE_API int swe_upload(swe_ctx* c, const double* un) {
 }
 
 SWE_API int swe_download(swe_ctx* c, double* un) {
+  NvtxRange nvtx("swe_download");
   if (!c || !un) return fail(c, SWE_ERR_ARG, "bad arguments");
   int rc = from_device_state(c, un, false, 0, c->node_off[c->n_inst], c->precision == SWE_PREC_FP64 ? &c->A : nullptr,
                              c->precision == SWE_PREC_FP64 ? nullptr : &c->mA);
@@ -1066,6 +1080,19 @@ SWE_API int swe_download_device(swe_ctx* c, double* d_un) {
                              c->precision == SWE_PREC_FP64 ? nullptr : &c->mA);
   if (rc) return rc;
   CK(cudaStreamSynchronize(c->stream));
+  return SWE_OK;
+}
+
+SWE_API int swe_get_time(swe_ctx* c, double* time, double* t_final, double* dt) {
+  if (!c) return SWE_ERR_ARG;
+  std::vector<InstState> hs;
+  int rc = save_state(c, hs);
+  if (rc) return rc;
+  for (int b = 0; b < c->n_inst; b++) {
+    if (time) time[b] = hs[b].time;
+    if (t_final) t_final[b] = hs[b].t_final;
+    if (dt) dt[b] = hs[b].dt;
+  }
   return SWE_OK;
 }
 
@@ -1229,6 +1256,7 @@ static int autotune(swe_ctx* c) {
 }
 
 SWE_API int swe_autotune(swe_ctx* c) {
+  NvtxRange nvtx("swe_autotune");
   if (!c) return SWE_ERR_ARG;
   return autotune(c);
 }
@@ -1332,6 +1360,7 @@ SWE_API int swe_frame_fields(swe_ctx* c, int inst, double hmax0, double* hpz, do
 }
 
 SWE_API int swe_frame_async(swe_ctx* c, int inst, double hmax0, const char* hpz_path, const char* h_path) {
+  NvtxRange nvtx("swe_frame_async");
   if (!c || inst < 0 || inst >= c->n_inst || !hpz_path || !h_path) return fail(c, SWE_ERR_ARG, "bad arguments");
   int rc = frame_setup(c);
   if (rc) return rc;
@@ -1408,6 +1437,7 @@ SWE_API int swe_gauges_set(swe_ctx* c, int n, const int* inst, const double* rr,
 }
 
 SWE_API int swe_gauges_read(swe_ctx* c, int max_rows, double* out, int* rows, long long* lost) {
+  NvtxRange nvtx("swe_gauges_read");
   if (!c || max_rows < 0 || !rows || (max_rows && !out)) return fail(c, SWE_ERR_ARG, "bad arguments");
   *rows = 0;
   if (lost) *lost = 0;
@@ -1436,6 +1466,7 @@ SWE_API int swe_gauges_read(swe_ctx* c, int max_rows, double* out, int* rows, lo
 }
 
 SWE_API int swe_rk3_steps(swe_ctx* c, int nsteps, double* time_out, double* dt_out, int* steps_done) {
+  NvtxRange nvtx("swe_rk3_steps");
   if (!c || nsteps < 0) return fail(c, SWE_ERR_ARG, "bad arguments");
   int rc;
   if (!c->tuned) {

@@ -38,7 +38,7 @@ EXPORTS = [
     "swe_set_time", "swe_rk3_steps", "swe_mass", "swe_last_launch_count", "swe_tuning",
     "swe_last_device_ms", "swe_profile_kernels", "swe_fct_positivity_noalloc", "swe_autotune",
     "swe_write_vtk_2d", "swe_frame_fields", "swe_frame_async", "swe_frames_wait", "swe_gauges_set",
-    "swe_gauges_read",
+    "swe_gauges_read", "swe_get_time",
 ]
 NOALLOC_MAX_NODES = 1 << 20   # SWE_NOALLOC_MAX_NODES
 KERNEL_KINDS = ("dt", "node", "low", "fct", "update")
@@ -89,6 +89,7 @@ def load(build: bool = True):
         "swe_upload_device": ([vp, ctypes.c_void_p], ctypes.c_int),
         "swe_download_device": ([vp, ctypes.c_void_p], ctypes.c_int),
         "swe_set_time": ([vp, dp, dp], ctypes.c_int),
+        "swe_get_time": ([vp, dp, dp, dp], ctypes.c_int),
         "swe_rk3_steps": ([vp, ctypes.c_int, dp, dp, ip], ctypes.c_int),
         "swe_mass": ([vp, dp], ctypes.c_int),
         "swe_last_launch_count": ([vp], ctypes.c_longlong),

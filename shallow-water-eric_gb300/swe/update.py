@@ -244,6 +244,28 @@ class Update:
         tf = np.broadcast_to(np.asarray(t_final, np.float64), (self.n_inst,)).copy()
         self._check(self._L.swe_set_time(self.h, _L.dp(t), _L.dp(tf)))
 
+    def get_time(self):
+        """(time, t_final, dt) per instance."""
+        t = np.zeros(self.n_inst); tf = np.zeros(self.n_inst); dt = np.zeros(self.n_inst)
+        self._check(self._L.swe_get_time(self.h, _L.dp(t), _L.dp(tf), _L.dp(dt)))
+        return t, tf, dt
+
+    def save_checkpoint(self, path):
+        """The state and the instances' clocks as raw FP64 (npz): resuming
+        from it continues the run bit for bit (the mixed state's double-float
+        depth and FP32 momenta round-trip exactly through FP64)."""
+        t, tf, dt = self.get_time()
+        np.savez(path, un=self.download(), time=t, t_final=tf, dt=dt, np_=self.np_, me=self._me,
+                 S=self.S, precision=self.params[0].precision)
+
+    def load_checkpoint(self, path):
+        with np.load(path) as z:
+            if not (np.array_equal(z["np_"], self.np_) and np.array_equal(z["me"], self._me) and int(z["S"]) == self.S
+                    and int(z["precision"]) == self.params[0].precision):
+                raise ValueError("checkpoint of another mesh, system or precision")
+            self.upload(z["un"])
+            self.set_time(z["time"], z["t_final"])
+
     def rk3_steps(self, nsteps):
         t = np.zeros(self.n_inst); dt = np.zeros(self.n_inst); n = ctypes.c_int()
         self._check(self._L.swe_rk3_steps(self.h, nsteps, _L.dp(t), _L.dp(dt), ctypes.byref(n)))

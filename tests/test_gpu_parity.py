@@ -703,3 +703,27 @@ def test_malpasset_time_loop_fixed_dt_and_htiny():
     assert n == 10 and dtg[0] == 2.5e-2 and tg[0] == pytest.approx(0.25, rel=1e-14)
     np.testing.assert_array_equal(upd.download(), u)
     upd.close()
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_checkpoint_resume_is_bit_exact(tmp_path, prec):
+    """A run stopped after 5 steps, saved, and resumed in a new context
+    continues bit for bit like the uninterrupted run."""
+    case = C.dam_break_case(n=31)
+    upd = from_case(case, precision=prec)
+    upd.upload(case.u0)
+    upd.set_time(0.0, 0.2)
+    upd.rk3_steps(5)
+    upd.save_checkpoint(tmp_path / "ck.npz")
+    upd.rk3_steps(7)
+    want, (t_want, _, _) = upd.download(), upd.get_time()
+    upd.close()
+    again = from_case(case, precision=prec)
+    again.load_checkpoint(tmp_path / "ck.npz")
+    again.rk3_steps(7)
+    np.testing.assert_array_equal(again.download(), want)
+    assert again.get_time()[0][0] == t_want[0]
+    other = from_case(C.dam_break_case(n=21), precision=prec)
+    with pytest.raises(ValueError):
+        other.load_checkpoint(tmp_path / "ck.npz")
+    again.close(); other.close()
