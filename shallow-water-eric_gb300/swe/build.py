@@ -77,7 +77,29 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
+    _build_driver()
     return LIB
+
+
+DRIVER = LIB.with_name("swe_main")
+
+
+def _build_driver():
+    """swe_main (csrc/swe_main.cpp): the reference's main program for the dam
+    break over the C++ host interface include/swe_update.hpp, linked against
+    the library next to it."""
+    src = CSRC / "swe_main.cpp"
+    deps = [src, LIB, INCLUDE / "swe_update.hpp", INCLUDE / "swe_gpu.h"]
+    if DRIVER.exists() and DRIVER.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
+        return DRIVER
+    tmp = DRIVER.with_name(f"swe_main.{os.getpid()}")
+    cmd = ["g++", "-O2", "-std=c++17", f"-I{INCLUDE}", str(src), f"-L{LIB.parent}", "-lswe_gpu",
+           "-Wl,-rpath,$ORIGIN", "-o", str(tmp)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, DRIVER)
+    return DRIVER
 
 
 if __name__ == "__main__":

@@ -91,3 +91,18 @@ def test_cases_shapes():
     s = C.sgn_case(nx=21, ny=3)
     assert s.u0.shape == (5, 63)
     np.testing.assert_allclose(s.u0[3], s.u0[0] ** 2)
+
+
+def test_cpp_driver_builds_and_stops_without_device():
+    """The C++ host side (include/swe_update.hpp) and the main-program driver
+    over it build with the library; with no CUDA device the driver reports
+    the library's refusal and stops with a nonzero status (no CPU path)."""
+    import subprocess
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from swe import build as B
+    L.load()
+    r = subprocess.run([str(B.DRIVER), "--n", "5"], capture_output=True, text=True)
+    assert r.returncode == 3
+    assert "no CUDA device" in r.stderr
