@@ -64,3 +64,21 @@ def test_driver_frames(tmp_path):
     for name, f in (("hpz_3.vtk", hpz), ("h_3.vtk", h)):
         assert (tmp_path / name).read_text() == oracle.vtk_2d_text(name.ljust(200), case.mesh["jj"],
                                                                     case.mesh["rr"], f)
+
+
+def test_cpp_update_interface_bit_exact(tmp_path):
+    """tests/cpp/test_update_parity.cpp: construct_matrices, compute_dij,
+    euler and FCT_positivity through the C++ host interface against the C++
+    oracle, bit for bit, on a dam break and a wet/dry basin."""
+    from pathlib import Path
+    L.load()
+    olib = oracle.build()
+    here = Path(__file__).resolve().parent
+    exe = tmp_path / "test_update_parity"
+    cmd = ["g++", "-O2", "-std=c++17", f"-I{here.parent / 'include'}", str(here / "cpp" / "test_update_parity.cpp"),
+           f"-L{B.LIB.parent}", "-lswe_gpu", f"-Wl,-rpath,{B.LIB.parent}", f"-L{olib.parent}", "-lswe_oracle",
+           f"-Wl,-rpath,{olib.parent}", "-o", str(exe)]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert sum(1 for line in r.stdout.splitlines() if line.startswith("ok ")) == 18, r.stdout
