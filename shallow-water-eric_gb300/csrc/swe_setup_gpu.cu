@@ -19,7 +19,10 @@
 namespace swe {
 namespace {
 
-constexpr int kMaxElemsPerNode = 64;   // a node in more elements is rejected
+// st_csr caps a row at nparm = 90 entries and nothing else; a node can then
+// lie in at most C(89, 2) distinct triangles, so a node listed in more
+// elements than that repeats an element.  The guard bounds the per-node sort.
+constexpr int kMaxElemsPerNode = 4096;
 constexpr int kNparm = 90;             // st_csr's row cap (st_sparsekit.f90:801)
 
 enum : int { SE_RANGE = 1, SE_ELEMS = 2, SE_ROW = 4, SE_LUMPED = 8 };
@@ -229,7 +232,7 @@ std::string construct_matrices_device(HostMesh& m) {
   }
   if (st != cudaSuccess) msg = std::string("device setup: ") + cudaGetErrorString(st);
   else if (herr & SE_RANGE) msg = "element node index out of range";
-  else if (herr & SE_ELEMS) msg = "a node belongs to more than 64 elements";
+  else if (herr & SE_ELEMS) msg = "a node belongs to more than 4096 elements (repeated elements)";
   else if (herr & SE_ROW) msg = "a CSR row exceeds 90 entries (st_csr nparm)";
   else if (herr & SE_LUMPED) msg = "non-positive lumped mass (clockwise or degenerate triangle)";
   for (void* p : {(void*)d_jj, (void*)d_cnt, (void*)d_eoff, (void*)d_elist, (void*)d_err, (void*)d_rowlen,

@@ -727,3 +727,55 @@ def test_checkpoint_resume_is_bit_exact(tmp_path, prec):
     with pytest.raises(ValueError):
         other.load_checkpoint(tmp_path / "ck.npz")
     again.close(); other.close()
+
+
+def _fan(k, closed=True):
+    """One centre node (1) in k triangles of a regular fan of radius 1."""
+    ang = 2 * np.pi * np.arange(k) / k
+    rr = np.vstack([np.r_[0.0, np.cos(ang)], np.r_[0.0, np.sin(ang)]])
+    nxt = [(a + 1) % k for a in range(k)] if closed else list(range(1, k))
+    jj = np.array([[1, a + 2, b + 2] for a, b in zip(range(len(nxt)), nxt)], np.int32).T
+    return {"jj": np.asfortranarray(jj), "rr": np.asfortranarray(rr)}
+
+
+def _fan_case(k):
+    mesh = _fan(k)
+    r2 = mesh["rr"][0] ** 2 + mesh["rr"][1] ** 2
+    u0 = np.asfortranarray(np.vstack([1.0 + 0.1 * r2, 0.01 * mesh["rr"][0], np.zeros(mesh["rr"].shape[1])]))
+    p = C.Params(gravity=9.81, cfl=0.25, max_water_h=1.1, htiny=1e-4, type_test=4)
+    return C.Case(name=f"fan{k}", mesh=mesh, bath=np.zeros(u0.shape[1]), params=p, u0=u0, tfinal=1e30)
+
+
+def test_mesh_edge_cases_match_oracle():
+    """A single triangle, and a fan whose centre row has 81 entries (st_csr
+    accepts rows up to nparm = 90): matrices, compute_dij and a few RK3 steps
+    equal the oracle bit for bit.  A fan whose centre row would need 96
+    entries is rejected by both, as the reference STOPs."""
+    tri = {"jj": np.asfortranarray(np.array([[1], [2], [3]], np.int32)),
+           "rr": np.asfortranarray(np.array([[0.0, 1.0, 0.0], [0.0, 0.0, 1.0]]))}
+    one = C.Case(name="triangle", mesh=tri, bath=np.zeros(3), params=C.Params(type_test=4),
+                 u0=np.asfortranarray(np.array([[1.0, 0.5, 0.2], [0.0, 0.1, 0.0], [0.0, 0.0, -0.1]])), tfinal=1e30)
+    for case in (one, _fan_case(80)):
+        o = _oracle_for(case)
+        upd = from_case(case)
+        a, b = upd.matrices(), o.matrices()
+        for k in ("ia", "ja", "diag", "mass", "lumped", "cx", "cy"):
+            np.testing.assert_array_equal(a[k], b[k], err_msg=f"{case.name} {k}")
+        dg, dtg = upd.compute_dij(case.u0)
+        dr, dtr = o.compute_dij(case.u0)
+        np.testing.assert_array_equal(dg, dr)
+        assert dtg == dtr
+        u = case.u0.copy(order="F")
+        t = 0.0
+        for _ in range(3):
+            t = o.rk3_step(u, t)
+        upd.upload(case.u0)
+        upd.set_time(0.0, 1e30)
+        upd.rk3_steps(3)
+        np.testing.assert_array_equal(upd.download(), u, err_msg=case.name)
+        upd.close()
+    big = _fan_case(95)
+    with pytest.raises(L.SweError, match="90 entries"):
+        from_case(big)
+    with pytest.raises(Exception):
+        _oracle_for(big)
