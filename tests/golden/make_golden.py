@@ -15,6 +15,8 @@ Fixtures written (all small, numpy .npz):
   ref_{bath,h_1,hpz_1}.vtk.gz  SOURCES/BACKUP/*.vtk, the reference's own vtk_2d
                                output on cav_0.2 (gzip of the files as shipped):
                                pins the VTK text byte for byte.
+  ref_cav_0.2.FEM              MESHES/PARABOLOID/cav_0.2.FEM as shipped: the
+                               .FEM reader's input for the mesh fixture test.
   ref_data_{sources,paraboloid,backup}.txt
                                SOURCES/data, PARABOLOID/data, SOURCES/BACKUP/data
                                as shipped: inputs for the data-file reader.
@@ -70,6 +72,7 @@ def main():
     np.savez(HERE / "pin_lis.npz", h=np.array([0.2, 0.1, 0.05, 0.025, 0.0125]), it_max=np.array(it_max),
              l1=np.array(l1), cfl=0.3)
 
+    (HERE / "ref_cav_0.2.FEM").write_bytes((REF / "MESHES/PARABOLOID/cav_0.2.FEM").read_bytes())
     for tag, rel in (("sources", "SOURCES/data"), ("paraboloid", "PARABOLOID/data"),
                      ("backup", "SOURCES/BACKUP/data")):
         (HERE / f"ref_data_{tag}.txt").write_bytes((REF / rel).read_bytes())
