@@ -638,7 +638,6 @@ __global__ void k_dt_f64(Graph G, const InstConst* __restrict__ C, InstState* __
         double d = 0.0;
         {
           const int j = G.col[e];
-          const double cxe = G.cx[e], cye = G.cy[e];
           const double norm = G.cnorm[e];                                  // sqrt(c.c)
           const double hj = u.h[j];
           const double ovhj = ovh ? ovh[j] : one_over_h(hj, c.htiny);
