@@ -57,6 +57,9 @@ class Case:
     dirichlet: list = field(default_factory=list)   # [(comp0, js 1-based, values)]
     nsteps: int | None = None        # fixed step count when the workload names one
     exact: object = None             # callable(k, rr, t) -> values, when known
+    t0: float = 0.0                  # inputs%time at the start (1 for the reference's type 4)
+    bdy: object = None               # callable(un, t): bdy (main.f90:176-188) on the host, when known
+    bdy_fixed: bool = True           # Dirichlet values independent of t: the device loop can run it
 
 
 def _walls(mesh, S):

@@ -15,6 +15,7 @@ Meshes are dicts with ``jj`` (3, me) int32 1-based, counter-clockwise;
 """
 from __future__ import annotations
 
+import gzip
 import struct
 from pathlib import Path
 
@@ -35,8 +36,11 @@ def _records(buf: bytes):
 
 
 def read_fem(path):
-    """Raw content of a P1 ``.FEM`` file (no renumbering)."""
-    recs = _records(Path(path).read_bytes())
+    """Raw content of a P1 ``.FEM`` file (no renumbering); a ``.gz`` name
+    is read through gzip."""
+    path = Path(path)
+    buf = gzip.decompress(path.read_bytes()) if path.suffix == ".gz" else path.read_bytes()
+    recs = _records(buf)
     np_, nw, me, nws, mes = struct.unpack("<5i", recs[0][:20])
     if (nw, nws) != (3, 2):
         raise ValueError("only P1 triangle meshes are supported")

@@ -300,8 +300,14 @@ class Update:
         return self._L.swe_tuning(self.h).decode()
 
 
-def from_case(case, precision=None):
-    """Build an Update for a cases.Case (bath, params and Dirichlet data)."""
+def from_case(case, precision=None, per_call=False):
+    """Build an Update for a cases.Case (bath, params and Dirichlet data).
+    A case whose Dirichlet values change with time cannot run in the device
+    loop (rk3_steps imposes fixed values): it needs ``per_call=True`` and a
+    host loop that calls euler and the case's bdy per stage."""
+    if not getattr(case, "bdy_fixed", True) and not per_call:
+        raise ValueError(f"case {case.name}: Dirichlet values change with time; build it with per_call=True "
+                         "and run it through the per-call operators")
     p = case.params
     if precision is not None:
         from dataclasses import replace

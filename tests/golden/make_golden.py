@@ -17,6 +17,12 @@ Fixtures written (all small, numpy .npz):
                                pins the VTK text byte for byte.
   ref_cav_0.2.FEM              MESHES/PARABOLOID/cav_0.2.FEM as shipped: the
                                .FEM reader's input for the mesh fixture test.
+  ref_{rectangle.1,cdisk.1_mesh,dam_cav_0.25,bump_cav_0.3}.FEM.gz
+                               MESHES/SGN_CANAL/rectangle.1.FEM,
+                               PARABOLOID/cdisk.1_mesh.FEM, DAM_BREAK/cav_0.25.FEM,
+                               BUMP_3_1/cav_0.3.FEM (gzip of the files as
+                               shipped): the meshes of the reference's test
+                               cases 13, 12, 4 and 2/3/6/7.
   ref_data_{sources,paraboloid,backup}.txt
                                SOURCES/data, PARABOLOID/data, SOURCES/BACKUP/data
                                as shipped: inputs for the data-file reader.
@@ -81,6 +87,11 @@ def main():
         data = (REF / "SOURCES/BACKUP" / f"{name}.vtk").read_bytes()
         with gzip.GzipFile(HERE / f"ref_{name}.vtk.gz", "wb", mtime=0) as f:
             f.write(data)
+
+    for name, rel in (("rectangle.1", "SGN_CANAL/rectangle.1.FEM"), ("cdisk.1_mesh", "PARABOLOID/cdisk.1_mesh.FEM"),
+                      ("dam_cav_0.25", "DAM_BREAK/cav_0.25.FEM"), ("bump_cav_0.3", "BUMP_3_1/cav_0.3.FEM")):
+        with gzip.GzipFile(HERE / f"ref_{name}.FEM.gz", "wb", mtime=0) as f:
+            f.write((REF / "MESHES" / rel).read_bytes())
 
     # oracle trajectories
     m = dict(np.load(HERE / "mesh_cav_0.2.npz"))

@@ -19,6 +19,7 @@ import oracle
 from swe import cases as C, mesh as M
 from swe import lib as L
 from swe.update import Update, from_case
+from conftest import REF_CASES, OraclePerCall
 
 pytestmark = pytest.mark.gpu
 
@@ -779,3 +780,61 @@ def test_mesh_edge_cases_match_oracle():
         from_case(big)
     with pytest.raises(Exception):
         _oracle_for(big)
+
+
+@pytest.mark.parametrize("tt", sorted(REF_CASES))
+def test_reference_cases_on_the_device_loop(ref_case, tt):
+    """The reference's test cases (init, sol_anal and bdy of condlim.f90 and
+    main.f90, Dirichlet data fixed over the run): ten FP64 steps of the
+    device loop equal the oracle bit for bit.  The mixed path keeps h >= 0
+    and stays within 3x the FP64 oracle's own sensitivity to a 1e-7
+    perturbation of the initial state (plus 1e-5)."""
+    case = ref_case(tt)
+    o = _oracle_for(case)
+    u = case.u0.copy(order="F")
+    t = case.t0
+    for _ in range(10):
+        t = o.rk3_step(u, t)
+    upd = from_case(case)
+    upd.upload(case.u0)
+    upd.set_time(case.t0, 1e30)
+    tg, _, n = upd.rk3_steps(10)
+    assert n == 10 and tg[0] == t
+    np.testing.assert_array_equal(upd.download(), u)
+    upd.close()
+    up = case.u0.copy(order="F")
+    up *= 1 + 1e-7 * np.random.default_rng(0).uniform(-1, 1, up.shape)
+    o2 = _oracle_for(case)
+    t = case.t0
+    for _ in range(10):
+        t = o2.rk3_step(up, t)
+    mx = from_case(case, precision=1)
+    mx.upload(case.u0)
+    mx.set_time(case.t0, 1e30)
+    mx.rk3_steps(10)
+    um = mx.download()
+    err = _rel_l1(um[0], u[0], mx.lumped)
+    sens = _rel_l1(up[0], u[0], mx.lumped)
+    assert um[0].min() >= 0.0
+    assert err <= 3 * sens + MIXED_L1_TOL, (err, sens)
+    mx.close()
+
+
+def test_time_dependent_dirichlet_through_per_call_euler(golden):
+    """SOURCES/data (type 13 solitary wave, 'entropy_visc', h imposed at both
+    channel ends from sol_anal(t)) on MESHES/SGN_CANAL/rectangle.1: main.f90's
+    loop on the host over the C ABI's per-call compute_dij / euler, with bdy
+    at the reference's stage times, equals the same loop over the oracle bit
+    for bit."""
+    from swe import data as D, refcases as R
+    d = D.read_my_data(golden / "ref_data_sources.txt")
+    mesh = M.load_mesh_free_format(golden / "ref_rectangle.1.FEM.gz")
+    case = R.case_from_data(d, mesh)
+    assert not case.bdy_fixed
+    o = _oracle_for(case)
+    want, tw, nw = R.host_time_loop(OraclePerCall(o), case.bdy, case.u0, case.t0, 1e30, 8)
+    upd = from_case(case, per_call=True)
+    got, tg, ng = R.host_time_loop(R.PerCall(upd), case.bdy, case.u0, case.t0, 1e30, 8)
+    assert (ng, tg) == (nw, tw) == (8, tw)
+    np.testing.assert_array_equal(got, want)
+    upd.close()
