@@ -1,23 +1,35 @@
-// swe_main: the reference's main program (SOURCES/main.f90) for the unit
-// square dam break, written against the C++ host interface (swe_update.hpp)
-// instead of the Fortran modules: mesh, init, construct_matrices, then
-// DO WHILE(time < Tfinal) { COMPUTE_DT; three SSP-RK stages; bdy } on the
-// device, with the time loop's VTK movie frames (main.f90:119-143).
+// swe_main: the reference's main program (SOURCES/main.f90) written against
+// the C++ host interfaces (swe_update.hpp, swe_case.hpp) instead of the
+// Fortran modules.  Two modes:
+//
+//   swe_main --data FILE [--mesh FILE] [--steps K] [--precision 0|1]
+//            [--out state.bin]
+//     main.f90:19-91 for a reference data file: read_my_data,
+//     construct_mesh (the .FEM file named in it, relative to the data file's
+//     directory, or --mesh), construct_matrices, init, then
+//     DO WHILE(time < Tfinal) { COMPUTE_DT; three SSP-RK stages; bdy }, at
+//     most K steps.  Where the values bdy writes stay fixed over
+//     (t0, Tfinal] the loop runs on the device; where they change with time
+//     it runs here over the per-call euler / compute_dij, with bdy at the
+//     reference's stage times.
 //
 //   swe_main [--n N] [--tfinal T] [--precision 0|1] [--frames K --dir D]
 //            [--out state.bin]
+//     the unit-square dam break: N x N vertices on [0,1]^2, every cell cut
+//     along its SW->NE diagonal, vertices numbered x fastest; walls qx = 0
+//     on x = 0, 1 and qy = 0 on y = 0, 1 (Dirichlet, as bdy imposes); h = 1
+//     for x < 0.5, 0.1 elsewhere, q = 0; on the device, with the time loop's
+//     VTK movie frames (main.f90:119-143).
 //
-// Mesh: N x N vertices on [0,1]^2, every cell cut along its SW->NE diagonal,
-// vertices numbered x fastest; walls qx = 0 on x = 0, 1 and qy = 0 on
-// y = 0, 1 (Dirichlet, as bdy imposes); h = 1 for x < 0.5, 0.1 elsewhere,
-// q = 0.  Prints the steps, the final time and dt and the water mass; --out
-// writes the final un(3, np) as raw FP64 (column-major).
+// Prints the steps, the final time and dt and the water mass; --out writes
+// the final un(S, np) as raw FP64 (column-major).
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
 
+#include "../../include/swe_case.hpp"
 #include "../../include/swe_update.hpp"
 
 namespace {
@@ -50,12 +62,137 @@ Mesh lattice(int n) {
   return m;
 }
 
+bool write_state(const std::string& out, const std::vector<double>& un) {
+  if (out.empty()) return true;
+  FILE* f = std::fopen(out.c_str(), "wb");
+  if (!f || std::fwrite(un.data(), sizeof(double), un.size(), f) != un.size()) {
+    std::fprintf(stderr, "cannot write %s\n", out.c_str());
+    if (f) std::fclose(f);
+    return false;
+  }
+  std::fclose(f);
+  return true;
+}
+
+// main.f90:19-91 for a data file (see the header comment)
+int run_data(const std::string& data_path, std::string mesh_path, int max_steps, int precision,
+             const std::string& out) {
+  const swe::DataFile d = swe::read_my_data(data_path);
+  if (mesh_path.empty()) {
+    const size_t slash = data_path.find_last_of('/');
+    const std::string base = slash == std::string::npos ? "." : data_path.substr(0, slash);
+    mesh_path = base + "/" + d.directory + "/" + d.file_name;
+  }
+  const swe::FemMesh m = swe::load_mesh_free_format(mesh_path, d.list_dom);
+  const int tt = d.type_test, S = tt == 13 ? 5 : 3;
+  const swe::CaseInit ci = swe::init_case(tt, m, d.epsilon);
+  std::string visc = d.viscosity_type;
+  while (!visc.empty() && visc.back() == ' ') visc.pop_back();
+  swe_params p{};
+  p.gravity = ci.gravity; p.cfl = d.CFL; p.htiny = ci.htiny; p.mannings = d.mannings;
+  p.lambda_sgn = d.lambdaSGN; p.max_water_h = ci.max_water_h; p.type_test = tt; p.syst_size = S;
+  p.viscosity_type = visc == "galerkin" ? SWE_VISC_GALERKIN : visc == "viscous" ? SWE_VISC_VISCOUS
+                   : visc == "entropy_visc" ? SWE_VISC_ENTROPY : visc == "fct" ? SWE_VISC_FCT : -1;
+  if (p.viscosity_type < 0) throw swe::Stop(SWE_ERR_ARG, "viscosity type '" + visc + "'");
+  if (d.viscous_type != "type1" && d.viscous_type != "type2")
+    throw swe::Stop(SWE_ERR_ARG, "first-order viscosity '" + d.viscous_type + "'");
+  p.viscous_type = d.viscous_type == "type1" ? 1 : 2;
+  p.if_alpha_limit = d.if_alpha_limit; p.if_lumped = d.if_lumped; p.if_roundoff_fix = 1;
+  p.precision = precision;
+  const double t0 = ci.t0, tfinal = ci.sets_tfinal ? ci.tfinal : d.Tfinal;
+  // un(k,:) = sol_anal(k, rr, time) (condlim.f90:235-237)
+  std::vector<double> un((size_t)S * m.np), col(m.np);
+  for (int k = 1; k <= S; k++) {
+    swe::sol_anal(tt, k, m.np, m.rr.data(), t0, ci.bath.data(), ci.gravity, ci.htiny, col.data());
+    for (int i = 0; i < m.np; i++) un[(size_t)S * i + k - 1] = col[i];
+  }
+  // bdy (main.f90:176-188): h on h_js_D, qx on ux_js_D, qy on uy_js_D, and
+  // for type 13 the fourth and fifth unknowns on ux_js_D and uy_js_D
+  struct Bc { int comp; std::vector<int> js; std::vector<double> rr, val; };
+  std::vector<Bc> bcs;
+  const std::vector<int>* lists[3] = {&d.h_Dir_list, &d.ux_Dir_list, &d.uy_Dir_list};
+  for (int c = 0; c < (tt == 13 ? 5 : 3); c++) {
+    Bc b;
+    b.comp = c;
+    b.js = swe::dirichlet_nodes(m, *lists[c < 3 ? c : c - 2]);
+    if (b.js.empty()) continue;
+    for (int j : b.js) { b.rr.push_back(m.rr[2 * (size_t)(j - 1)]); b.rr.push_back(m.rr[2 * (size_t)(j - 1) + 1]); }
+    b.val.resize(b.js.size());
+    bcs.push_back(b);
+  }
+  auto bdy_values = [&](Bc& b, double t) {
+    swe::sol_anal(tt, b.comp + 1, (int)b.js.size(), b.rr.data(), t, ci.bath.data(), ci.gravity, ci.htiny,
+                  b.val.data());
+  };
+  // fixed over (t0, Tfinal]? the values at t0 + 1e-6 and at 16 times up to Tfinal
+  bool fixed = true;
+  for (Bc& b : bcs) {
+    std::vector<double> first;
+    for (int s = 0; s <= 16 && fixed; s++) {
+      const double t = s == 0 ? t0 + 1.e-6 : lin(t0, tfinal, 17, s);
+      try {
+        bdy_values(b, t);
+      } catch (const std::runtime_error&) {
+        fixed = false;
+        break;
+      }
+      if (s == 0) first = b.val;
+      else if (b.val != first) fixed = false;
+    }
+  }
+  swe::Update upd(m.np, m.me, m.jj.data(), m.rr.data(), ci.bath.data(), p);
+  double time = t0, dt = 0.0;
+  int steps = 0;
+  if (fixed) {
+    for (Bc& b : bcs) upd.set_dirichlet(b.comp, b.js, b.val);
+    while (steps < max_steps) {
+      const int chunk = std::min(64, max_steps - steps);
+      double t = time;
+      const int done = upd.rk3(un.data(), t, tfinal, chunk, &dt);
+      time = t;
+      steps += done;
+      if (done < chunk) break;
+    }
+  } else {                                                       // main.f90:61-91 over the per-call ABI
+    auto bdy = [&](std::vector<double>& uu, double t) {
+      for (Bc& b : bcs) {
+        bdy_values(b, t);
+        for (size_t q = 0; q < b.js.size(); q++) uu[(size_t)S * (b.js[q] - 1) + b.comp] = b.val[q];
+      }
+    };
+    std::vector<double> uo, ui(un.size()), dij(upd.nnz());
+    while (time < tfinal && steps < max_steps) {
+      dt = upd.compute_dij(un.data(), dij.data());               // COMPUTE_DT
+      p.dt = dt;
+      upd.set_inputs(p);
+      const double to = time;
+      uo = un;
+      upd.euler(uo.data(), un.data());
+      bdy(un, time + dt);
+      time = to + dt;
+      upd.euler(un.data(), ui.data());
+      for (size_t q = 0; q < un.size(); q++) un[q] = (3 * uo[q] + ui[q]) / 4;
+      bdy(un, time + dt / 2);
+      time = to + dt / 2;
+      upd.euler(un.data(), ui.data());
+      for (size_t q = 0; q < un.size(); q++) un[q] = (uo[q] + 2 * ui[q]) / 3;
+      bdy(un, time + dt);
+      time = to + dt;
+      steps++;
+    }
+    if (swe_upload(upd.context(), un.data()) != SWE_OK) throw swe::Stop(SWE_ERR_CUDA, "upload");
+  }
+  std::printf("type %d np %d %s steps %d time %.17g dt %.17g mass %.17g\n", tt, m.np,
+              fixed ? "device-loop" : "per-call", steps, time, dt, upd.total_mass());
+  return write_state(out, un) ? 0 : 1;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
-  int n = 101, precision = SWE_PREC_FP64, nb_frame = 0;
+  int n = 101, precision = SWE_PREC_FP64, nb_frame = 0, max_steps = 1 << 30;
   double tfinal = 0.2;
-  std::string out, dir = ".";
+  std::string out, dir = ".", data, mesh_file;
   for (int a = 1; a + 1 < argc; a += 2) {
     const std::string k = argv[a];
     if (k == "--n") n = std::atoi(argv[a + 1]);
@@ -64,7 +201,21 @@ int main(int argc, char** argv) {
     else if (k == "--frames") nb_frame = std::atoi(argv[a + 1]);
     else if (k == "--dir") dir = argv[a + 1];
     else if (k == "--out") out = argv[a + 1];
+    else if (k == "--data") data = argv[a + 1];
+    else if (k == "--mesh") mesh_file = argv[a + 1];
+    else if (k == "--steps") max_steps = std::atoi(argv[a + 1]);
     else { std::fprintf(stderr, "unknown option %s\n", k.c_str()); return 2; }
+  }
+  if (!data.empty()) {
+    try {
+      return run_data(data, mesh_file, max_steps, precision, out);
+    } catch (const swe::Stop& e) {   // the reference's WRITE + STOP
+      std::fprintf(stderr, "%s\n", e.what());
+      return 3;
+    } catch (const std::runtime_error& e) {
+      std::fprintf(stderr, "%s\n", e.what());
+      return 2;
+    }
   }
   if (n < 3 || !(tfinal > 0)) { std::fprintf(stderr, "need --n >= 3 and --tfinal > 0\n"); return 2; }
   const Mesh mesh = lattice(n);
@@ -123,15 +274,7 @@ int main(int argc, char** argv) {
       if (swe_download(upd.context(), un.data()) != SWE_OK) throw swe::Stop(SWE_ERR_CUDA, "download");
     }
     std::printf("steps %d time %.17g dt %.17g mass %.17g\n", steps, time, dt, upd.total_mass());
-    if (!out.empty()) {
-      FILE* f = std::fopen(out.c_str(), "wb");
-      if (!f || std::fwrite(un.data(), sizeof(double), un.size(), f) != un.size()) {
-        std::fprintf(stderr, "cannot write %s\n", out.c_str());
-        if (f) std::fclose(f);
-        return 1;
-      }
-      std::fclose(f);
-    }
+    if (!write_state(out, un)) return 1;
   } catch (const swe::Stop& e) {   // the reference's WRITE + STOP
     std::fprintf(stderr, "%s\n", e.what());
     return 3;

@@ -82,3 +82,40 @@ def test_cpp_update_interface_bit_exact(tmp_path):
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert sum(1 for line in r.stdout.splitlines() if line.startswith("ok ")) == 18, r.stdout
+
+
+@pytest.mark.parametrize("data,mesh,steps", [("ref_data_paraboloid.txt", "ref_cdisk.1_mesh.FEM.gz", 10),
+                                             ("ref_data_sources.txt", "ref_rectangle.1.FEM.gz", 6)])
+def test_driver_runs_a_reference_data_file(tmp_path, golden, data, mesh, steps):
+    """swe_main --data: main.f90 for a reference data file in C++
+    (read_my_data, the .FEM reader, init, the Dirichlet lists and bdy) equals
+    the Python host side's run of the same data file bit for bit.
+    PARABOLOID/data (type 12, 'viscous', dry rim) runs the device loop;
+    SOURCES/data (type 13, 'entropy_visc', h at the channel ends moving with
+    the wave) runs main.f90's loop over the per-call euler."""
+    import gzip
+    from swe import data as D, mesh as M, refcases as R
+    L.load()
+    fem = tmp_path / "mesh.FEM"
+    fem.write_bytes(gzip.decompress((golden / mesh).read_bytes()))
+    out = tmp_path / "state.bin"
+    r = subprocess.run([str(B.DRIVER), "--data", str(golden / data), "--mesh", str(fem), "--steps", str(steps),
+                        "--out", str(out)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    d = D.read_my_data(golden / data)
+    case = R.case_from_data(d, M.load_mesh_free_format(fem, d["list_dom"]))
+    if case.bdy_fixed:
+        upd = from_case(case)
+        upd.upload(case.u0)
+        upd.set_time(case.t0, case.tfinal)
+        t, _, n = upd.rk3_steps(steps)
+        u, t = upd.download(), t[0]
+        assert "device-loop" in r.stdout
+    else:
+        upd = from_case(case, per_call=True)
+        u, t, n = R.host_time_loop(R.PerCall(upd), case.bdy, case.u0, case.t0, case.tfinal, steps)
+        assert "per-call" in r.stdout
+    upd.close()
+    got = np.fromfile(out, np.float64).reshape(u.shape, order="F")
+    np.testing.assert_array_equal(got, u)
+    assert f"steps {n} time {t!r}" in r.stdout or f"steps {n} time {t:.17g}" in r.stdout
