@@ -88,14 +88,18 @@ def _build_driver():
     """swe_main (csrc/swe_main.cpp): the reference's main program (a data
     file's run, or the dam break) over the C++ host interfaces
     include/swe_update.hpp and include/swe_case.hpp (csrc/swe_case.cpp),
-    linked against the library next to it."""
+    linked against the library next to it.  No FMA contraction (g++
+    contracts a*b + c on aarch64 by default): its host arithmetic (init,
+    sol_anal, the RK combinations of the per-call loop) follows the
+    reference's evaluation order like the Python host side."""
     src = CSRC / "swe_main.cpp"
     case_src = CSRC / "swe_case.cpp"
     deps = [src, case_src, LIB, INCLUDE / "swe_update.hpp", INCLUDE / "swe_case.hpp", INCLUDE / "swe_gpu.h"]
     if DRIVER.exists() and DRIVER.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
         return DRIVER
     tmp = DRIVER.with_name(f"swe_main.{os.getpid()}")
-    cmd = ["g++", "-O2", "-std=c++17", f"-I{INCLUDE}", str(src), str(case_src), f"-L{LIB.parent}", "-lswe_gpu",
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", f"-I{INCLUDE}", str(src), str(case_src),
+           f"-L{LIB.parent}", "-lswe_gpu",
            "-Wl,-rpath,$ORIGIN", "-o", str(tmp)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

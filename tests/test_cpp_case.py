@@ -21,7 +21,7 @@ REPO = HERE.parent
 @pytest.fixture(scope="module")
 def dump_case(tmp_path_factory):
     out = tmp_path_factory.mktemp("cpp") / "dump_case"
-    cmd = ["g++", "-O2", "-std=c++17", f"-I{REPO / 'include'}", str(HERE / "cpp" / "dump_case.cpp"),
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", f"-I{REPO / 'include'}", str(HERE / "cpp" / "dump_case.cpp"),
            str(REPO / "shallow-water-eric_gb300" / "csrc" / "swe_case.cpp"), "-o", str(out)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr

@@ -75,7 +75,7 @@ def test_cpp_update_interface_bit_exact(tmp_path):
     olib = oracle.build()
     here = Path(__file__).resolve().parent
     exe = tmp_path / "test_update_parity"
-    cmd = ["g++", "-O2", "-std=c++17", f"-I{here.parent / 'include'}", str(here / "cpp" / "test_update_parity.cpp"),
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", f"-I{here.parent / 'include'}", str(here / "cpp" / "test_update_parity.cpp"),
            f"-L{B.LIB.parent}", "-lswe_gpu", f"-Wl,-rpath,{B.LIB.parent}", f"-L{olib.parent}", "-lswe_oracle",
            f"-Wl,-rpath,{olib.parent}", "-o", str(exe)]
     subprocess.run(cmd, check=True, capture_output=True, text=True)
