@@ -3,7 +3,7 @@
 // Fortran modules.  Two modes:
 //
 //   swe_main --data FILE [--mesh FILE] [--steps K] [--precision 0|1]
-//            [--out state.bin]
+//            [--frames K --dir D] [--out state.bin]
 //     main.f90:19-91 for a reference data file: read_my_data,
 //     construct_mesh (the .FEM file named in it, relative to the data file's
 //     directory, or --mesh), construct_matrices, init, then
@@ -11,7 +11,10 @@
 //     most K steps.  Where the values bdy writes stay fixed over
 //     (t0, Tfinal] the loop runs on the device; where they change with time
 //     it runs here over the per-call euler / compute_dij, with bdy at the
-//     reference's stage times.
+//     reference's stage times.  The loop's movie frames are written as
+//     main.f90 writes them (nb_frame = 200 unless --frames says otherwise;
+//     --frames 0 writes none), and compute_errors' relative L1 / L2 errors
+//     on h are printed for the types that have an exact solution.
 //
 //   swe_main [--n N] [--tfinal T] [--precision 0|1] [--frames K --dir D]
 //            [--out state.bin]
@@ -23,6 +26,8 @@
 //
 // Prints the steps, the final time and dt and the water mass; --out writes
 // the final un(S, np) as raw FP64 (column-major).
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -76,7 +81,7 @@ bool write_state(const std::string& out, const std::vector<double>& un) {
 
 // main.f90:19-91 for a data file (see the header comment)
 int run_data(const std::string& data_path, std::string mesh_path, int max_steps, int precision,
-             const std::string& out) {
+             const std::string& out, int nb_frame, const std::string& dir) {
   const swe::DataFile d = swe::read_my_data(data_path);
   if (mesh_path.empty()) {
     const size_t slash = data_path.find_last_of('/');
@@ -143,8 +148,56 @@ int run_data(const std::string& data_path, std::string mesh_path, int max_steps,
   swe::Update upd(m.np, m.me, m.jj.data(), m.rr.data(), ci.bath.data(), p);
   double time = t0, dt = 0.0;
   int steps = 0;
+  // movie frames (main.f90:42-47, 119-143): types 5, 8, 9, 11, 12, 13 every
+  // Tfinal/(nb_frame-1), starting with the first step; type 3 writes frames
+  // too but never sets dt_frame (zero): a frame after every step
+  const bool frame_type = tt == 5 || tt == 8 || tt == 9 || tt == 11 || tt == 12 || tt == 13;
+  const bool movie = nb_frame > 1 && (frame_type || tt == 3);
+  double hmax0 = 0.0;
+  for (int i = 0; i < m.np; i++) hmax0 = std::max(hmax0, un[(size_t)S * i]);
+  double dt_frame = 0.0, t_frame = 0.0;
+  int kit = 0;
+  auto vtk = [&](const std::string& name, const std::string& title, const std::vector<double>& f) {
+    const std::string path = dir + "/" + name;
+    if (swe_write_vtk_2d(path.c_str(), title.c_str(), m.np, m.me, m.jj.data(), m.rr.data(), f.data()) != SWE_OK)
+      throw swe::Stop(SWE_ERR_ARG, "cannot write " + path);
+  };
+  if (movie && frame_type) {
+    dt_frame = tfinal / (nb_frame - 1);
+    vtk("bath.vtk", "bath.vtk", ci.bath);
+    std::vector<double> hex(m.np);
+    swe::sol_anal(tt, 1, m.np, m.rr.data(), tfinal, ci.bath.data(), ci.gravity, ci.htiny, hex.data());
+    vtk("hexact.vtk", "hexact.vtk", hex);
+  }
+  auto frame_due = [&]() {
+    if (!movie || !(0.0 <= time) || !(time >= t_frame - 1.e-10)) return std::string();
+    kit++;
+    t_frame += dt_frame;
+    return kit < 1000 ? std::to_string(kit) : std::string("***");   // WRITE(frame,'(I3)') kit
+  };
   if (fixed) {
     for (Bc& b : bcs) upd.set_dirichlet(b.comp, b.js, b.val);
+  }
+  if (fixed && movie) {                                          // a step at a time, frames from the device
+    if (swe_upload(upd.context(), un.data()) != SWE_OK) throw swe::Stop(SWE_ERR_CUDA, "upload");
+    if (swe_set_time(upd.context(), &time, &tfinal) != SWE_OK) throw swe::Stop(SWE_ERR_ARG, "set_time");
+    while (time < tfinal && steps < max_steps) {
+      int done = 0;
+      const int rc = swe_rk3_steps(upd.context(), 1, &time, &dt, &done);
+      if (rc != SWE_OK) throw swe::Stop(rc, swe_last_error(upd.context()));
+      if (!done) break;
+      steps += done;
+      const std::string k = frame_due();
+      if (!k.empty()) {
+        const std::string a = dir + "/hpz_" + k + ".vtk", b = dir + "/h_" + k + ".vtk";
+        const int fr = swe_frame_async(upd.context(), 0, hmax0, a.c_str(), b.c_str());
+        if (fr != SWE_OK) throw swe::Stop(fr, swe_last_error(upd.context()));
+      }
+    }
+    const int fw = swe_frames_wait(upd.context());
+    if (fw != SWE_OK) throw swe::Stop(fw, swe_last_error(upd.context()));
+    if (swe_download(upd.context(), un.data()) != SWE_OK) throw swe::Stop(SWE_ERR_CUDA, "download");
+  } else if (fixed) {
     while (steps < max_steps) {
       const int chunk = std::min(64, max_steps - steps);
       double t = time;
@@ -179,11 +232,40 @@ int run_data(const std::string& data_path, std::string mesh_path, int max_steps,
       bdy(un, time + dt);
       time = to + dt;
       steps++;
+      const std::string k = frame_due();
+      if (!k.empty()) {                                          // the frame fields of main.f90:124-141
+        std::vector<double> hpz(m.np), h(m.np);
+        for (int i = 0; i < m.np; i++) {
+          const double hi = un[(size_t)S * i];
+          const bool dry = hi <= 1.e-4 * hmax0;
+          hpz[i] = dry ? -1.e-7 * hmax0 + ci.bath[i] : hi + ci.bath[i];
+          h[i] = dry ? 0.0 : hi;
+        }
+        const std::string a = "hpz_" + k + ".vtk", b = "h_" + k + ".vtk";
+        vtk(a, std::string(a).append(200 - a.size(), ' '), hpz);
+        vtk(b, std::string(b).append(200 - b.size(), ' '), h);
+      }
     }
     if (swe_upload(upd.context(), un.data()) != SWE_OK) throw swe::Stop(SWE_ERR_CUDA, "upload");
   }
   std::printf("type %d np %d %s steps %d time %.17g dt %.17g mass %.17g\n", tt, m.np,
               fixed ? "device-loop" : "per-call", steps, time, dt, upd.total_mass());
+  // compute_errors (main.f90:198-263): relative L1 and L2 errors on h at the
+  // Gauss points against sol_anal(1, r_gauss, time), on the device state
+  if (tt == 3 || tt == 4 || tt == 5 || tt == 6 || tt == 7 || tt == 11 || tt == 12 || tt == 13) {
+    std::vector<double> rj(3 * (size_t)m.me), rg(6 * (size_t)m.me), fa(3 * (size_t)m.me);
+    if (swe_gauss_points(upd.context(), 0, rj.data(), rg.data()) != SWE_OK)
+      throw swe::Stop(SWE_ERR_CUDA, swe_last_error(upd.context()));
+    swe::sol_anal(tt, 1, 3 * m.me, rg.data(), time, ci.bath.data(), ci.gravity, ci.htiny, fa.data());
+    double e1 = 0.0, e2 = 0.0, n1 = 0.0, n2 = 0.0;
+    if (swe_norms(upd.context(), 0, 0, fa.data(), &e1, &e2) != SWE_OK)
+      throw swe::Stop(SWE_ERR_CUDA, swe_last_error(upd.context()));
+    for (size_t q = 0; q < fa.size(); q++) { n1 += std::fabs(fa[q]) * rj[q]; n2 += fa[q] * fa[q] * rj[q]; }
+    n2 = std::sqrt(n2);
+    std::printf(" Total number of elements %d\n Total number of points   %d\n", m.me, m.np);
+    std::printf(" Relative L1 error on h (Gaussian) %.17g\n Relative L2 error on h (Gaussian) %.17g\n", e1 / n1,
+                e2 / n2);
+  }
   return write_state(out, un) ? 0 : 1;
 }
 
@@ -191,6 +273,7 @@ int run_data(const std::string& data_path, std::string mesh_path, int max_steps,
 
 int main(int argc, char** argv) {
   int n = 101, precision = SWE_PREC_FP64, nb_frame = 0, max_steps = 1 << 30;
+  bool nb_frame_set = false;
   double tfinal = 0.2;
   std::string out, dir = ".", data, mesh_file;
   for (int a = 1; a + 1 < argc; a += 2) {
@@ -198,7 +281,7 @@ int main(int argc, char** argv) {
     if (k == "--n") n = std::atoi(argv[a + 1]);
     else if (k == "--tfinal") tfinal = std::atof(argv[a + 1]);
     else if (k == "--precision") precision = std::atoi(argv[a + 1]);
-    else if (k == "--frames") nb_frame = std::atoi(argv[a + 1]);
+    else if (k == "--frames") { nb_frame = std::atoi(argv[a + 1]); nb_frame_set = true; }
     else if (k == "--dir") dir = argv[a + 1];
     else if (k == "--out") out = argv[a + 1];
     else if (k == "--data") data = argv[a + 1];
@@ -208,7 +291,7 @@ int main(int argc, char** argv) {
   }
   if (!data.empty()) {
     try {
-      return run_data(data, mesh_file, max_steps, precision, out);
+      return run_data(data, mesh_file, max_steps, precision, out, nb_frame_set ? nb_frame : 200, dir);
     } catch (const swe::Stop& e) {   // the reference's WRITE + STOP
       std::fprintf(stderr, "%s\n", e.what());
       return 3;

@@ -100,7 +100,7 @@ def test_driver_runs_a_reference_data_file(tmp_path, golden, data, mesh, steps):
     fem.write_bytes(gzip.decompress((golden / mesh).read_bytes()))
     out = tmp_path / "state.bin"
     r = subprocess.run([str(B.DRIVER), "--data", str(golden / data), "--mesh", str(fem), "--steps", str(steps),
-                        "--out", str(out)], capture_output=True, text=True, timeout=300)
+                        "--frames", "0", "--out", str(out)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     d = D.read_my_data(golden / data)
     case = R.case_from_data(d, M.load_mesh_free_format(fem, d["list_dom"]))
@@ -119,3 +119,56 @@ def test_driver_runs_a_reference_data_file(tmp_path, golden, data, mesh, steps):
     got = np.fromfile(out, np.float64).reshape(u.shape, order="F")
     np.testing.assert_array_equal(got, u)
     assert f"steps {n} time {t!r}" in r.stdout or f"steps {n} time {t:.17g}" in r.stdout
+
+
+@pytest.mark.parametrize("data,mesh", [("ref_data_paraboloid.txt", "ref_cdisk.1_mesh.FEM.gz"),
+                                       ("ref_data_sources.txt", "ref_rectangle.1.FEM.gz")])
+def test_driver_data_file_frames_and_errors(tmp_path, golden, data, mesh):
+    """swe_main --data writes main.f90's files for a run with frames
+    (bath.vtk, hexact.vtk = sol_anal(1, rr, Tfinal), then hpz_k / h_k after
+    the first step, the next one Tfinal/(nb_frame-1) later) with the
+    reference's text, from the device state (device loop) or the host state
+    (per-call loop), and prints compute_errors' relative L1 / L2 errors on h
+    at the Gauss points."""
+    import gzip
+    from swe import data as D, mesh as M, refcases as R
+    L.load()
+    fem = tmp_path / "mesh.FEM"
+    fem.write_bytes(gzip.decompress((golden / mesh).read_bytes()))
+    r = subprocess.run([str(B.DRIVER), "--data", str(golden / data), "--mesh", str(fem), "--steps", "2",
+                        "--frames", "3", "--dir", str(tmp_path)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    d = D.read_my_data(golden / data)
+    m = M.load_mesh_free_format(fem, d["list_dom"])
+    case = R.case_from_data(d, m)
+    jj, rr = m["jj"], m["rr"]
+    assert sorted(p.name for p in tmp_path.glob("*.vtk")) == ["bath.vtk", "h_1.vtk", "hexact.vtk", "hpz_1.vtk"]
+    assert (tmp_path / "bath.vtk").read_text() == oracle.vtk_2d_text("bath.vtk", jj, rr, case.bath)
+    hex_ = case.exact(1, rr, case.tfinal)
+    assert (tmp_path / "hexact.vtk").read_text() == oracle.vtk_2d_text("hexact.vtk", jj, rr, hex_)
+    hmax0 = case.u0[0].max()
+    upd = from_case(case, per_call=not case.bdy_fixed)
+    if case.bdy_fixed:
+        upd.upload(case.u0)
+        upd.set_time(case.t0, case.tfinal)
+        upd.rk3_steps(1)
+        u1 = upd.download()
+        upd.rk3_steps(1)
+        t = upd.get_time()[0][0]
+    else:
+        u1, t1, _ = R.host_time_loop(R.PerCall(upd), case.bdy, case.u0, case.t0, case.tfinal, 1)
+        u2, t, _ = R.host_time_loop(R.PerCall(upd), case.bdy, u1, t1, case.tfinal, 1)
+        upd.upload(u2)
+    hpz, h = oracle.frame_fields(u1[0], case.bath, hmax0)
+    for name, f in (("hpz_1.vtk", hpz), ("h_1.vtk", h)):
+        assert (tmp_path / name).read_text() == oracle.vtk_2d_text(name.ljust(200), jj, rr, f)
+    rj, rg = upd.gauss_points()
+    fa = case.exact(1, rg, t)
+    e1, e2 = upd.norms(0, fa)
+    n1, n2 = np.sum(np.abs(fa) * rj), np.sqrt(np.sum(fa * fa * rj))
+    got = {ln.split(" (Gaussian) ")[0].strip(): float(ln.split()[-1]) for ln in r.stdout.splitlines()
+           if "(Gaussian)" in ln}
+    assert got["Relative L1 error on h"] == pytest.approx(e1 / n1, rel=1e-12)
+    assert got["Relative L2 error on h"] == pytest.approx(e2 / n2, rel=1e-12)
+    upd.close()
+
