@@ -89,7 +89,6 @@ def test_critical_bump_jump_conserves_momentum_flux():
     eps = 1e-9
     rr = np.array([[xs - eps, xs + eps, 5.0, 11.0], [0.0, 0.0, 0.0, 0.0]])
     h = R.sol_anal(7, 1, rr, 1.0, None, g, 2e-4)
-    zpre, zpost = R._bump(np.array([xs - eps, xs + eps]))
     M = lambda d: q0 ** 2 / d + g * d ** 2 / 2
     assert M(h[0]) == pytest.approx(M(h[1]), rel=1e-6)
     assert h[0] < (q0 ** 2 / g) ** (1 / 3) < h[1]                # super- then subcritical
