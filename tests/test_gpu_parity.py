@@ -838,3 +838,26 @@ def test_time_dependent_dirichlet_through_per_call_euler(golden):
     assert (ng, tg) == (nw, tw) == (8, tw)
     np.testing.assert_array_equal(got, want)
     upd.close()
+
+
+def test_degenerate_meshes_are_refused():
+    """An empty mesh, an element node number out of range, a node that no
+    element touches (zero lumped mass, which the reference would divide by)
+    and a clockwise triangle are refused with an error status when the
+    matrices are built; the device set-up checks every index before it
+    reads through it."""
+    p = C.Params(type_test=4)
+    tri = np.asfortranarray(np.array([[0.0, 1.0, 0.0], [0.0, 0.0, 1.0]]))
+    four = np.asfortranarray(np.array([[0.0, 1.0, 0.0, 2.0], [0.0, 0.0, 1.0, 2.0]]))
+    cases = [(np.zeros((3, 0), np.int32), tri, L.SWE_ERR_ARG, "empty mesh"),
+             (np.array([[1], [2], [4]], np.int32), tri, L.SWE_ERR_MESH, "out of range"),
+             (np.array([[1], [2], [0]], np.int32), tri, L.SWE_ERR_MESH, "out of range"),
+             (np.array([[1], [2], [3]], np.int32), four, L.SWE_ERR_MESH, "lumped mass"),
+             (np.array([[1], [3], [2]], np.int32), tri, L.SWE_ERR_MESH, "lumped mass")]
+    for jj, rr, code, msg in cases:
+        mesh = {"jj": np.asfortranarray(jj), "rr": rr}
+        with pytest.raises(L.SweError, match=msg) as ei:
+            Update(mesh, np.zeros(rr.shape[1]), p)
+        assert ei.value.code == code
+    ok = Update({"jj": np.asfortranarray(np.array([[1], [2], [3]], np.int32)), "rr": tri}, np.zeros(3), p)
+    ok.close()
