@@ -228,11 +228,15 @@ FemMesh load_mesh_free_format(const std::string& path, const std::vector<int>& l
         if (v != jjs0[2 * (size_t)s] && v != jjs0[2 * (size_t)s + 1]) break;
       }
       const int m2 = neigh0[3 * (size_t)(m1 - 1) + (n < 3 ? n : 2)];
+      if (m2 < 0 || m2 > me0) fail("neighbour element out of range in .FEM file");
       ok = m2 != 0 && in_dom(m2);
     }
     if (!ok) continue;
-    m.jjs.push_back(nouv_nd[jjs0[2 * (size_t)s]]);
-    m.jjs.push_back(nouv_nd[jjs0[2 * (size_t)s + 1]]);
+    for (int q = 0; q < 2; q++) {
+      const int v = jjs0[2 * (size_t)s + q];
+      if (v < 1 || v > np0) fail("side node out of range in .FEM file");
+      m.jjs.push_back(nouv_nd[v]);
+    }
     m.sides.push_back(sides0[s]);
   }
   m.mes = (int)m.sides.size();
