@@ -9,7 +9,6 @@
 #include <cstdint>
 #include <cstring>
 #include <fstream>
-#include <sstream>
 #include <stdexcept>
 
 namespace swe {
@@ -181,6 +180,7 @@ FemMesh load_mesh_free_format(const std::string& path, const std::vector<int>& l
   std::memcpy(hd, &buf[rec[0].first], 20);
   const int np0 = hd[0], nw = hd[1], me0 = hd[2], nws = hd[3], mes0 = hd[4];
   if (nw != 3 || nws != 2) fail("only P1 triangle meshes are supported");
+  if (np0 <= 0 || me0 <= 0 || mes0 < 0) fail("bad sizes in .FEM file header");
   auto ints = [&](int r, size_t count) {
     if (rec[r].second < count * 4) fail("short record in .FEM file");
     std::vector<int32_t> v(count);
