@@ -14,7 +14,8 @@
 //     reference's stage times.  The loop's movie frames are written as
 //     main.f90 writes them (nb_frame = 200 unless --frames says otherwise;
 //     --frames 0 writes none), and compute_errors' relative L1 / L2 errors
-//     on h are printed for the types that have an exact solution.
+//     on h are printed for the types that have an exact solution; types 1
+//     and 2 write the loop's monitor to fort.10.
 //
 //   swe_main [--n N] [--tfinal T] [--precision 0|1] [--frames K --dir D]
 //            [--out state.bin]
@@ -175,10 +176,28 @@ int run_data(const std::string& data_path, std::string mesh_path, int max_steps,
     t_frame += dt_frame;
     return kit < 1000 ? std::to_string(kit) : std::string("***");   // WRITE(frame,'(I3)') kit
   };
+  // the monitor of main.f90:94-99 for types 1 and 2: time and
+  // 0.5 (|qx|_1 + |qy|_1) / (g |h^(3/2)|_1) after every step, into fort.10
+  // (the unit it WRITEs to), from the device state
+  FILE* mon = nullptr;
+  if (tt == 1 || tt == 2) {
+    const std::string path = dir + "/fort.10";
+    mon = std::fopen(path.c_str(), "w");
+    if (!mon) throw swe::Stop(SWE_ERR_ARG, "cannot write " + path);
+  }
+  auto monitor = [&]() {
+    if (!mon) return;
+    double q1 = 0.0, q2 = 0.0, q3 = 0.0;
+    if (swe_norms(upd.context(), 0, 1, nullptr, &q1, nullptr) != SWE_OK ||
+        swe_norms(upd.context(), 0, 2, nullptr, &q2, nullptr) != SWE_OK ||
+        swe_norms(upd.context(), 0, SWE_FIELD_H32, nullptr, &q3, nullptr) != SWE_OK)
+      throw swe::Stop(SWE_ERR_CUDA, swe_last_error(upd.context()));
+    std::fprintf(mon, "%.17g %.17g\n", time, 0.5 * (q1 + q2) / (ci.gravity * q3));
+  };
   if (fixed) {
     for (Bc& b : bcs) upd.set_dirichlet(b.comp, b.js, b.val);
   }
-  if (fixed && movie) {                                          // a step at a time, frames from the device
+  if (fixed && (movie || mon)) {                                 // a step at a time: frames, monitor
     if (swe_upload(upd.context(), un.data()) != SWE_OK) throw swe::Stop(SWE_ERR_CUDA, "upload");
     if (swe_set_time(upd.context(), &time, &tfinal) != SWE_OK) throw swe::Stop(SWE_ERR_ARG, "set_time");
     while (time < tfinal && steps < max_steps) {
@@ -187,6 +206,7 @@ int run_data(const std::string& data_path, std::string mesh_path, int max_steps,
       if (rc != SWE_OK) throw swe::Stop(rc, swe_last_error(upd.context()));
       if (!done) break;
       steps += done;
+      monitor();
       const std::string k = frame_due();
       if (!k.empty()) {
         const std::string a = dir + "/hpz_" + k + ".vtk", b = dir + "/h_" + k + ".vtk";
@@ -232,6 +252,10 @@ int run_data(const std::string& data_path, std::string mesh_path, int max_steps,
       bdy(un, time + dt);
       time = to + dt;
       steps++;
+      if (mon) {
+        if (swe_upload(upd.context(), un.data()) != SWE_OK) throw swe::Stop(SWE_ERR_CUDA, "upload");
+        monitor();
+      }
       const std::string k = frame_due();
       if (!k.empty()) {                                          // the frame fields of main.f90:124-141
         std::vector<double> hpz(m.np), h(m.np);
@@ -248,6 +272,7 @@ int run_data(const std::string& data_path, std::string mesh_path, int max_steps,
     }
     if (swe_upload(upd.context(), un.data()) != SWE_OK) throw swe::Stop(SWE_ERR_CUDA, "upload");
   }
+  if (mon) std::fclose(mon);
   std::printf("type %d np %d %s steps %d time %.17g dt %.17g mass %.17g\n", tt, m.np,
               fixed ? "device-loop" : "per-call", steps, time, dt, upd.total_mass());
   // compute_errors (main.f90:198-263): relative L1 and L2 errors on h at the

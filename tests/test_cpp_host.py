@@ -172,3 +172,73 @@ def test_driver_data_file_frames_and_errors(tmp_path, golden, data, mesh):
     assert got["Relative L2 error on h"] == pytest.approx(e2 / n2, rel=1e-12)
     upd.close()
 
+
+
+_DATA_TYPE2 = """===Name of directory for mesh file===
+'.'
+===Name of mesh file===
+mesh.FEM
+===Test case number===
+2
+===Final time===
+10.
+===CFL number===
+.25d0
+===Viscosity type (galerkin, viscous, entropy_visc, fct)===
+'fct'
+===Type of first-order viscosity===
+'type2'
+===Alpha limitation? (True/False)===
+.t.
+===Lumping the mass matrix? (true/false)===
+.t.
+===How many Dirichlet boundaries for h?===
+0
+===List of Dirichlet boundaries for h?===
+1
+===How many Dirichlet boundaries for ux?===
+2
+===List of Dirichlet boundaries for ux?===
+1 3
+===How many Dirichlet boundaries for uy?===
+2
+===List of Dirichlet boundaries for uy?===
+2 4
+===Number of subdomains in the mesh===
+1
+===List of subdomain in the mesh===
+1
+===Type of finite element===
+1
+"""
+
+
+def test_driver_monitor_of_types_1_and_2(tmp_path, golden):
+    """Type 2 (lake at rest over the bump of BUMP_3_1/cav_0.3, walls): the
+    driver finds the mesh next to its data file, runs the device loop a step
+    at a time and writes main.f90's monitor, time and
+    0.5 (|qx|_1 + |qy|_1) / (g |h^(3/2)|_1), to fort.10 after every step,
+    equal to the same norms taken through the Python host side."""
+    import gzip
+    from swe import data as D, mesh as M, refcases as R
+    L.load()
+    (tmp_path / "mesh.FEM").write_bytes(gzip.decompress((golden / "ref_bump_cav_0.3.FEM.gz").read_bytes()))
+    (tmp_path / "data").write_text(_DATA_TYPE2)
+    r = subprocess.run([str(B.DRIVER), "--data", str(tmp_path / "data"), "--steps", "5", "--dir", str(tmp_path)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    rows = [tuple(float(v) for v in ln.split()) for ln in (tmp_path / "fort.10").read_text().splitlines()]
+    d = D.read_my_data(tmp_path / "data")
+    case = R.case_from_data(d, M.load_mesh_free_format(tmp_path / "mesh.FEM", d["list_dom"]))
+    assert case.bdy_fixed
+    upd = from_case(case)
+    upd.upload(case.u0)
+    upd.set_time(case.t0, case.tfinal)
+    want = []
+    for _ in range(5):
+        t, _, _ = upd.rk3_steps(1)
+        q1, q2, q3 = upd.norms(1)[0], upd.norms(2)[0], upd.norms(L.FIELD_H32)[0]
+        want.append((t[0], 0.5 * (q1 + q2) / (case.params.gravity * q3)))
+    upd.close()
+    assert rows == want
+    assert not list(tmp_path.glob("*.vtk"))          # type 2 writes no frames
