@@ -82,6 +82,8 @@ struct swe_ctx {
   double* d_norm_acc = nullptr;
   double* d_fanal = nullptr;
   size_t fanal_cap = 0;
+  double* d_norm_part = nullptr;     // per-warp partial sums of k_norms
+  size_t norm_part_cap = 0;
   // graph of `graph_steps` time steps
   cudaGraphExec_t gexec = nullptr;
   int graph_steps = 0;
@@ -1032,12 +1034,17 @@ SWE_API int swe_norms(swe_ctx* c, int inst, int field, const double* f_anal, dou
     c->d_fanal = c->buf.alloc<double>((size_t)3 * m.me, st);
     c->fanal_cap = (size_t)3 * m.me;
   }
+  const size_t nparts = 4 * (size_t)norm_partials(m.me);
+  if (c->norm_part_cap < nparts) {
+    c->d_norm_part = c->buf.alloc<double>(nparts, st);
+    c->norm_part_cap = nparts;
+  }
   if (st != cudaSuccess) return cuda_check(c, st, "swe_norms allocation");
   if (f_anal)
     CK(cudaMemcpyAsync(c->d_fanal, f_anal, (size_t)3 * m.me * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  CK(cudaMemsetAsync(c->d_norm_acc, 0, 4 * sizeof(double), c->stream));
   launch_norms(field, c->precision == SWE_PREC_FP64 ? 0 : 1, c->A, c->mA, c->d_jj_inst[inst], c->d_rj_inst[inst],
-               m.me, c->d_row_of_node + c->node_off[inst], f_anal ? c->d_fanal : nullptr, c->d_norm_acc, c->stream);
+               m.me, c->d_row_of_node + c->node_off[inst], f_anal ? c->d_fanal : nullptr, c->d_norm_part,
+               c->d_norm_acc, c->stream);
   CK(cudaGetLastError());
   double acc[4];
   CK(cudaMemcpyAsync(acc, c->d_norm_acc, sizeof acc, cudaMemcpyDeviceToHost, c->stream));

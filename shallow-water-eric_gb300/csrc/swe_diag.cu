@@ -7,8 +7,9 @@
 // One thread per element interpolates the field at the three Gauss points
 // (the same expression as the reference, sum_n f(jj(n,m)) ww(n,l)) and adds
 // |f - f_anal| rj and (f - f_anal)^2 rj; the sums are combined per warp in
-// double-double and accumulated with atomics, so they equal the reference's
-// sequential sums to rounding (order-independent to ~1e-16 relative).
+// double-double, and the warps' partial sums are added by one block in a
+// fixed order: equal to the reference's sequential sums to rounding, and the
+// same bits on every call.
 #include "swe_kernels.hpp"
 
 namespace swe {
@@ -59,10 +60,18 @@ __device__ __forceinline__ void dd_warp_sum(double& v, double& c) {
   }
 }
 
-// acc[0..1]: L1 sum (hi, lo); acc[2..3]: L2 sum of squares (hi, lo)
+__device__ __forceinline__ void dd_add(double& v, double& c, double o, double oc) {
+  const double s = v + o;               // two-sum
+  const double bb = s - v;
+  const double e = (v - (s - bb)) + (o - bb);
+  v = s;
+  c = c + oc + e;
+}
+
+// part[4 w + 0..3], per warp w: L1 sum (hi, lo), L2 sum of squares (hi, lo)
 __global__ void k_norms(DiagField f, const int* __restrict__ jj, const double* __restrict__ rj, int me,
                         const int* __restrict__ row_of_node, const double* __restrict__ f_anal,
-                        double* __restrict__ acc) {
+                        double* __restrict__ part) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   double t1 = 0.0, t2 = 0.0;
   if (m < me) {
@@ -85,17 +94,46 @@ __global__ void k_norms(DiagField f, const int* __restrict__ jj, const double* _
   dd_warp_sum(t1, c1);
   dd_warp_sum(t2, c2);
   if ((threadIdx.x & 31) == 0) {
-    atomicAdd(&acc[0], t1);
-    atomicAdd(&acc[1], c1);
-    atomicAdd(&acc[2], t2);
-    atomicAdd(&acc[3], c2);
+    const size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    part[4 * w + 0] = t1;
+    part[4 * w + 1] = c1;
+    part[4 * w + 2] = t2;
+    part[4 * w + 3] = c2;
   }
 }
 
+// One block of kNormThreads: thread t adds the partials t, t + kNormThreads,
+// ... in order, the warps combine by the fixed shuffle tree, thread 0 adds
+// the warps in order into acc[0..3].
+constexpr int kNormThreads = 256;
+
+__global__ void __launch_bounds__(kNormThreads) k_norms_final(const double* __restrict__ part, int64_t nw,
+                                                              double* __restrict__ acc) {
+  double v1 = 0.0, c1 = 0.0, v2 = 0.0, c2 = 0.0;
+  for (int64_t w = threadIdx.x; w < nw; w += kNormThreads) {
+    dd_add(v1, c1, part[4 * w + 0], part[4 * w + 1]);
+    dd_add(v2, c2, part[4 * w + 2], part[4 * w + 3]);
+  }
+  dd_warp_sum(v1, c1);
+  dd_warp_sum(v2, c2);
+  __shared__ double sw[kNormThreads / 32][4];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) { sw[warp][0] = v1; sw[warp][1] = c1; sw[warp][2] = v2; sw[warp][3] = c2; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a1 = 0.0, b1 = 0.0, a2 = 0.0, b2 = 0.0;
+    for (int k = 0; k < kNormThreads / 32; k++) { dd_add(a1, b1, sw[k][0], sw[k][1]); dd_add(a2, b2, sw[k][2], sw[k][3]); }
+    acc[0] = a1; acc[1] = b1; acc[2] = a2; acc[3] = b2;
+  }
+}
+
+int64_t norm_partials(int me) { return (int64_t)((me + 255) / 256) * (256 / 32); }
+
 void launch_norms(int field, int precision, const StateF64& a, const StateMix& mx, const int* jj, const double* rj,
-                  int me, const int* row_of_node, const double* f_anal, double* acc, cudaStream_t s) {
+                  int me, const int* row_of_node, const double* f_anal, double* part, double* acc, cudaStream_t s) {
   DiagField f{field, precision, a, mx};
-  k_norms<<<(unsigned)((me + 255) / 256), 256, 0, s>>>(f, jj, rj, me, row_of_node, f_anal, acc);
+  k_norms<<<(unsigned)((me + 255) / 256), 256, 0, s>>>(f, jj, rj, me, row_of_node, f_anal, part);
+  k_norms_final<<<1, kNormThreads, 0, s>>>(part, norm_partials(me), acc);
 }
 
 }  // namespace swe

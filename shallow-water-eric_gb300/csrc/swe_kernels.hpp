@@ -131,8 +131,10 @@ void launch_mass_mix(const Graph& G, const float2* h, double* acc, cudaStream_t 
 
 // Diagnostics (swe_diag.cu): field index kFieldH32 selects h^(3/2)
 constexpr int kFieldH32 = 16;
+// per-warp partial sums k_norms writes for me elements (4 doubles each)
+int64_t norm_partials(int me);
 void launch_norms(int field, int precision, const StateF64& a, const StateMix& mx, const int* jj, const double* rj,
-                  int me, const int* row_of_node, const double* f_anal, double* acc, cudaStream_t s);
+                  int me, const int* row_of_node, const double* f_anal, double* part, double* acc, cudaStream_t s);
 
 // kernels launched per stage / per step (for launch accounting)
 constexpr int kLaunchesPerStage = 4;
