@@ -48,18 +48,20 @@ UNIT = "node-stage updates/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=2000, help="lattice points per side of the wet/dry basin")
-    ap.add_argument("--cpu-n", type=int, default=500, help="lattice size of the CPU baseline sample")
-    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--parity-steps", type=int, default=15,
+                    help="steps of the oracle leg on the same mesh (CPU baseline and full-size parity); 0 skips it")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--profile-steps", type=int, default=3)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--workload", choices=["wetdry", "thacker", "batch", "dam", "sgn"], default="wetdry",
                     help="wetdry (default line) or one of the other workloads, printed as extra JSON lines")
     ap.add_argument("--batch-count", type=int, default=512)
+    ap.add_argument("--batch-subset", type=int, default=64,
+                    help="instances of the batched ensemble (the first ones of its seed) in the default line; 0 skips")
     ap.add_argument("--sgn-nx", type=int, default=10001)
     return ap.parse_args()
 
@@ -138,15 +140,20 @@ def make_case(n):
     return C.bump_basin_case(n=n, nsteps=200)
 
 
-def cpu_baseline(n, steps, warm=1):
-    """FP64 oracle (row-parallel OpenMP, every host core) on a bounded sample."""
+def oracle_for(case):
     import oracle
-    case = make_case(n)
     o = oracle.Oracle(case.mesh["jj"], case.mesh["rr"])
     o.set_params(oracle.Params(*case.params.fields()))
     o.set_bath(case.bath)
     for comp, js, vals in case.dirichlet:
         o.set_dirichlet(comp, js, vals)
+    return o
+
+
+def oracle_steps(case, steps, warm=0):
+    """The FP64 oracle (row-parallel OpenMP over every host core) advancing
+    the workload's own initial state: returns (state, node-stage/s, s)."""
+    o = oracle_for(case)
     u = case.u0.copy(order="F")
     t = 0.0
     for _ in range(warm):
@@ -156,25 +163,57 @@ def cpu_baseline(n, steps, warm=1):
         t = o.rk3_step(u, t)
     el = time.perf_counter() - t0
     N = case.mesh["rr"].shape[1]
-    return N * 3 * steps / el, N, el
+    return u, N * 3 * steps / el, el
+
+
+def host_cpu():
+    try:
+        for ln in open("/proc/cpuinfo"):
+            if ln.lower().startswith(("model name", "cpu part")):
+                return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+def workload_config(args, N, nnz, steps):
+    return {"workload": "wetdry_basin_4M" if args.n == 2000 else f"wetdry_basin_{args.n}x{args.n}",
+            "nodes": N, "nnz": nnz, "steps_timed": steps, "replicas": int(os.environ.get("WORLD_SIZE", "1")),
+            "l2": "working set larger than L2 (no flush)", "manning_n": 0.03, "cfl": 0.25}
 
 
 # ------------------------------------------------------------------ arms
 def run_reference(args, rank):
+    """The reference's CPU implementation of the step (the FP64 restatement:
+    no Fortran compiler exists here or on the GPU machine) on the same workload as
+    the GPU arm: the same mesh, W untimed then K timed SSP-RK3 steps."""
     if rank != 0:
         return
     threads = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(threads))
-    value, N, el = cpu_baseline(args.cpu_n, args.steps, warm=args.warmup)
-    sample = (f"{args.steps} SSP-RK3 steps of the {args.cpu_n}x{args.cpu_n}-point wet/dry basin ({N} nodes), "
-              f"FP64 restatement (oracle), OpenMP over rows")
+    case = make_case(args.n)
+    N = case.mesh["rr"].shape[1]
+    log(f"reference arm: mesh ready ({N} nodes)")
+    o = oracle_for(case)
+    nnz = len(o.matrices()["ja"])
+    u = case.u0.copy(order="F")
+    t = 0.0
+    for _ in range(args.warmup):
+        t = o.rk3_step(u, t)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        t = o.rk3_step(u, t)
+    el = time.perf_counter() - t0
+    value = N * 3 * args.steps / el
+    cores = int(os.environ["OMP_NUM_THREADS"])
+    sample = (f"{args.steps} timed SSP-RK3 steps (after {args.warmup} untimed) of the full workload, {N} nodes, "
+              f"FP64 restatement of the reference step (oracle), OpenMP over rows, {cores} threads, {host_cpu()}")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "wetdry_basin", "nodes": N, "precision": "fp64"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
-                         "sample": sample},
+        "config": workload_config(args, N, nnz, args.steps), "precision": "fp64",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -208,6 +247,81 @@ def timed_run(upd, u0, steps, warmup, dist, sampler=None):
     return dict(dev_ms=dev_ms, wall_s=wall, steps=n, launches=launches, clocks=clocks, last_dt=float(dt[0]))
 
 
+def parity_leg(args, case, N, world):
+    """Oracle leg on the same mesh, outside every timed region: the FP64
+    oracle runs --parity-steps steps of the workload (timed: the CPU
+    baseline); the FP64 and mixed GPU paths run the same steps from the same
+    initial state and are compared with it."""
+    from swe.update import from_case
+    k = args.parity_steps
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    u_orc, v_orc, el = oracle_steps(case, k)
+    log(f"oracle leg: {k} steps in {el:.1f} s")
+    out = {"steps": k}
+    for prec in (0, 1):
+        upd = from_case(case, precision=prec)
+        upd.upload(case.u0)
+        upd.set_time(0.0, 1e30)
+        upd.rk3_steps(k)
+        u = upd.download()
+        lump = upd.lumped
+        upd.close()
+        if prec == 0:
+            out["fp64_bit_exact_vs_oracle"] = bool(np.array_equal(u, u_orc))
+            out["fp64_max_abs_diff_vs_oracle"] = float(np.abs(u - u_orc).max())
+        else:
+            w = lump
+            out["l1_rel_h_mixed_vs_oracle"] = float(np.sum(w * np.abs(u[0] - u_orc[0])) / np.sum(w * np.abs(u_orc[0])))
+            out["max_abs_h_mixed_vs_oracle"] = float(np.abs(u[0] - u_orc[0]).max())
+            out["min_h_mixed"] = float(u[0].min())
+    cores = int(os.environ["OMP_NUM_THREADS"])
+    cpu = {"value": v_orc, "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": f"{k} SSP-RK3 steps of the same workload ({N} nodes, {el:.1f} s), FP64 restatement of the "
+                     f"reference step (oracle), OpenMP over rows, {cores} threads, {host_cpu()}"}
+    return out, cpu
+
+
+def batched_leg(args):
+    """C4 in the default line: the first --batch-subset instances of the
+    batched dam-break ensemble (seed 2; node counts log-uniform in [2e3, 2e5])
+    in one batched context (one launch per kernel for all instances,
+    per-instance dt), against the same meshes looped one context at a time
+    with the batched context's launch shapes; the same steps."""
+    from swe import cases as C
+    from swe.update import Update, from_case
+    cases = C.batch_instances(n_inst=args.batch_subset, precision=1)
+    NT = sum(c.mesh["rr"].shape[1] for c in cases)
+    log(f"batched leg: {len(cases)} instances, {NT} nodes")
+    upd = Update(batch=[(c.mesh, c.bath, c.params) for c in cases])
+    for b, c in enumerate(cases):
+        for comp, js, vals in c.dirichlet:
+            upd.set_dirichlet(comp, js, vals, inst=b)
+    u0 = [c.u0 for c in cases]
+    upd.upload(u0); upd.set_time(0.0, 1e30); upd.rk3_steps(args.warmup)
+    upd.upload(u0); upd.set_time(0.0, 1e30)
+    _, _, n = upd.rk3_steps(args.steps)
+    batched_ms = upd.last_device_ms
+    spec = upd.tuning.split("autotuned ", 1)[-1]
+    got = upd.download_split()
+    upd.close()
+    loop_ms, same = 0.0, True
+    for b, c in enumerate(cases):
+        s = from_case(c, precision=1)
+        s.set_tuning(spec)
+        s.upload(c.u0); s.set_time(0.0, 1e30); s.rk3_steps(args.warmup)
+        s.upload(c.u0); s.set_time(0.0, 1e30)
+        s.rk3_steps(args.steps)
+        loop_ms += s.last_device_ms
+        same = same and np.array_equal(s.download(), got[b])
+        s.close()
+    vb = NT * 3 * n / (batched_ms / 1e3)
+    vl = NT * 3 * n / (loop_ms / 1e3)
+    return {"workload": f"batched_dam_breaks_first_{len(cases)}_of_512", "instances": len(cases), "nodes": NT,
+            "steps": n, "batched_node_stage_per_s": vb, "looped_single_instance_node_stage_per_s": vl,
+            "batched_over_looped": vb / vl, "batched_equals_looped_bitwise": bool(same),
+            "launch_shapes": "autotuned on the batched context, the same for the looped contexts"}
+
+
 def run_ours(args, rank, world, dist):
     import torch
     from swe.update import from_case
@@ -219,7 +333,7 @@ def run_ours(args, rank, world, dist):
     t_setup = time.perf_counter()
     upd = from_case(case, precision=1)
     setup_s = time.perf_counter() - t_setup
-    log(f"mixed context ready ({setup_s:.2f} s: device assembly, RCM, layout, upload)")
+    log(f"mixed context ready ({setup_s:.2f} s: device assembly, Morton order, layout, upload)")
     nnz = upd.sizes()[1]
     lump = upd.lumped
     u0 = case.u0
@@ -291,22 +405,20 @@ def run_ours(args, rank, world, dist):
 
     if rank != 0:
         return
-    cpu = None
-    if world == 1:
-        os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
-        cv, cN, cel = cpu_baseline(args.cpu_n, args.cpu_steps)
-        cpu = {"value": cv, "unit": UNIT, "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
-               "sample": f"{args.cpu_steps} SSP-RK3 steps of the {args.cpu_n}x{args.cpu_n}-point wet/dry basin "
-                         f"({cN} nodes, {cel:.1f} s), FP64 restatement, OpenMP over rows"}
+    parity, cpu = None, None
+    if world == 1 and args.parity_steps > 0:
+        parity, cpu = parity_leg(args, case, N, world)
+    batched = None
+    if world == 1 and args.batch_subset > 0:
+        batched = batched_leg(args)
+        log(f"batched leg: {batched['batched_over_looped']:.2f}x looped")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r["dev_ms"] / r["steps"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (double-float depth)",
         "data": "synthetic (seeded jittered-lattice Delaunay mesh, Gaussian-bump bathymetry)",
-        "config": {"workload": "wetdry_basin_4M" if args.n == 2000 else f"wetdry_basin_{args.n}x{args.n}",
-                   "nodes": N, "nnz": nnz, "precision": "mixed (FP32 arithmetic, double-float depth)",
-                   "steps_timed": r["steps"], "replicas": world,
-                   "l2": "working set larger than L2 (no flush)", "manning_n": 0.03, "cfl": 0.25},
+        "config": workload_config(args, N, nnz, r["steps"]),
+        "precision": "mixed (FP32 arithmetic, double-float depth)",
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_kind": peak_kind,
                      "unit_of_work": "one RK stage (k_node+k_low+k_fct+k_update), algorithmic bytes "
@@ -319,6 +431,8 @@ def run_ours(args, rank, world, dist):
         "gpu_launches": r["launches"],
         "fp64": fp64,
         "speedup_mixed_vs_fp64": (value / fp64["value"]) if fp64 else None,
+        "parity_vs_oracle": parity,
+        "batched": batched,
         "mass_rel_drift_mixed": (mass_mix - mass0) / mass0,
         "min_h_mixed": float(u_mix[0].min()),
         "kernel_time_share_of_step": step_kernel_ms / (r["dev_ms"] / r["steps"]),

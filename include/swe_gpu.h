@@ -72,8 +72,9 @@ typedef struct swe_params {
 typedef struct swe_ctx swe_ctx;
 
 /* construct_matrices (SOURCES/update.f90:18-132) for one mesh: builds the CSR
- * pattern, consistent and lumped mass, diag and c_ij, renumbers the nodes by
- * reverse Cuthill-McKee and uploads the SELL-32 edge graph.
+ * pattern, consistent and lumped mass, diag and c_ij, renumbers the nodes
+ * along a Z-order (Morton) curve of their coordinates (SWE_ORDER=rcm: reverse
+ * Cuthill-McKee) and uploads the SELL-32 edge graph.
  * jj(3, me) 1-based counter-clockwise triangles, rr(2, np), bath(np). */
 int swe_create(swe_ctx** ctx, int np, int me, const int* jj, const double* rr,
                const double* bath, const swe_params* params);
@@ -183,7 +184,8 @@ int swe_get_time(swe_ctx* ctx, double* time, double* t_final, double* dt);
  * time and last dt; steps_done (nullable) the number of steps instance 0 ran. */
 int swe_rk3_steps(swe_ctx* ctx, int nsteps, double* time_out, double* dt_out, int* steps_done);
 
-/* Total water mass sum_i m_i h_i per instance (compensated summation). */
+/* Total water mass sum_i m_i h_i per instance: double-double sums added in a
+ * fixed order, so every call on the same state gives the same bits. */
 int swe_mass(swe_ctx* ctx, double* mass_out);
 
 /* Kernel launches issued by the last swe_rk3_steps call (for accounting). */
@@ -201,14 +203,21 @@ int swe_profile_kernels(swe_ctx* ctx, int nsteps, double* ms_out);
 
 /* Autotuner: times every block-size / entry-batch / grid variant of the
  * mixed kernels (including the shared-memory row-tile variants) on the
- * current state and keeps the fastest per kernel (variants agree to FP32
- * rounding).  swe_rk3_steps runs it on its first call unless the environment
+ * current state and keeps the fastest per kernel (every variant gives the
+ * same bits).  swe_rk3_steps runs it on its first call unless the environment
  * sets SWE_AUTOTUNE=0.  swe_tuning names the chosen configuration; setting
  * SWE_TUNE to that description (the text after "autotuned ") makes a later
  * context launch exactly those variants without timing (a malformed value
  * -> SWE_ERR_ARG). */
 int swe_autotune(swe_ctx* ctx);
 const char* swe_tuning(const swe_ctx* ctx);
+/* Launch exactly the variants of a tuning description (the text after
+ * "autotuned " or "fixed " in swe_tuning) without timing, as SWE_TUNE does;
+ * a checkpoint stores the description and a resumed run sets it, so the
+ * resumed context runs the same launch shapes.  Every variant gives the
+ * same bits, so this changes speed only.  No-op on FP64 contexts; a
+ * malformed description -> SWE_ERR_ARG. */
+int swe_set_tuning(swe_ctx* ctx, const char* spec);
 
 /* FCT_positivity for callers that cannot allocate device memory.
  *
@@ -219,8 +228,11 @@ const char* swe_tuning(const swe_ctx* ctx);
  * caller owns, and the only scratch (R^- per node) lives in a fixed device
  * array compiled into the library.  Nothing is allocated or freed.
  *   np        rows (1..SWE_NOALLOC_MAX_NODES; larger values -> SWE_ERR_ARG)
- *   d_ia      row pointers, np+1 ints, 1-based like mass%ia
- *   d_ja      column indices, 1-based
+ *   d_ia      row pointers, np+1 ints, 1-based like mass%ia: ia(1) = 1,
+ *             non-decreasing, ia(np+1)-1 entries in d_mat and d_lij
+ *   d_ja      column indices, 1-based, each in 1..np (checked on the device:
+ *             a column out of range is not read through and the call
+ *             returns SWE_ERR_ARG with d_lij unspecified)
  *   d_unext   (lumped/dt)*h^L per row
  *   d_mat     f_ij per CSR entry
  *   htiny     inputs%htiny

@@ -76,6 +76,8 @@ struct swe_ctx {
   TileCtl tiles{};                       // row tiles of the shared-memory variants
   bool tiles_ok = false;
   double* d_mass_acc = nullptr;
+  double* d_mass_part = nullptr;         // per-slice partial sums of swe_mass
+  int64_t* d_inst_slice = nullptr;       // n_inst + 1 slice offsets
   // diagnostics: per-instance element lists and Gauss weights, on first use
   std::vector<int*> d_jj_inst;
   std::vector<double*> d_rj_inst;
@@ -221,6 +223,13 @@ static T* upload_vec(swe_ctx* c, const std::vector<T>& v, cudaError_t& st) {
   return d;
 }
 
+// Bathymetry as a double-float pair hi + lo (hi = z rounded to FP32): the
+// mixed kernels form the free surface eta = h + z from it.
+static float2 bath_df(double z) {
+  const float hi = (float)z;
+  return make_float2(hi, (float)(z - (double)hi));
+}
+
 static int build_device(swe_ctx* c, const std::vector<std::vector<double>>& baths) {
   c->L = build_layout(c->meshes, baths);
   const Layout& L = c->L;
@@ -273,9 +282,9 @@ static int build_device(swe_ctx* c, const std::vector<std::vector<double>>& bath
     G.cxiif = upload_vec(c, fr, st);
     for (int64_t r = 0; r < L.n_rows; r++) fr[r] = (float)L.cyii[r];
     G.cyiif = upload_vec(c, fr, st);
-    std::vector<float> bf(L.n_rows);
-    for (int64_t r = 0; r < L.n_rows; r++) bf[r] = (float)L.bath[r];
-    G.bathf = upload_vec(c, bf, st);
+    std::vector<float2> bdf(L.n_rows);
+    for (int64_t r = 0; r < L.n_rows; r++) bdf[r] = bath_df(L.bath[r]);
+    G.bathdf = upload_vec(c, bdf, st);
   }
   c->h_dir_mask.assign(L.n_rows, 0);
   c->h_dir_val.assign((size_t)c->S * L.n_rows, 0.0);
@@ -304,6 +313,12 @@ static int build_device(swe_ctx* c, const std::vector<std::vector<double>>& bath
   c->d_row_of_node = upload_vec(c, row_of_node, st);
   c->d_stage = c->buf.alloc<double>((size_t)c->S * c->node_off[c->n_inst], st);
   c->d_mass_acc = c->buf.alloc<double>(2 * (size_t)c->n_inst, st);
+  c->d_mass_part = c->buf.alloc<double>(2 * (size_t)L.n_slices, st);
+  {
+    std::vector<int64_t> inst_slice(c->n_inst + 1);
+    for (int b = 0; b <= c->n_inst; b++) inst_slice[b] = L.row_off[b] / 32;
+    c->d_inst_slice = upload_vec(c, inst_slice, st);
+  }
   const size_t n = L.n_rows, ne = L.n_entries;
   if (c->precision == SWE_PREC_FP64) {
     alloc_state_f64(c, c->A, st); alloc_state_f64(c, c->B, st); alloc_state_f64(c, c->Cs, st);
@@ -320,7 +335,7 @@ static int build_device(swe_ctx* c, const std::vector<std::vector<double>>& bath
     alloc_state_mix(c, c->mA, st); alloc_state_mix(c, c->mB, st); alloc_state_mix(c, c->mC, st);
     WorkMix& w = c->wm;
     w.alpha = c->buf.alloc<float>(n, st); w.res = c->buf.alloc<float>(n, st);
-    w.rminus = c->buf.alloc<float>(n, st); w.rneg = c->buf.alloc<float>(n, st);
+    w.rminus = c->buf.alloc<float>(n, st);
     w.dmu = c->buf.alloc<float2>(ne, st);
     w.dlam = c->buf.alloc<float>(ne, st);
     w.hL = c->buf.alloc<float2>(n, st);
@@ -363,14 +378,16 @@ __global__ void k_gather_out(double* __restrict__ stage, const int* __restrict__
 }
 __global__ void k_scatter_in_mix(const double* __restrict__ stage, const int* __restrict__ row_of_node,
                                  int64_t n_nodes, int S, StateMix a, const int* __restrict__ slice_inst,
-                                 const InstConst* __restrict__ C, const float* __restrict__ bathf) {
+                                 const InstConst* __restrict__ C, const float2* __restrict__ bathdf) {
   int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (n >= n_nodes) return;
   const int64_t r = row_of_node[n];
   const double h = stage[n * S];
-  a.h[r] = df_from_double(h);
+  const float2 hdf = df_from_double(h);
+  a.h[r] = hdf;
+  // free surface eta = h + z rounded once, as the stage kernels form it
   a.nq[r] = make_float4(shadow_depth(h, C[slice_inst[r >> 5]].htiny), (float)stage[n * S + 1],
-                        (float)stage[n * S + 2], bathf[r]);
+                        (float)stage[n * S + 2], df_add(hdf, bathdf[r]).x);
   if (S == 5) { a.q3[r] = (float)stage[n * S + 3]; a.q4[r] = (float)stage[n * S + 4]; }
 }
 // mixed state (sm) or the mixed low-order state (w) back to the reference layout
@@ -438,7 +455,7 @@ static int to_device(swe_ctx* c, const double* un, bool device_src, int64_t node
       k_scatter_in<<<nb, 256, 0, c->stream>>>(c->d_stage + (size_t)c->S * b, c->d_row_of_node + b, e - b, c->S, c->A);
     else
       k_scatter_in_mix<<<nb, 256, 0, c->stream>>>(c->d_stage + (size_t)c->S * b, c->d_row_of_node + b, e - b, c->S,
-                                                   c->mA, c->G.slice_inst, c->d_C, c->G.bathf);
+                                                   c->mA, c->G.slice_inst, c->d_C, c->G.bathdf);
     CK(cudaGetLastError());
   }
   return SWE_OK;
@@ -768,12 +785,12 @@ SWE_API int swe_set_bath(swe_ctx* c, int inst, const double* bath) {
     CK(cudaMemcpyAsync((double*)c->G.bath + r0, L.bath.data() + r0, nr * sizeof(double), cudaMemcpyHostToDevice,
                        c->stream));
   } else {
-    std::vector<float> bf(nr);
-    for (int64_t r = 0; r < nr; r++) bf[r] = (float)L.bath[r0 + r];
+    std::vector<float2> bf(nr);
+    for (int64_t r = 0; r < nr; r++) bf[r] = bath_df(L.bath[r0 + r]);
     CK(cudaMemcpyAsync((double*)c->G.bath + r0, L.bath.data() + r0, nr * sizeof(double), cudaMemcpyHostToDevice,
                        c->stream));
-    CK(cudaMemcpyAsync((float*)c->G.bathf + r0, bf.data(), nr * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-    launch_refresh_z(c->G, c->mA, c->stream);
+    CK(cudaMemcpyAsync((float2*)c->G.bathdf + r0, bf.data(), nr * sizeof(float2), cudaMemcpyHostToDevice, c->stream));
+    launch_refresh_eta(c->G, c->mA, c->stream);
     CK(cudaGetLastError());
   }
   CK(cudaStreamSynchronize(c->stream));
@@ -1170,17 +1187,20 @@ static bool parse_tuning(const char* spec, bool tiles, KernelTune& t) {
   return true;
 }
 
+// A fixed launch configuration (the autotuner's description) instead of timing
+static int apply_tuning(swe_ctx* c, const char* spec, const char* what) {
+  KernelTune t;
+  if (!parse_tuning(spec, c->tiles_ok, t)) return fail(c, SWE_ERR_ARG, std::string("bad ") + what + ": " + spec);
+  c->tune = t;
+  c->tuned = true;
+  c->tuning = std::string("thread-per-row SELL-32; fixed ") + spec;
+  drop_graphs(c);
+  return SWE_OK;
+}
+
 static int autotune(swe_ctx* c) {
   if (c->precision != SWE_PREC_MIXED) { c->tuned = true; return SWE_OK; }
-  if (const char* spec = getenv("SWE_TUNE")) {   // a fixed configuration instead of timing
-    KernelTune t;
-    if (!parse_tuning(spec, c->tiles_ok, t)) return fail(c, SWE_ERR_ARG, std::string("bad SWE_TUNE: ") + spec);
-    c->tune = t;
-    c->tuned = true;
-    c->tuning = std::string("thread-per-row SELL-32; fixed ") + spec;
-    drop_graphs(c);
-    return SWE_OK;
-  }
+  if (const char* spec = getenv("SWE_TUNE")) return apply_tuning(c, spec, "SWE_TUNE");
   int rc;
   std::vector<InstState> saved;
   if ((rc = save_state(c, saved))) return rc;
@@ -1266,6 +1286,12 @@ SWE_API int swe_autotune(swe_ctx* c) {
   NvtxRange nvtx("swe_autotune");
   if (!c) return SWE_ERR_ARG;
   return autotune(c);
+}
+
+SWE_API int swe_set_tuning(swe_ctx* c, const char* spec) {
+  if (!c || !spec) return SWE_ERR_ARG;
+  if (c->precision != SWE_PREC_MIXED) { c->tuned = true; return SWE_OK; }
+  return apply_tuning(c, spec, "tuning");
 }
 
 // ---- movie frames (main.f90:119-143, sub_plot.f90:1036-1095) ----
@@ -1539,8 +1565,9 @@ SWE_API int swe_profile_kernels(swe_ctx* c, int nsteps, double* ms_out) {
 SWE_API int swe_mass(swe_ctx* c, double* mass_out) {
   if (!c || !mass_out) return fail(c, SWE_ERR_ARG, "bad arguments");
   CK(cudaMemsetAsync(c->d_mass_acc, 0, 2 * sizeof(double) * c->n_inst, c->stream));
-  if (c->precision == SWE_PREC_FP64) launch_mass_f64(c->G, c->A.h, c->d_mass_acc, c->stream);
-  else launch_mass_mix(c->G, c->mA.h, c->d_mass_acc, c->stream);
+  launch_mass(c->G, c->n_inst, c->precision == SWE_PREC_FP64 ? c->A.h : nullptr,
+              c->precision == SWE_PREC_FP64 ? nullptr : c->mA.h, c->d_inst_slice, c->d_mass_part, c->d_mass_acc,
+              c->stream);
   CK(cudaGetLastError());
   std::vector<double> acc(2 * c->n_inst);
   CK(cudaMemcpyAsync(acc.data(), c->d_mass_acc, acc.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));

@@ -66,7 +66,7 @@ struct Graph {
   const float* __restrict__ lumpedf;      // FP32 copies (mixed path)
   const float* __restrict__ inv_lumpedf;
   const double* __restrict__ bath;
-  const float* __restrict__ bathf;
+  const float2* __restrict__ bathdf;     // mixed path: bathymetry as a double-float pair
   const uint8_t* __restrict__ dir_mask;   // bit k: component k is Dirichlet
   const double* __restrict__ dir_val;     // (S, n_rows) SoA, read where masked
 };

@@ -15,8 +15,8 @@ struct StateF64 {
 
 // Mixed-precision state: h as a double-float pair (hi + lo, about 48
 // significant bits: positivity and mass) plus a packed FP32 node record
-// {h shadow, qx, qy, z} that neighbours gather with one 16-byte load; type
-// 13's h*eta and h*w in FP32.
+// {h shadow, qx, qy, eta} that neighbours gather with one 16-byte load (eta =
+// h + z rounded once per node); type 13's h*eta and h*w in FP32.
 struct StateMix {
   float2* h;
   float4* nq;
@@ -37,7 +37,6 @@ struct WorkF64 {
 struct WorkMix {
   float *alpha, *res;                    // per row
   float* rminus;                         // per row: R^-_i
-  float* rneg;                           // per row: R^-_i * sum_{f_ij<0} f_ij
   float2* dmu;                           // per entry: (d_ij, mu_ij), one 8-byte load
   float* dlam;                           // per entry: |c_ij| lambda_max from k_dt_mix (stage 1)
   float2* hL;                            // low-order depth (double-float)
@@ -102,7 +101,6 @@ void launch_fct_positivity_f64(const Graph& G, const InstConst* C, const double*
                                const double* matii, double* rtmp, double* lij, cudaStream_t s);
 void launch_fct_generic_f64(const Graph& G, double* unext, const double* maxn, const double* minn, const double* dg,
                             const double* mat, const double* matii, double* rplus, double* rminus, cudaStream_t s);
-void launch_mass_f64(const Graph& G, const double* h, double* acc, cudaStream_t s);
 
 // Launch configuration of the mixed kernels, per kernel kind (0 dt, 1 node,
 // 2 low, 3 fct, 4 update): block size, entry batch (1, 2, 4 or 8; 1 or 2
@@ -110,9 +108,10 @@ void launch_mass_f64(const Graph& G, const double* h, double* acc, cudaStream_t 
 // rows, or one block per tile of rows with shared-memory neighbours), and for
 // low a register cap (cap_low 0, 1, 2: at least 3, 4 or 5 resident blocks of
 // 256 threads per SM, i.e. at most 85, 64 or 51 registers; the tightest
-// spills a little).  Chosen by the autotuner in swe_api.cu.  Every choice sums in the same entry order; the
-// variants are separate instantiations whose FMA contraction may differ, so
-// results agree to FP32 rounding.
+// spills a little).  Chosen by the autotuner in swe_api.cu.  Every choice
+// performs the same IEEE operations in the same entry order (the mixed
+// kernels are built without FMA contraction and spell out every fused
+// multiply-add), so every choice gives bit-identical results.
 struct KernelTune {
   int block[5] = {128, 128, 128, 128, 128};
   int batch[5] = {1, 1, 1, 1, 1};
@@ -126,13 +125,18 @@ void launch_kernel_mix(int kind, const StageArgsMix& a, const KernelTune& t, cud
 bool kind_has_tiles(int kind);   // kernel kinds with a shared-memory tile variant
 void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, float* dlam, float* alpha,
                    unsigned* err, const KernelTune& t, const TileCtl* tiles, cudaStream_t s);
-void launch_refresh_z(const Graph& G, StateMix u, cudaStream_t s);
-void launch_mass_mix(const Graph& G, const float2* h, double* acc, cudaStream_t s);
+void launch_refresh_eta(const Graph& G, StateMix u, cudaStream_t s);
 
 // Diagnostics (swe_diag.cu): field index kFieldH32 selects h^(3/2)
 constexpr int kFieldH32 = 16;
 // per-warp partial sums k_norms writes for me elements (4 doubles each)
 int64_t norm_partials(int me);
+// Total mass sum m_i h_i per instance in a fixed order (bit-reproducible):
+// per-slice double-double partials (part: 2 per slice), then one block per
+// instance adds its slices (inst_slice: n_inst + 1 slice offsets) into
+// acc[2 b], acc[2 b + 1].  One of h64 (FP64 state) and hdf (mixed) is non-null.
+void launch_mass(const Graph& G, int n_inst, const double* h64, const float2* hdf, const int64_t* inst_slice,
+                 double* part, double* acc, cudaStream_t s);
 void launch_norms(int field, int precision, const StateF64& a, const StateMix& mx, const int* jj, const double* rj,
                   int me, const int* row_of_node, const double* f_anal, double* part, double* acc, cudaStream_t s);
 

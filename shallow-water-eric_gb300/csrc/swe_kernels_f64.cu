@@ -769,29 +769,6 @@ __global__ void k_fct_generic_f64(Graph G, double* __restrict__ unext, const dou
   }
 }
 
-// Total mass sum m_i h_i per instance, Kahan-compensated per thread then
-// combined in double-double per warp (atomics on two words per instance).
-__global__ void k_mass_f64(Graph G, const double* __restrict__ h, double* __restrict__ acc) {
-  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  double v = 0.0;
-  int b = -1;
-  if (r < G.n_rows && G.len[r] > 0) { b = G.slice_inst[r >> 5]; v = G.lumped[r] * h[r]; }
-  double cmp = 0.0;
-  for (int off = 16; off > 0; off >>= 1) {
-    double o = __shfl_down_sync(0xffffffffu, v, off);
-    double oc = __shfl_down_sync(0xffffffffu, cmp, off);
-    double s = v + o;                    // two-sum
-    double bb = s - v;
-    double err = (v - (s - bb)) + (o - bb);
-    v = s;
-    cmp = cmp + oc + err;
-  }
-  int b0 = __shfl_sync(0xffffffffu, b, 0);
-  if ((threadIdx.x & 31) == 0 && b0 >= 0) {
-    atomicAdd(&acc[2 * b0], v);
-    atomicAdd(&acc[2 * b0 + 1], cmp);
-  }
-}
 
 // ----------------------------- launchers -----------------------------------
 static inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
@@ -853,8 +830,5 @@ void launch_fct_generic_f64(const Graph& G, double* unext, const double* maxn, c
   k_fct_generic_f64<<<nblk(G.n_rows, 128), 128, 0, s>>>(G, unext, maxn, minn, dg, mat, matii, rplus, rminus, 1);
 }
 
-void launch_mass_f64(const Graph& G, const double* h, double* acc, cudaStream_t s) {
-  k_mass_f64<<<nblk(G.n_rows, 256), 256, 0, s>>>(G, h, acc);
-}
 
 }  // namespace swe

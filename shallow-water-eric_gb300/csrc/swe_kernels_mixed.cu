@@ -3,18 +3,18 @@
 //
 // Same sweep structure as the FP64 path (one thread per row, SELL-32 graph)
 // with the flux, lambda_max, viscosity, entropy-residual and antidiffusion
-// arithmetic in FP32 on FP32 data (q, z, c_ij, d_ij, mu_ij and an FP32 shadow
-// of h).  A warp-wide FP64 instruction, or a float<->double conversion, costs
-// GB300 tens of SM cycles (FP64 runs at ~1/64 of the FP32 rate), and a design
-// that kept the limiter sums and the per-row depth updates in FP64 measured
-// its FP64 pipe 73-79% busy in the limiter and update sweeps.  The precision
-// the scheme needs is kept without FP64:
+// arithmetic in FP32 on FP32 data (q, the free surface eta, c_ij, d_ij,
+// mu_ij and an FP32 shadow of h).  A warp-wide FP64 instruction, or a
+// float<->double conversion, costs GB300 tens of SM cycles (FP64 runs at
+// ~1/64 of the FP32 rate), and a design that kept the limiter sums and the
+// per-row depth updates in FP64 measured its FP64 pipe 73-79% busy in the
+// limiter and update sweeps.  The precision the scheme needs is kept without
+// FP64:
 //   * the depth h (state, low-order h^L, new depth, RK combination) is a
 //     double-float pair hi + lo (about 48 significant bits), so the FP32
 //     increments of a stage are never lost to the rounding of h;
-//   * h^L = h + a (fix h + rk_1) with a = dt/m_i: non-negative in any
-//     rounding, because a |fix| <= CFL < 1 and rk_1 >= 0 (SOURCES/update.f90:
-//     202-215);
+//   * h^L = h + a (P - N - c_ii.v_i h) with a = dt/m_i, P >= 0 and
+//     a N <= CFL h (SOURCES/update.f90:202-215): non-negative in any rounding;
 //   * the limiter R^-_i = min(1, (1 - 2^-18) Q^-_i / P^-_i) (fct.f90:15-30) is
 //     FP32; the 2^-18 margin (64 units in the last place) bounds the at most
 //     ~12 roundings between the limiter and the depth update, so the limited
@@ -23,13 +23,31 @@
 //     of h that keeps both decisions exact, and m h^L/dt <= htiny is decided in
 //     FP64 inside a 1e-5 band around htiny.
 //
-// Node data that neighbours gather is packed per node as float4
-// {h shadow, qx, qy, z}: one 16-byte load (one L2 sector) per neighbour.
+// Well-balancing.  Node data that neighbours gather is packed per node as
+// float4 {h shadow, qx, qy, eta}: one 16-byte load (one L2 sector) per
+// neighbour, with the free surface eta = h + z rounded once per node from
+// the double-float depth and the double-float bathymetry.  A lake at rest
+// then has bit-identical eta at every wet node, and every term of a row
+// vanishes exactly there:
+//   * the topography term g h_i (eta_j - eta_i) c_ij (update.f90:606-610);
+//   * the bathymetry difference z_j - z_i = (eta_j - eta_i) + (h_i - h_j),
+//     which is then h_i - h_j exactly (Sterbenz), so the hydrostatic depths
+//     H*_ij = max(0, h_i - max(0, z_j - z_i)) and H*_ji are equal bit for bit;
+//   * the mass rows in the difference form d (H*_ji - H*_ij) (the reference's
+//     d (h_j rat_ji - h_i rat_ij), with h rat = H* written out).
+//
+// Reproducibility.  The file is built without FMA contraction (-fmad=false);
+// every fused multiply-add is written out with __fmaf_rn.  Every launch
+// variant (block size, entry batch, resident grid, shared-memory tile,
+// register cap) and the lambda_max reuse of stage 1 therefore perform the
+// same IEEE operations on the same values in the same order: all variants,
+// and hence any autotuner choice, give bit-identical results.
 #include "swe_kernels.hpp"
 
 namespace swe {
 
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ float fma_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 
 // c . v with an explicit rounding sequence.  The low-order mass flux
 // (mu_ij - c.v_j) h_j is non-negative only if mu_ij >= c.v_j holds bit for
@@ -54,30 +72,41 @@ __device__ __forceinline__ float shadow_df(float2 h, const InstConst& c) {
   return f;
 }
 
+// Free surface eta = h + z of a node record, rounded once from the
+// double-float depth and the double-float bathymetry.
+__device__ __forceinline__ float eta_of(float2 h, float2 z) { return df_add(h, z).x; }
+
 // Hydrostatic reconstruction H*_ij = max(0, h_i + z_i - max(z_i, z_j))
 // (SOURCES/update.f90:569-570) in the algebraically equal, cancellation-free
-// form max(0, h_i - max(0, z_j - z_i)).  In FP32 the reference form loses
-// (h_i + z_i) - z_i to rounding at the scale of z, which for thin layers on
-// high bathymetry is a large relative error in H*/h.  rat = H*/h is 1
-// exactly when z_j <= z_i and never exceeds 1.
+// form max(0, h_i - max(0, dz)), dz = z_j - z_i.  In FP32 the reference form
+// loses (h_i + z_i) - z_i to rounding at the scale of z, which for thin
+// layers on high bathymetry is a large relative error in H*/h.  H*_ij = h_i
+// exactly when dz <= 0 and never exceeds h_i.
 struct Recon {
-  float Hij, Hji, rij, rji;   // rij, rji: H*/h with the h <= 0 tests
+  float Hij, Hji;
 };
-__device__ __forceinline__ Recon recon(float hi, float hj, float dz, float invhi, float invhj) {
+__device__ __forceinline__ Recon recon(float hi, float hj, float dz) {
   Recon R;
-  R.Hij = (dz <= 0.f) ? hi : fmaxf(0.f, hi - dz);
-  R.Hji = (dz >= 0.f) ? hj : fmaxf(0.f, hj + dz);
-  R.rij = (hi > 0.f) ? ((dz <= 0.f) ? 1.f : fminf(__fmul_rn(R.Hij, invhi), 1.f)) : 0.f;
-  R.rji = (hj > 0.f) ? ((dz >= 0.f) ? 1.f : fminf(__fmul_rn(R.Hji, invhj), 1.f)) : 0.f;
+  R.Hij = (dz <= 0.f) ? hi : fmaxf(0.f, __fsub_rn(hi, dz));
+  R.Hji = (dz >= 0.f) ? hj : fmaxf(0.f, __fadd_rn(hj, dz));
   return R;
 }
+// rat_ij = H*_ij / h_i with the reference's h <= 0 test (0 there); 1 exactly
+// downhill and never above 1.
+__device__ __forceinline__ float rat_of(float H, float h, bool flat, float invh) {
+  return (h > 0.f) ? (flat ? 1.f : fminf(__fmul_rn(H, invh), 1.f)) : 0.f;
+}
 __device__ __forceinline__ float inv_pos(float h) { return (h > 0.f) ? fdiv(1.0f, h) : 0.f; }
+// z_j - z_i from the node records: (eta_j - eta_i) + (h_i - h_j)
+__device__ __forceinline__ float dz_of(float deta, float hi, float hj) { return __fadd_rn(deta, __fsub_rn(hi, hj)); }
 
-// antidiffusive h-flux f_ij of compute_fct_matrix (update.f90:744-745) with
-// explicit roundings: k_fct and k_update must see the same f, bit for bit.
+// antidiffusive h-flux f_ij of compute_fct_matrix (update.f90:744-745),
+// dd (h_j rat_ji - h_i rat_ij) + dm (h_j (1 - rat_ji) - h_i (1 - rat_ij)) with
+// h rat = H* written out, in explicit roundings: k_fct and k_update must see
+// the same f, bit for bit.
 __device__ __forceinline__ float fct_from(float dd, float dm, float hi, float hj, const Recon& R) {
-  const float a = __fsub_rn(__fmul_rn(hj, R.rji), __fmul_rn(hi, R.rij));
-  const float b = __fsub_rn(__fmul_rn(hj, __fsub_rn(1.f, R.rji)), __fmul_rn(hi, __fsub_rn(1.f, R.rij)));
+  const float a = __fsub_rn(R.Hji, R.Hij);
+  const float b = __fsub_rn(__fsub_rn(hj, R.Hji), __fsub_rn(hi, R.Hij));
   return __fadd_rn(__fmul_rn(dd, a), __fmul_rn(dm, b));
 }
 
@@ -95,14 +124,15 @@ __device__ __forceinline__ LamK lam_k(float g, float htiny) { return LamK{g, hti
 __device__ __forceinline__ float phi_f(float h, float vl, float hl, float vr, float hr, float ovhl, float ovhr,
                                        float sql, float sqr, const LamK& k) {
   const float ovh = ovh_f(h, k.htiny);
+  const float hg = 0.5f * k.g;
   float fl, fr;
   if (h > hl && h > hr) {              // two shocks: the usual case at h = x0 h_min
-    fl = (h - hl) * sqrtf(0.5f * k.g * (ovh + ovhl));
-    fr = (h - hr) * sqrtf(0.5f * k.g * (ovh + ovhr));
+    fl = (h - hl) * sqrtf(hg * (ovh + ovhl));
+    fr = (h - hr) * sqrtf(hg * (ovh + ovhr));
   } else {
     const float sgh = sqrtf(k.g * h);
-    fl = (h > hl) ? (h - hl) * sqrtf(0.5f * k.g * (ovh + ovhl)) : 2.f * (sgh - sql);
-    fr = (h > hr) ? (h - hr) * sqrtf(0.5f * k.g * (ovh + ovhr)) : 2.f * (sgh - sqr);
+    fl = (h > hl) ? (h - hl) * sqrtf(hg * (ovh + ovhl)) : 2.f * (sgh - sql);
+    fr = (h > hr) ? (h - hr) * sqrtf(hg * (ovh + ovhr)) : 2.f * (sgh - sqr);
   }
   return fl + fr + vr - vl;
 }
@@ -120,15 +150,15 @@ __device__ __forceinline__ bool lambda_f(float hl, float hr, float vl, float vr,
   float ht;
   float fh = phi_f(x0 * hmin, vl, hl, vr, hr, ovhl, ovhr, sql, sqr, k);
   if (0.f <= fh) {
-    const float s = fmaxf(vl - vr + 2.f * sql + 2.f * sqr, 0.f);
+    const float s = fmaxf(fma_(2.f, sqr, fma_(2.f, sql, vl - vr)), 0.f);
     ht = fminf(x0 * hmin, fdiv(s * s, 16.f * k.g));
   } else {
     fh = phi_f(x0 * hmax, vl, hl, vr, hr, ovhl, ovhr, sql, sqr, k);
     const float sqrmin = (lmin ? sql : sqr) * k.rsg, sqrmax = (lmin ? sqr : sql) * k.rsg;
     if (0.f <= fh) {
       const float a = 0.353553391f;   // 1 / (2 sqrt(2))
-      const float cc = -(hmin * a) - sqrmin * sqrmax + sqrmin * (vr - vl) * (0.5f * k.rsg);
-      float Delta = hmin - 4.f * a * cc;
+      const float cc = fma_(sqrmin * (vr - vl), 0.5f * k.rsg, -(hmin * a) - sqrmin * sqrmax);
+      float Delta = fma_(-4.f * a, cc, hmin);
       if (Delta < 0.f) {
         if (Delta < -1e-5f * hmin) ok = false;
         Delta = 0.f;
@@ -136,20 +166,32 @@ __device__ __forceinline__ bool lambda_f(float hl, float hr, float vl, float vr,
       const float s = (sqrtf(Delta) - sqrmin) * 1.41421356f;   // / (2a)
       ht = fminf(x0 * hmax, s * s);
     } else {
-      ht = sqrmin * sqrmax * (1.f + 1.41421356f * k.rsg * fdiv(vl - vr, sqrmin + sqrmax));
+      ht = sqrmin * sqrmax * fma_(1.41421356f * k.rsg, fdiv(vl - vr, sqrmin + sqrmax), 1.f);
     }
   }
-  const float lbdl = vl - sql * sqrtf((1.f + fmaxf((ht - hl) * ovhl * 0.5f, 0.f)) * (1.f + fmaxf((ht - hl) * ovhl, 0.f)));
-  const float lbdr = vr + sqr * sqrtf((1.f + fmaxf((ht - hr) * ovhr * 0.5f, 0.f)) * (1.f + fmaxf((ht - hr) * ovhr, 0.f)));
+  const float tl = (ht - hl) * ovhl, tr = (ht - hr) * ovhr;
+  const float lbdl = fma_(-sql, sqrtf((1.f + fmaxf(tl * 0.5f, 0.f)) * (1.f + fmaxf(tl, 0.f))), vl);
+  const float lbdr = fma_(sqr, sqrtf((1.f + fmaxf(tr * 0.5f, 0.f)) * (1.f + fmaxf(tr, 0.f))), vr);
   *lambda = fmaxf(fabsf(lbdl), fabsf(lbdr));
+  return ok;
+}
+
+// |c_ij| lambda_max for one entry: the same operations wherever it is formed
+// (k_dt_mix for stage 1, k_low_mix otherwise), so stage 1's reuse is exact.
+__device__ __forceinline__ bool dlam_f(float cxe, float cye, float cvi, float cvj, float hi, float hj, float ovhi,
+                                       float ovhj, float sqi, float sqj, const LamK& k, float* dl) {
+  const float n2 = fma_(cxe, cxe, cye * cye);
+  const float inv = rsqrtf(n2);
+  float lam;
+  const bool ok = lambda_f(hi, hj, cvi * inv, cvj * inv, ovhi, ovhj, sqi, sqj, k, &lam);
+  *dl = (n2 * inv) * lam;
   return ok;
 }
 
 // Entry loops are processed in batches of B entries: every load of a batch is
 // issued before any of them is used, so a thread keeps B gathers in flight
-// (the kernels are latency-bound otherwise).  Sums keep the entry order; the
-// instantiations may contract FMAs differently, so batch sizes agree to FP32
-// rounding.  The autotuner picks B per kernel.
+// (the kernels are latency-bound otherwise).  Sums keep the entry order, so
+// every batch size gives the same bits.  The autotuner picks B per kernel.
 
 // Neighbour access of the entry loops: straight from HBM by column index
 // (NbGlobal), or from the block's shared-memory copy of its tile and halo
@@ -214,7 +256,15 @@ __device__ __forceinline__ int64_t tile_end(const Graph& G, const TileCtl& tc, i
   return t0 + tc.tile_rows < G.n_rows ? t0 + tc.tile_rows : G.n_rows;
 }
 
-// k_node_mix: alpha_i (SOURCES/update.f90:758-781) from the FP32 depth.
+// alpha_i (SOURCES/update.f90:758-781) from the stencil sums of the FP32
+// depth: |num| / denom, 1 where denom <= |num|, to the 8th power.
+__device__ __forceinline__ float alpha_from(float num, float denom) {
+  const float a = (denom <= fabsf(num)) ? 1.0f : fdiv(fabsf(num), denom);
+  const float a2 = a * a, a4 = a2 * a2;
+  return a4 * a4;
+}
+
+// k_node_mix: alpha_i from the FP32 depth.
 template <int B, class Nb>
 __device__ __forceinline__ void node_row(int64_t r, Graph G, const InstConst* __restrict__ C,
                                                   const InstState* __restrict__ St, StateMix u,
@@ -244,9 +294,7 @@ __device__ __forceinline__ void node_row(int64_t r, Graph G, const InstConst* __
           denom += fabsf(hj[q] - h);
         }
     }
-    const float a = (denom <= fabsf(num)) ? 1.0f : fdiv(fabsf(num), denom);
-    const float a2 = a * a, a4 = a2 * a2;
-    alpha = a4 * a4;
+    alpha = alpha_from(num, denom);
   }
   alpha_out[r] = alpha;
 }
@@ -273,16 +321,21 @@ __global__ void __launch_bounds__(256) k_node_tile(Graph G, const InstConst* __r
 }
 
 struct NodeF {   // FP32 view of one node used by the edge loop
-  float h, q1, q2, z, ovh, v1, v2;
+  float h, q1, q2, eta, ovh, v1, v2;
 };
 
 __device__ __forceinline__ NodeF node_from(const float4 a, float htiny) {
   NodeF n;
-  n.h = a.x; n.q1 = a.y; n.q2 = a.z; n.z = a.w;
+  n.h = a.x; n.q1 = a.y; n.q2 = a.z; n.eta = a.w;
   n.ovh = ovh_f(n.h, htiny);
   n.v1 = n.q1 * n.ovh;
   n.v2 = n.q2 * n.ovh;
   return n;
+}
+
+// 0.5 (g h^2 + v1 q1 + v2 q2): the entropy of the reference's entropy_residual
+__device__ __forceinline__ float entropy_f(float g, float h, float v1, float q1, float v2, float q2) {
+  return 0.5f * fma_(v2, q2, fma_(v1, q1, (g * h) * h));
 }
 
 __device__ __forceinline__ float sgn_pressure(float lambda_sgn, float g, float m, float h, float heta) {
@@ -299,6 +352,13 @@ __device__ __forceinline__ float sgn_pressure(float lambda_sgn, float g, float m
 // formed once and shared by mu_ij, lambda_max and the Galerkin flux.  The
 // diagonal entry only enters through terms that vanish identically
 // (u_i rat_ii - u_i rat_ii) and the Galerkin boundary term -c_ii.v_i.
+//
+// The smb_2_roundoff mass row h (1 + a fix) + a rk_1 is formed as
+// h + a (P - N - c_ii.v_i h) with P = sum (mu - c.v_j) h_j + (d - mu) H*_ji
+// (every term >= 0) and N = sum mu h_i + (d - mu) H*_ij [h_i > htiny]
+// (N <= h_i sum d, so a N <= CFL h_i): the reference's fix h + rk_1 with
+// rat_ij h_i = H*_ij.  At rest the two sums add equal terms in the same
+// order, so P - N is exactly 0.
 template <int B, bool LAMIN, int MINB, class Nb>
 __device__ __forceinline__ void low_row(int64_t r, Graph G, const InstConst* __restrict__ C,
                                                        const InstState* __restrict__ St, StateMix u,
@@ -327,32 +387,31 @@ __device__ __forceinline__ void low_row(int64_t r, Graph G, const InstConst* __r
   const float v2i_flux = sgn ? 0.f : ni.v2;          // flux() zeroes velocity(2) for type 13
   const float ai = alpha[r];
   const float m = G.lumpedf[r];
+  const float ghi = g * ni.h;
+  const bool wet_i = !(ni.h <= hthr);
   float ui3 = 0.f, ui4 = 0.f;
   if (S == 5) { ui3 = u.q3[r]; ui4 = u.q4[r]; }
   const float invhi = inv_pos(ni.h);
   bool delta_bad = false;
 
-  float fix = 0.f, rk0 = 0.f;
+  float P = 0.f, N = 0.f;                                          // smb_2_roundoff mass row
   float rk1 = 0.f, rk2_ = 0.f, rk3 = 0.f, rk4 = 0.f;               // smb_2_roundoff momenta
   float g0 = 0.f, g1 = 0.f, g2 = 0.f, g3 = 0.f, g4 = 0.f;          // smb_2
-  const float Ei = 0.5f * (g * ni.h * ni.h + ni.v1 * ni.q1 + v2i_flux * ni.q2);
+  const float Ei = entropy_f(g, ni.h, ni.v1, ni.q1, v2i_flux, ni.q2);
   float emax = Ei, emin = Ei;
   float ptx = 0.f, pty = 0.f;
-  {
-    // diagonal: Galerkin boundary term -c_ii.v_i (fix_roundoff / smb_2);
-    // its viscous and topography terms vanish
-    const float cxe = G.cxiif[r], cye = G.cyiif[r];
-    const float cvi = dotc(cxe, cye, ni.v1, v2i_flux);
-    fix -= cvi;
-    g0 -= cvi * ni.h;
-    rk1 -= cvi * ni.q1; rk2_ -= cvi * ni.q2;
-    g1 -= cvi * ni.q1; g2 -= cvi * ni.q2;
-    if (S == 5) { rk3 -= cvi * ui3; rk4 -= cvi * ui4; g3 -= cvi * ui3; g4 -= cvi * ui4; }
-    if (sgn) {
-      const float pt = sgn_pressure(c.lambda_sgnf, g, m, ni.h, ui3);
-      ptx -= pt * cxe;
-      pty -= pt * cye;
-    }
+  // diagonal: Galerkin boundary term -c_ii.v_i (fix_roundoff / smb_2);
+  // its viscous and topography terms vanish
+  const float cxd = G.cxiif[r], cyd = G.cyiif[r];
+  const float cvd = dotc(cxd, cyd, ni.v1, v2i_flux);
+  g0 = -cvd * ni.h;
+  rk1 = -cvd * ni.q1; rk2_ = -cvd * ni.q2;
+  g1 = rk1; g2 = rk2_;
+  if (S == 5) { rk3 = -cvd * ui3; rk4 = -cvd * ui4; g3 = rk3; g4 = rk4; }
+  if (sgn) {
+    const float pt = sgn_pressure(c.lambda_sgnf, g, m, ni.h, ui3);
+    ptx = -pt * cxd;
+    pty = -pt * cyd;
   }
   for (int k0 = 0; k0 < L; k0 += B) {
    int jb[B];
@@ -384,13 +443,8 @@ __device__ __forceinline__ void low_row(int64_t r, Graph G, const InstConst* __r
     float dlam;                                                       // |c_ij| lambda_max
     if (LAMIN) {
       dlam = dlb[q];                                                  // from k_dt_mix on this state
-    } else {
-      const float n2 = cxe * cxe + cye * cye;
-      const float inv = rsqrtf(n2);
-      float lam;
-      if (!lambda_f(ni.h, nj.h, cvi * inv, cvj * inv, ni.ovh, nj.ovh, sqi, sqrtf(g * fabsf(nj.h)), lk, &lam))
-        delta_bad = true;
-      dlam = (n2 * inv) * lam;
+    } else if (!dlam_f(cxe, cye, cvi, cvj, ni.h, nj.h, ni.ovh, nj.ovh, sqi, sqrtf(g * fabsf(nj.h)), lk, &dlam)) {
+      delta_bad = true;
     }
     float mu = fmaxf(fmaxf(-cvi, 0.f), fmaxf(cvj, 0.f));
     float d = fmaxf(dlam, mu);
@@ -400,53 +454,55 @@ __device__ __forceinline__ void low_row(int64_t r, Graph G, const InstConst* __r
     dmu[e] = make_float2(d, mu);
     // --- entropy stencil
     const float v2j_flux = sgn ? 0.f : nj.v2;
-    const float Ej = 0.5f * (g * nj.h * nj.h + nj.v1 * nj.q1 + v2j_flux * nj.q2);
+    const float Ej = entropy_f(g, nj.h, nj.v1, nj.q1, v2j_flux, nj.q2);
     emax = fmaxf(emax, Ej);
     emin = fminf(emin, Ej);
-    // --- hydrostatic reconstruction
-    const float dz = nj.z - ni.z;
-    const Recon R = recon(ni.h, nj.h, dz, invhi, inv_pos(nj.h));
-    const float rij = R.rij, rji = R.rji;                             // h <= 0 tests (smb_2)
-    const float rijt = (ni.h <= hthr) ? 0.f : rij;                    // h <= htiny tests
-    const float rjit = (nj.h <= hthr) ? 0.f : rji;
+    // --- hydrostatic reconstruction from the free surface
+    const float deta = __fsub_rn(nj.eta, ni.eta);
+    const float dz = dz_of(deta, ni.h, nj.h);
+    const Recon R = recon(ni.h, nj.h, dz);
+    const float rij = rat_of(R.Hij, ni.h, dz <= 0.f, invhi);          // h <= 0 tests (smb_2)
+    const float rji = rat_of(R.Hji, nj.h, dz >= 0.f, inv_pos(nj.h));
+    const bool wet_j = !(nj.h <= hthr);
+    const float rijt = wet_i ? rij : 0.f;                             // h <= htiny tests
+    const float rjit = wet_j ? rji : 0.f;
     const float cvj_flux = sgn ? dotc(cxe, cye, nj.v1, 0.f) : cvj;   // c.velocity_j of flux()
-    const float topo = g * ni.h * ((nj.h - ni.h) + dz);               // g h_i (eta_j - eta_i)
-    // --- smb_2_roundoff mass row (fix_roundoff, rk_1), in the reference's
-    // form: its sign properties give h^L >= 0
+    const float topo = ghi * deta;                                    // g h_i (eta_j - eta_i)
     const float dmu = d - mu;
-    fix += -mu - dmu * rijt;
-    rk0 += (mu - cvj_flux) * nj.h + fmaxf(dmu * R.Hji, 0.f);
+    // --- smb_2_roundoff mass row: P - N
+    P = fma_(dmu, R.Hji, fma_(mu - cvj_flux, nj.h, P));
+    N = fma_(dmu, wet_i ? R.Hij : 0.f, fma_(mu, ni.h, N));
     // --- smb_2 mass row and the momenta of both RHS, written as
     // -c.v_j u_j + mu (u_j - u_i) + (d - mu) (u_j rat_ji - u_i rat_ij), which
     // equals d (u_j rat_ji - u_i rat_ij) + mu (u_j (1 - rat_ji) - u_i (1 - rat_ij))
-    g0 += -cvj_flux * nj.h + mu * (nj.h - ni.h) + dmu * (nj.h * rji - ni.h * rij);
-    const float A1 = mu * (nj.q1 - ni.q1) - cvj_flux * nj.q1;
-    const float A2 = mu * (nj.q2 - ni.q2) - cvj_flux * nj.q2;
-    const float T1 = A1 + dmu * (nj.q1 * rji - ni.q1 * rij);
-    const float T2 = A2 + dmu * (nj.q2 * rji - ni.q2 * rij);
-    g1 += T1;
-    g2 += T2;
+    g0 = fma_(dmu, __fsub_rn(R.Hji, R.Hij), fma_(mu, nj.h - ni.h, fma_(-cvj_flux, nj.h, g0)));
+    const float A1 = fma_(mu, nj.q1 - ni.q1, -cvj_flux * nj.q1);
+    const float A2 = fma_(mu, nj.q2 - ni.q2, -cvj_flux * nj.q2);
+    const float T1 = fma_(dmu, fma_(nj.q1, rji, -ni.q1 * rij), A1);
+    const float T2 = fma_(dmu, fma_(nj.q2, rji, -ni.q2 * rij), A2);
+    g1 = fma_(-topo, cxe, g1 + T1);
+    g2 = fma_(-topo, cye, g2 + T2);
     if (rijt == rij && rjit == rji) {                                 // both wet: same terms
       rk1 += T1;
       rk2_ += T2;
     } else {
-      rk1 += A1 + dmu * (nj.q1 * rjit - ni.q1 * rijt);
-      rk2_ += A2 + dmu * (nj.q2 * rjit - ni.q2 * rijt);
+      rk1 += fma_(dmu, fma_(nj.q1, rjit, -ni.q1 * rijt), A1);
+      rk2_ += fma_(dmu, fma_(nj.q2, rjit, -ni.q2 * rijt), A2);
     }
-    rk1 -= topo * cxe; rk2_ -= topo * cye;
-    g1 -= topo * cxe; g2 -= topo * cye;
+    rk1 = fma_(-topo, cxe, rk1);
+    rk2_ = fma_(-topo, cye, rk2_);
     if (Nb::kGlobal && S == 5) {
       const float uj3 = u.q3[j], uj4 = u.q4[j];
-      const float A3 = mu * (uj3 - ui3) - cvj_flux * uj3;
-      const float A4 = mu * (uj4 - ui4) - cvj_flux * uj4;
-      rk3 += A3 + dmu * (uj3 * rjit - ui3 * rijt);
-      rk4 += A4 + dmu * (uj4 * rjit - ui4 * rijt);
-      g3 += A3 + dmu * (uj3 * rji - ui3 * rij);
-      g4 += A4 + dmu * (uj4 * rji - ui4 * rij);
+      const float A3 = fma_(mu, uj3 - ui3, -cvj_flux * uj3);
+      const float A4 = fma_(mu, uj4 - ui4, -cvj_flux * uj4);
+      rk3 += fma_(dmu, fma_(uj3, rjit, -ui3 * rijt), A3);
+      rk4 += fma_(dmu, fma_(uj4, rjit, -ui4 * rijt), A4);
+      g3 += fma_(dmu, fma_(uj3, rji, -ui3 * rij), A3);
+      g4 += fma_(dmu, fma_(uj4, rji, -ui4 * rij), A4);
       if (sgn) {
         const float pt = sgn_pressure(c.lambda_sgnf, g, G.lumpedf[j], nj.h, uj3);
-        ptx -= pt * cxe;
-        pty -= pt * cye;
+        ptx = fma_(-pt, cxe, ptx);
+        pty = fma_(-pt, cye, pty);
       }
     }
    }
@@ -454,14 +510,15 @@ __device__ __forceinline__ void low_row(int64_t r, Graph G, const InstConst* __r
   // source terms (update.f90:425-551)
   if (c.type_test == 9 || c.type_test == 10) {
     const float hstar = __powf(fmaxf(ni.h, htiny), 4.0f / 3.0f);
-    const float vel = c.fricf * sqrtf(ni.v1 * ni.v1 + ni.v2 * ni.v2);
+    const float vel = c.fricf * sqrtf(fma_(ni.v1, ni.v1, ni.v2 * ni.v2));
     const float hloc = vel * dtf;
     const float coef = fdiv(m * vel * 2.f, hstar + fmaxf(hstar, hloc));
-    rk1 -= coef * ni.q1; rk2_ -= coef * ni.q2;
-    g1 -= coef * ni.q1; g2 -= coef * ni.q2;
+    rk1 = fma_(-coef, ni.q1, rk1); rk2_ = fma_(-coef, ni.q2, rk2_);
+    g1 = fma_(-coef, ni.q1, g1); g2 = fma_(-coef, ni.q2, g2);
   } else if (c.type_test == 11) {
-    rk1 -= m * 0.2f * ni.q1; rk2_ -= m * 0.2f * ni.q2;
-    g1 -= m * 0.2f * ni.q1; g2 -= m * 0.2f * ni.q2;
+    const float k = m * 0.2f;
+    rk1 = fma_(-k, ni.q1, rk1); rk2_ = fma_(-k, ni.q2, rk2_);
+    g1 = fma_(-k, ni.q1, g1); g2 = fma_(-k, ni.q2, g2);
   } else if (c.type_test == 12) {
     const float a1 = m * 2.0f * ni.q2, a2 = m * 2.0f * ni.q1;
     rk1 += a1; rk2_ -= a2; g1 += a1; g2 -= a2;
@@ -471,8 +528,8 @@ __device__ __forceinline__ void low_row(int64_t r, Graph G, const InstConst* __r
     const float x = fdiv(ui3, ni.h * ni.h);
     const float s_i = 3.f * pc * t * t * 12.f * (x - 1.f);
     rk1 += ptx; rk2_ += pty; g1 += ptx; g2 += pty;
-    rk3 += m * ui4; rk4 -= m * s_i;
-    g3 += m * ui4; g4 -= m * s_i;
+    rk3 = fma_(m, ui4, rk3); rk4 = fma_(-m, s_i, rk4);
+    g3 = fma_(m, ui4, g3); g4 = fma_(-m, s_i, g4);
   }
   // low-order state: double-float depth plus an FP32 increment
   const float invm = G.inv_lumpedf[r];
@@ -480,24 +537,24 @@ __device__ __forceinline__ void low_row(int64_t r, Graph G, const InstConst* __r
   const float2 h = u.h[r];
   float2 hL;
   if (roundoff) {
-    hL = df_add_f(h, a * __fmaf_rn(fix, ni.h, rk0));   // h + a (fix h + rk_1), a |fix| <= CFL
-  } else {                                             // smb_2 and MAX(h + dt rk, 0)
+    hL = df_add_f(h, a * fma_(-cvd, ni.h, P - N));   // h + a (fix h + rk_1), a N <= CFL h
+  } else {                                            // smb_2 and MAX(h + dt rk, 0)
     hL = df_add_f(h, a * g0);
     if (hL.x < 0.f) hL = make_float2(0.f, 0.f);
   }
   w.hL[r] = hL;
-  w.qL[r] = make_float2(ni.q1 + dtf * (rk1 * invm), ni.q2 + dtf * (rk2_ * invm));
-  if (S == 5) { w.q3L[r] = ui3 + dtf * (rk3 * invm); w.q4L[r] = ui4 + dtf * (rk4 * invm); }
+  w.qL[r] = make_float2(fma_(dtf, rk1 * invm, ni.q1), fma_(dtf, rk2_ * invm, ni.q2));
+  if (S == 5) { w.q3L[r] = fma_(dtf, rk3 * invm, ui3); w.q4L[r] = fma_(dtf, rk4 * invm, ui4); }
   // entropy residual (update.f90:838-868), rescale once per node
-  const float un0 = ni.h + dtf * (g0 * invm);
-  const float un1 = ni.q1 + dtf * (g1 * invm);
-  const float un2 = ni.q2 + dtf * (g2 * invm);
+  const float un0 = fma_(dtf, g0 * invm, ni.h);
+  const float un1 = fma_(dtf, g1 * invm, ni.q1);
+  const float un2 = fma_(dtf, g2 * invm, ni.q2);
   const float on = ovh_f(un0, htiny);
-  const float En = 0.5f * (g * un0 * un0 + (un1 * on) * un1 + (un2 * on) * un2);
-  const float Ep0 = g * ni.h - 0.5f * (ni.v1 * ni.v1) - 0.5f * (v2i_flux * v2i_flux);
+  const float En = entropy_f(g, un0, un1 * on, un1, un2 * on, un2);
+  const float Ep0 = fma_(-0.5f * v2i_flux, v2i_flux, fma_(-0.5f * ni.v1, ni.v1, g * ni.h));
   float rs = m * (En - Ei) * st.inv_dtf;
-  rs -= g0 * Ep0 + g1 * ni.v1 + g2 * v2i_flux;
-  const float rescale = 0.5f * fabsf(emax - emin) + c.rescale_floorf;
+  rs -= fma_(g2, v2i_flux, fma_(g1, ni.v1, g0 * Ep0));
+  const float rescale = fma_(0.5f, fabsf(emax - emin), c.rescale_floorf);
   res[r] = fdiv(fabsf(rs), rescale);
   if (delta_bad) atomicOr(err, ERRB_DELTA);
 }
@@ -535,10 +592,14 @@ __global__ void __launch_bounds__(256, MINB) k_low_tile(Graph G, const InstConst
 // removes more than h^L from a node.
 constexpr float kLimiterShrink = 1.0f - 3.814697265625e-6f;
 
+// f_ij with the high-order viscosities MIN(d, res_ij), MIN(mu, res_ij)
+// (update.f90:233-239, 721-748) for one entry; k_fct and k_update share it.
+__device__ __forceinline__ float fct_entry(float d0, float m0, float rij, float hi, float hj, const Recon& R) {
+  return fct_from(fminf(d0, rij) - d0, fminf(m0, rij) - m0, hi, hj, R);
+}
+
 // k_fct_mix: f_ij and the limiter R^-_i (fct.f90:15-30): P^- = sum f^- - 1e-15,
-// Q^- = -m h^L/dt, R^- = min(Q^-/P^-, 1), 0 where m h^L/dt <= htiny.  Also
-// stores R^-_i P_i (the limited negative part of the h-row, reused by the
-// update).
+// Q^- = -m h^L/dt, R^- = min(Q^-/P^-, 1), 0 where m h^L/dt <= htiny.
 template <int B, class Nb>
 __device__ __forceinline__ void fct_row(int64_t r, Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St, StateMix u,
                           const float2* __restrict__ dmu, WorkMix w, const float* __restrict__ res,
@@ -552,8 +613,7 @@ __device__ __forceinline__ void fct_row(int64_t r, Graph G, const InstConst* __r
   if (c.visc != VISC_FCT) return;
   const int64_t base = entry_base(G, r);
   const float4 ni = u.nq[r];
-  const float hi = ni.x, zi = ni.w, resi = res[r];
-  const float invhi = inv_pos(hi);
+  const float hi = ni.x, etai = ni.w, resi = res[r];
   float neg = 0.f;                       // f_ii = 0 adds nothing
   for (int k0 = 0; k0 < L; k0 += B) {
     int jb[B];
@@ -574,10 +634,9 @@ __device__ __forceinline__ void fct_row(int64_t r, Graph G, const InstConst* __r
 #pragma unroll
     for (int q = 0; q < B; q++) {
       if (k0 + q >= L) break;
-      const float d0 = d0b[q], m0 = m0b[q], rij = fmaxf(resi, rsb[q]);
       const float4 nj = njb[q];
-      const Recon R = recon(hi, nj.x, nj.w - zi, invhi, inv_pos(nj.x));
-      const float f = fct_from(fminf(d0, rij) - d0, fminf(m0, rij) - m0, hi, nj.x, R);
+      const Recon R = recon(hi, nj.x, dz_of(__fsub_rn(nj.w, etai), hi, nj.x));
+      const float f = fct_entry(d0b[q], m0b[q], fmaxf(resi, rsb[q]), hi, nj.x, R);
       if (f < 0.f) neg = __fadd_rn(neg, f);
     }
   }
@@ -594,7 +653,6 @@ __device__ __forceinline__ void fct_row(int64_t r, Graph G, const InstConst* __r
     R = (Q >= mP) ? 1.f : __fdiv_rn(Q, mP);
   }
   w.rminus[r] = R;
-  w.rneg[r] = __fmul_rn(R, neg);
 }
 
 template <int B>
@@ -620,9 +678,10 @@ __global__ void __launch_bounds__(256) k_fct_tile(Graph G, const InstConst* __re
 }
 
 // End of a stage for one row: non-finite check, the SSP-RK combination and
-// bdy of the time loop (main.f90:77-90) when rk_stage > 0, and the store.
+// bdy of the time loop (main.f90:77-90) when rk_stage > 0, and the store of
+// the double-float depth and the node record with its free surface.
 __device__ __forceinline__ void finish_mix(const Graph& G, const InstConst& c, int64_t r, int S, float2 hn, float q1,
-                                           float q2, float q3, float q4, float zi, int rk_stage, const StateMix& u0,
+                                           float q2, float q3, float q4, int rk_stage, const StateMix& u0,
                                            const StateMix& out, unsigned* err) {
   if (!(hn.x == hn.x) || !(q1 == q1) || !(q2 == q2)) atomicOr(err, ERRB_NAN);
   if (rk_stage >= 2) {
@@ -630,14 +689,14 @@ __device__ __forceinline__ void finish_mix(const Graph& G, const InstConst& c, i
     const float2 h0 = u0.h[r];
     if (rk_stage == 2) {
       hn = df_scale(df_add(df_mul_f(h0, 3.f), hn), 0.25f);
-      q1 = (3.f * a0.y + q1) * 0.25f;
-      q2 = (3.f * a0.z + q2) * 0.25f;
-      if (S == 5) { q3 = (3.f * u0.q3[r] + q3) * 0.25f; q4 = (3.f * u0.q4[r] + q4) * 0.25f; }
+      q1 = fma_(3.f, a0.y, q1) * 0.25f;
+      q2 = fma_(3.f, a0.z, q2) * 0.25f;
+      if (S == 5) { q3 = fma_(3.f, u0.q3[r], q3) * 0.25f; q4 = fma_(3.f, u0.q4[r], q4) * 0.25f; }
     } else {
       hn = df_div3(df_add(h0, df_scale(hn, 2.f)));
-      q1 = (a0.y + 2.f * q1) * (1.f / 3.f);
-      q2 = (a0.z + 2.f * q2) * (1.f / 3.f);
-      if (S == 5) { q3 = (u0.q3[r] + 2.f * q3) * (1.f / 3.f); q4 = (u0.q4[r] + 2.f * q4) * (1.f / 3.f); }
+      q1 = fma_(2.f, q1, a0.y) * (1.f / 3.f);
+      q2 = fma_(2.f, q2, a0.z) * (1.f / 3.f);
+      if (S == 5) { q3 = fma_(2.f, q3, u0.q3[r]) * (1.f / 3.f); q4 = fma_(2.f, q4, u0.q4[r]) * (1.f / 3.f); }
     }
   }
   if (rk_stage >= 1 && G.dir_mask) {
@@ -651,13 +710,15 @@ __device__ __forceinline__ void finish_mix(const Graph& G, const InstConst& c, i
     }
   }
   out.h[r] = hn;
-  out.nq[r] = make_float4(shadow_df(hn, c), q1, q2, zi);
+  out.nq[r] = make_float4(shadow_df(hn, c), q1, q2, eta_of(hn, G.bathdf[r]));
   if (S == 5) { out.q3[r] = q3; out.q4[r] = q4; }
 }
 
 // k_update_mix: limited antidiffusion (update.f90:276-282, apply_viscosity
 // :684-718), RK combination and Dirichlet data (main.f90:77-90).  The h-row
-// sum is R^-_i P_i (from k_fct_mix) plus sum_{f_ij >= 0} R^-_j f_ij.
+// sum is R^-_i P_i plus sum_{f_ij >= 0} R^-_j f_ij, with P_i = sum_{f_ij < 0}
+// f_ij formed in the entry order of k_fct_mix (the same value, bit for bit,
+// as the one the limiter saw).
 template <int B, class Nb>
 __device__ __forceinline__ void update_row(int64_t r, Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St,
                              StateMix u, const float2* __restrict__ dmu, WorkMix w,
@@ -673,17 +734,17 @@ __device__ __forceinline__ void update_row(int64_t r, Graph G, const InstConst* 
   const float4 ni = u.nq[r];
   if (c.visc != VISC_FCT) {                     // 'galerkin' / 'viscous': u^L is the result
     const float2 qL = w.qL[r];
-    finish_mix(G, c, r, S, w.hL[r], qL.x, qL.y, S == 5 ? w.q3L[r] : 0.f, S == 5 ? w.q4L[r] : 0.f, ni.w, rk_stage,
-               u0, out, err);
+    finish_mix(G, c, r, S, w.hL[r], qL.x, qL.y, S == 5 ? w.q3L[r] : 0.f, S == 5 ? w.q4L[r] : 0.f, rk_stage, u0,
+               out, err);
     return;
   }
   const int64_t base = entry_base(G, r);
-  const float hi = ni.x, zi = ni.w, resi = res[r];
+  const float hi = ni.x, etai = ni.w, resi = res[r];
   const float invhi = inv_pos(hi);
   const float Ri = w.rminus[r];
   float ui3 = 0.f, ui4 = 0.f;
   if (S == 5) { ui3 = u.q3[r]; ui4 = u.q4[r]; }
-  float pos = 0.f;                       // sum_{f >= 0} R_j f_ij
+  float neg = 0.f, pos = 0.f;            // sum_{f < 0} f_ij, sum_{f >= 0} R_j f_ij
   float x1 = 0.f, x2 = 0.f, x3 = 0.f, x4 = 0.f;
   for (int k0 = 0; k0 < L; k0 += B) {    // the diagonal's terms vanish: u_i rat_ii - u_i rat_ii = 0
    int jb[B];
@@ -708,35 +769,39 @@ __device__ __forceinline__ void update_row(int64_t r, Graph G, const InstConst* 
     const float d0 = d0b[q], m0 = m0b[q];
     const float rij = fmaxf(resi, rsb[q]);
     const float ddr = fminf(d0, rij) - d0, dmr = fminf(m0, rij) - m0;
-    const Recon R = recon(hi, nj.x, nj.w - zi, invhi, inv_pos(nj.x));
+    const float dz = dz_of(__fsub_rn(nj.w, etai), hi, nj.x);
+    const Recon R = recon(hi, nj.x, dz);
     const float f = fct_from(ddr, dmr, hi, nj.x, R);
     float lf = Ri;
     if (f >= 0.f) { lf = Rjb[q]; pos = __fmaf_rn(lf, f, pos); }
+    else neg = __fadd_rn(neg, f);
+    const float rij_ = rat_of(R.Hij, hi, dz <= 0.f, invhi);
+    const float rji_ = rat_of(R.Hji, nj.x, dz >= 0.f, inv_pos(nj.x));
     // l (dd (u_j rat_ji - u_i rat_ij) + dm (u_j (1 - rat_ji) - u_i (1 - rat_ij)))
     // = l (dm (u_j - u_i) + (dd - dm) (u_j rat_ji - u_i rat_ij))
     const float dm = dmr * lf, dx = (ddr - dmr) * lf;
-    x1 += dm * (nj.y - ni.y) + dx * (nj.y * R.rji - ni.y * R.rij);
-    x2 += dm * (nj.z - ni.z) + dx * (nj.z * R.rji - ni.z * R.rij);
+    x1 = fma_(dx, fma_(nj.y, rji_, -ni.y * rij_), fma_(dm, nj.y - ni.y, x1));
+    x2 = fma_(dx, fma_(nj.z, rji_, -ni.z * rij_), fma_(dm, nj.z - ni.z, x2));
     if constexpr (Nb::kGlobal) {
       if (S == 5) {
         const int j = jb[q];
         const float uj3 = u.q3[j], uj4 = u.q4[j];
-        x3 += dm * (uj3 - ui3) + dx * (uj3 * R.rji - ui3 * R.rij);
-        x4 += dm * (uj4 - ui4) + dx * (uj4 * R.rji - ui4 * R.rij);
+        x3 = fma_(dx, fma_(uj3, rji_, -ui3 * rij_), fma_(dm, uj3 - ui3, x3));
+        x4 = fma_(dx, fma_(uj4, rji_, -ui4 * rij_), fma_(dm, uj4 - ui4, x4));
       }
     }
    }
   }
   const float invm = G.inv_lumpedf[r], dtf = st.dtf;
-  const float sh = __fadd_rn(w.rneg[r], pos);
+  const float sh = __fadd_rn(__fmul_rn(Ri, neg), pos);
   const float2 hn = df_add_f(w.hL[r], __fmul_rn(__fmul_rn(dtf, invm), sh));
   const float2 qL = w.qL[r];
-  const float q1 = qL.x + dtf * (x1 * invm);
-  const float q2 = qL.y + dtf * (x2 * invm);
+  const float q1 = fma_(dtf, x1 * invm, qL.x);
+  const float q2 = fma_(dtf, x2 * invm, qL.y);
   float q3 = 0.f, q4 = 0.f;
-  if (S == 5) { q3 = w.q3L[r] + dtf * (x3 * invm); q4 = w.q4L[r] + dtf * (x4 * invm); }
+  if (S == 5) { q3 = fma_(dtf, x3 * invm, w.q3L[r]); q4 = fma_(dtf, x4 * invm, w.q4L[r]); }
   if (hn.x < 0.f) atomicOr(err, ERRB_NEG_H);   // check_hmin (update.f90:285)
-  finish_mix(G, c, r, S, hn, q1, q2, q3, q4, zi, rk_stage, u0, out, err);
+  finish_mix(G, c, r, S, hn, q1, q2, q3, q4, rk_stage, u0, out, err);
 }
 
 template <int B>
@@ -764,11 +829,11 @@ __global__ void __launch_bounds__(256) k_update_tile(Graph G, const InstConst* _
     update_row<B>(r, G, C, St, u, dmu, w, res, u0, out, rk_stage, err, nb);
 }
 
-// k_dt_mix: FP32 lambda_max, max |d_ii|/m_i per instance (main.f90:166-174).
-// It walks the neighbours of the state that stage 1 starts from, so it also
-// stores |c_ij| lambda_max per entry (dlam, reused by stage 1's k_low_mix)
-// and alpha_i (alpha_out, stage 1's k_node_mix), when those are non-null.
-// One row of k_dt_mix; returns |d_ii| / m_i (0 for padding and finished rows).
+// One row of k_dt_mix: FP32 lambda_max, |d_ii| / m_i (main.f90:166-174; 0 for
+// padding and finished rows).  It walks the neighbours of the state that
+// stage 1 starts from, so it also stores |c_ij| lambda_max per entry (dlam,
+// reused by stage 1's k_low_mix) and alpha_i (alpha_out, stage 1's
+// k_node_mix), when those are non-null.
 template <int B, class Nb>
 __device__ __forceinline__ float dt_row(int64_t r, const Graph& G, const InstConst* __restrict__ C,
                                         const InstState* __restrict__ St, const StateMix& u, float* __restrict__ dlam,
@@ -806,34 +871,23 @@ __device__ __forceinline__ float dt_row(int64_t r, const Graph& G, const InstCon
       if (k0 + q >= L) break;
       const NodeF nj = node_from(njb[q], htiny);
       const float cxe = cxb[q], cye = cyb[q];
-      const float n2 = cxe * cxe + cye * cye;
-      const float inv = rsqrtf(n2);
-      float lam;
-      if (!lambda_f(ni.h, nj.h, dotc(cxe, cye, ni.v1, ni.v2) * inv, dotc(cxe, cye, nj.v1, nj.v2) * inv, ni.ovh,
-                    nj.ovh, sqi, sqrtf(g * fabsf(nj.h)), lk, &lam))
+      float dl;
+      if (!dlam_f(cxe, cye, dotc(cxe, cye, ni.v1, ni.v2), dotc(cxe, cye, nj.v1, nj.v2), ni.h, nj.h, ni.ovh, nj.ovh,
+                  sqi, sqrtf(g * fabsf(nj.h)), lk, &dl))
         bad = true;
-      const float dl = (n2 * inv) * lam;
       if (dlam) dlam[base + 32 * (k0 + q)] = dl;
       s += dl;
       num += nj.h - ni.h;
       denom += fabsf(nj.h - ni.h);
     }
   }
-  if (alpha_out) {
-    float alpha = 1.0f;
-    if (c.alpha_limit && !(ni.h <= c.htinyf)) {
-      const float a = (denom <= fabsf(num)) ? 1.0f : fdiv(fabsf(num), denom);
-      const float a2 = a * a, a4 = a2 * a2;
-      alpha = a4 * a4;
-    }
-    alpha_out[r] = alpha;
-  }
+  if (alpha_out) alpha_out[r] = (c.alpha_limit && !(ni.h <= c.htinyf)) ? alpha_from(num, denom) : 1.0f;
   if (bad) atomicOr(err, ERRB_DELTA);
   return s * G.inv_lumpedf[r];
 }
 
 // Warp max of |d_ii| / m_i into the instance's maximum (the 32 rows of a warp
-// are one slice, so one instance).
+// are one slice, so one instance).  A maximum does not depend on the order.
 __device__ __forceinline__ void dt_reduce(float val, int64_t r, const Graph& G, InstState* __restrict__ St) {
   for (int off = 16; off > 0; off >>= 1) val = fmaxf(val, __shfl_down_sync(0xffffffffu, val, off));
   const int64_t r0 = r & ~(int64_t)31;
@@ -845,9 +899,6 @@ __device__ __forceinline__ void dt_reduce(float val, int64_t r, const Graph& G, 
 }
 
 // k_dt_mix: FP32 lambda_max, max |d_ii|/m_i per instance (main.f90:166-174).
-// It walks the neighbours of the state that stage 1 starts from, so it also
-// stores |c_ij| lambda_max per entry (dlam, reused by stage 1's k_low_mix)
-// and alpha_i (alpha_out, stage 1's k_node_mix), when those are non-null.
 template <int B>
 __global__ void __launch_bounds__(256) k_dt_mix(Graph G, const InstConst* __restrict__ C, InstState* __restrict__ St, StateMix u,
                          float* __restrict__ dlam, float* __restrict__ alpha_out, unsigned* __restrict__ err) {
@@ -876,35 +927,11 @@ __global__ void __launch_bounds__(256) k_dt_tile(Graph G, const InstConst* __res
   }
 }
 
-// Copy the bathymetry into the packed node records after a bathymetry change
-__global__ void k_refresh_z(Graph G, StateMix u) {
+// Free surface of the packed node records after a bathymetry change
+__global__ void k_refresh_eta(Graph G, StateMix u) {
   int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= G.n_rows) return;
-  u.nq[r].w = G.bathf[r];
-}
-
-// Total mass sum m_i h_i per instance from the double-float depth, combined
-// in double-double per warp (atomics on two words per instance).
-__global__ void k_mass_mix(Graph G, const float2* __restrict__ h, double* __restrict__ acc) {
-  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  double v = 0.0;
-  int b = -1;
-  if (r < G.n_rows && G.len[r] > 0) { b = G.slice_inst[r >> 5]; v = G.lumped[r] * df_to_double(h[r]); }
-  double cmp = 0.0;
-  for (int off = 16; off > 0; off >>= 1) {
-    const double o = __shfl_down_sync(0xffffffffu, v, off);
-    const double oc = __shfl_down_sync(0xffffffffu, cmp, off);
-    const double s = v + o;              // two-sum
-    const double bb = s - v;
-    const double e = (v - (s - bb)) + (o - bb);
-    v = s;
-    cmp = cmp + oc + e;
-  }
-  const int b0 = __shfl_sync(0xffffffffu, b, 0);
-  if ((threadIdx.x & 31) == 0 && b0 >= 0) {
-    atomicAdd(&acc[2 * b0], v);
-    atomicAdd(&acc[2 * b0 + 1], cmp);
-  }
+  u.nq[r].w = eta_of(u.h[r], G.bathdf[r]);
 }
 
 static inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
@@ -1037,12 +1064,8 @@ void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const Stat
   }
 }
 
-void launch_refresh_z(const Graph& G, StateMix u, cudaStream_t s) {
-  k_refresh_z<<<nblk(G.n_rows, 256), 256, 0, s>>>(G, u);
-}
-
-void launch_mass_mix(const Graph& G, const float2* h, double* acc, cudaStream_t s) {
-  k_mass_mix<<<nblk(G.n_rows, 256), 256, 0, s>>>(G, h, acc);
+void launch_refresh_eta(const Graph& G, StateMix u, cudaStream_t s) {
+  k_refresh_eta<<<nblk(G.n_rows, 256), 256, 0, s>>>(G, u);
 }
 
 }  // namespace swe

@@ -22,6 +22,10 @@
 //  * The first call on a device looks up the array's device address with
 //    cudaGetSymbolAddress while that device is current, once per device.  Make
 //    that first call before any stream capture.
+//  * d_ia and d_ja must form a valid 1-based CSR structure of the caller's
+//    d_mat / d_lij arrays (ia(1) = 1, non-decreasing).  Column indices are
+//    checked on the device: a column outside 1..np is not read through, and
+//    the call returns SWE_ERR_ARG (d_lij is then unspecified).
 //  * No cudaMalloc, cudaFree or allocating library routine is called.
 #include <cuda_runtime.h>
 
@@ -32,16 +36,21 @@
 namespace {
 
 static __device__ __align__(256) double g_rminus_scratch[SWE_NOALLOC_MAX_NODES];
+// set by the kernels when the CSR structure is out of range (cleared per call)
+static __device__ unsigned g_noalloc_bad;
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 double* g_scratch_addr[kMaxDevices] = {nullptr};
+unsigned* g_bad_addr[kMaxDevices] = {nullptr};
 
 // R^-_i (fct.f90:15-30): P^- = -1e-15 + sum_{f_ij<0} f_ij in CSR order,
 // R^- = min(Q^-/P^-, 1) with Q^- = 0 - unext, 0 where unext <= htiny.
 __global__ void k_noalloc_rminus(int np, const int* __restrict__ ia, const double* __restrict__ unext,
-                                 const double* __restrict__ mat, double htiny, double* __restrict__ rminus) {
+                                 const double* __restrict__ mat, double htiny, double* __restrict__ rminus,
+                                 unsigned* __restrict__ bad) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+    if ((i == 0 && ia[0] != 1) || ia[i + 1] < ia[i]) atomicOr(bad, 1u);
     double P = -1.e-15;
     for (int p = ia[i] - 1; p < ia[i + 1] - 1; p++) {
       const double f = mat[p];
@@ -56,25 +65,37 @@ __global__ void k_noalloc_rminus(int np, const int* __restrict__ ia, const doubl
 }
 
 // l_ij = R^-_j if f_ij >= 0 else R^-_i (fct.f90:31-41)
+// A column outside 1..np is flagged and not read through.
 __global__ void k_noalloc_lij(int np, const int* __restrict__ ia, const int* __restrict__ ja,
                               const double* __restrict__ mat, const double* __restrict__ rminus,
-                              double* __restrict__ lij) {
+                              double* __restrict__ lij, unsigned* __restrict__ bad) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
     const double Ri = rminus[i];
-    for (int p = ia[i] - 1; p < ia[i + 1] - 1; p++) lij[p] = (mat[p] >= 0.0) ? rminus[ja[p] - 1] : Ri;
+    for (int p = ia[i] - 1; p < ia[i + 1] - 1; p++) {
+      const int j = ja[p];
+      if (j < 1 || j > np) {
+        atomicOr(bad, 2u);
+        continue;
+      }
+      lij[p] = (mat[p] >= 0.0) ? rminus[j - 1] : Ri;
+    }
   }
 }
 
-int scratch_address(double** out) {
+int scratch_address(double** out, unsigned** bad) {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return SWE_ERR_CUDA;
   std::lock_guard<std::mutex> lock(g_setup_mutex);
   if (!g_scratch_addr[dev]) {
     void* p = nullptr;
+    void* q = nullptr;
     if (cudaGetSymbolAddress(&p, g_rminus_scratch) != cudaSuccess || !p) return SWE_ERR_CUDA;
+    if (cudaGetSymbolAddress(&q, g_noalloc_bad) != cudaSuccess || !q) return SWE_ERR_CUDA;
     g_scratch_addr[dev] = static_cast<double*>(p);
+    g_bad_addr[dev] = static_cast<unsigned*>(q);
   }
   *out = g_scratch_addr[dev];
+  *bad = g_bad_addr[dev];
   return SWE_OK;
 }
 
@@ -86,14 +107,20 @@ extern "C" __attribute__((visibility("default"))) int swe_fct_positivity_noalloc
   if (np <= 0 || !d_ia || !d_ja || !d_unext || !d_mat || !d_lij) return SWE_ERR_ARG;
   if (np > SWE_NOALLOC_MAX_NODES) return SWE_ERR_ARG;
   double* rminus = nullptr;
-  int rc = scratch_address(&rminus);
+  unsigned* bad = nullptr;
+  int rc = scratch_address(&rminus, &bad);
   if (rc) return rc;
+  // an error left by earlier, unrelated launches is not this call's
+  (void)cudaGetLastError();
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int bs = 256;
   const int nb = (np + bs - 1) / bs;
-  k_noalloc_rminus<<<nb, bs, 0, s>>>(np, d_ia, d_unext, d_mat, htiny, rminus);
-  k_noalloc_lij<<<nb, bs, 0, s>>>(np, d_ia, d_ja, d_mat, rminus, d_lij);
+  unsigned flag = 0;
+  if (cudaMemsetAsync(bad, 0, sizeof(unsigned), s) != cudaSuccess) return SWE_ERR_CUDA;
+  k_noalloc_rminus<<<nb, bs, 0, s>>>(np, d_ia, d_unext, d_mat, htiny, rminus, bad);
+  k_noalloc_lij<<<nb, bs, 0, s>>>(np, d_ia, d_ja, d_mat, rminus, d_lij, bad);
   if (cudaGetLastError() != cudaSuccess) return SWE_ERR_CUDA;
+  if (cudaMemcpyAsync(&flag, bad, sizeof(unsigned), cudaMemcpyDeviceToHost, s) != cudaSuccess) return SWE_ERR_CUDA;
   if (cudaStreamSynchronize(s) != cudaSuccess) return SWE_ERR_CUDA;
-  return SWE_OK;
+  return flag ? SWE_ERR_ARG : SWE_OK;
 }

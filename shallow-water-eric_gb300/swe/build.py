@@ -3,8 +3,10 @@
 Translation units are compiled in parallel into ``_build/`` and linked
 in-tree next to this package.  The FP64 kernels are compiled without FMA
 contraction (they reproduce the FP64 restatement bit for bit); the mixed
-kernels use fast single-precision intrinsics; host setup code is compiled
-with -ffp-contract=off so its matrices are identical on x86-64 and aarch64.
+kernels use approximate single-precision division and square root, and no
+contraction either (their fused multiply-adds are written out, so every
+launch variant gives the same bits); host setup code is compiled with
+-ffp-contract=off so its matrices are identical on x86-64 and aarch64.
 """
 from __future__ import annotations
 
@@ -26,7 +28,11 @@ NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibili
 
 UNITS = {
     "swe_kernels_f64.cu": ["-fmad=false"],
-    "swe_kernels_mixed.cu": ["--use_fast_math", "-Xptxas", "-warn-spills"],
+    # approximate FP32 division and square root, flush-to-zero, and no FMA
+    # contraction: the kernels spell out every fused multiply-add, so every
+    # launch variant performs the same operations and gives the same bits
+    "swe_kernels_mixed.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false", "-fmad=false",
+                             "-Xptxas", "-warn-spills"],
     "swe_api.cu": [],
     "swe_noalloc.cu": ["-fmad=false"],
     "swe_setup_gpu.cu": ["-fmad=false"],

@@ -38,7 +38,7 @@ EXPORTS = [
     "swe_set_time", "swe_rk3_steps", "swe_mass", "swe_last_launch_count", "swe_tuning",
     "swe_last_device_ms", "swe_profile_kernels", "swe_fct_positivity_noalloc", "swe_autotune",
     "swe_write_vtk_2d", "swe_frame_fields", "swe_frame_async", "swe_frames_wait", "swe_gauges_set",
-    "swe_gauges_read", "swe_get_time",
+    "swe_gauges_read", "swe_get_time", "swe_set_tuning",
 ]
 NOALLOC_MAX_NODES = 1 << 20   # SWE_NOALLOC_MAX_NODES
 KERNEL_KINDS = ("dt", "node", "low", "fct", "update")
@@ -96,6 +96,7 @@ def load(build: bool = True):
         "swe_tuning": ([vp], ctypes.c_char_p),
         "swe_last_device_ms": ([vp], ctypes.c_double),
         "swe_autotune": ([vp], ctypes.c_int),
+        "swe_set_tuning": ([vp, ctypes.c_char_p], ctypes.c_int),
         "swe_profile_kernels": ([vp, ctypes.c_int, dp], ctypes.c_int),
         "swe_fct_positivity_noalloc": ([ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p],

@@ -251,12 +251,17 @@ class Update:
         return t, tf, dt
 
     def save_checkpoint(self, path):
-        """The state and the instances' clocks as raw FP64 (npz): resuming
-        from it continues the run bit for bit (the mixed state's double-float
-        depth and FP32 momenta round-trip exactly through FP64)."""
+        """The state and the instances' clocks as raw FP64 (npz), with the
+        launch configuration: resuming from it continues the run bit for bit
+        (the mixed state's double-float depth and FP32 momenta round-trip
+        exactly through FP64, and every launch variant gives the same bits;
+        the stored configuration keeps the resumed run's launch shapes)."""
         t, tf, dt = self.get_time()
+        tuning = self.tuning
+        spec = tuning.split("autotuned ", 1)[1] if "autotuned " in tuning else (
+            tuning.split("fixed ", 1)[1] if "fixed " in tuning else "")
         np.savez(path, un=self.download(), time=t, t_final=tf, dt=dt, np_=self.np_, me=self._me,
-                 S=self.S, precision=self.params[0].precision)
+                 S=self.S, precision=self.params[0].precision, tuning=np.array(spec))
 
     def load_checkpoint(self, path):
         with np.load(path) as z:
@@ -265,6 +270,14 @@ class Update:
                 raise ValueError("checkpoint of another mesh, system or precision")
             self.upload(z["un"])
             self.set_time(z["time"], z["t_final"])
+            spec = str(z["tuning"]) if "tuning" in z.files else ""
+        if spec:
+            self.set_tuning(spec)
+
+    def set_tuning(self, spec):
+        """Launch exactly the variants of a tuning description (the text
+        after "autotuned " in `tuning`) without timing."""
+        self._check(self._L.swe_set_tuning(self.h, spec.encode()))
 
     def rk3_steps(self, nsteps):
         t = np.zeros(self.n_inst); dt = np.zeros(self.n_inst); n = ctypes.c_int()

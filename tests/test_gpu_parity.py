@@ -265,9 +265,8 @@ def test_batch_tiled_mixed_equals_single_instances(monkeypatch):
     """Mixed path with every kernel in its shared-memory tile variant and
     64-row tiles, so that tiles straddle instances (row offsets are padded to
     32 only): a batch of three instances against each instance alone.  The
-    two may run other entry batches (FMA contraction), and the dam breaks'
-    shocks amplify that FP32 rounding: relative L1 of h <= 1e-6, every
-    component within 5e-5 of its maximum."""
+    two may run other launch variants, which perform the same operations:
+    bit for bit."""
     monkeypatch.setenv("SWE_TILED", "1")
     monkeypatch.setenv("SWE_TILE", "64")
     cases = C.batch_instances(n_inst=3, nmin=200, nmax=2000, seed=11, precision=1)
@@ -288,9 +287,7 @@ def test_batch_tiled_mixed_equals_single_instances(monkeypatch):
         one.rk3_steps(12)
         ref = one.download()
         one.close()
-        assert np.sum(np.abs(got[b][0] - ref[0])) <= 1e-6 * np.sum(np.abs(ref[0])), b
-        scale = np.abs(ref).max(axis=1, keepdims=True) + 1e-300
-        assert np.max(np.abs(got[b] - ref) / scale) < 5e-5, b
+        np.testing.assert_array_equal(got[b], ref, err_msg=str(b))
 
 
 def test_negative_depth_is_reported_not_trapped():
@@ -357,13 +354,112 @@ def test_mixed_precision_thacker_within_conditioning(golden):
     assert err <= 3 * sens + MIXED_L1_TOL, (err, sens)
 
 
-def test_mass_monitor():
+@pytest.mark.parametrize("prec", [0, 1])
+def test_mass_monitor(prec):
+    """swe_mass adds in a fixed order: the same bits on every call, equal to
+    the host's compensated sum to rounding."""
     case = C.dam_break_case(n=21)
-    upd = from_case(case)
+    upd = from_case(case, precision=prec)
     upd.upload(case.u0)
     m = upd.total_mass()[0]
     lump = upd.lumped
-    assert m == pytest.approx(float(np.sum(lump * case.u0[0])), rel=1e-15)
+    assert m == pytest.approx(math.fsum(lump * case.u0[0]), rel=1e-15)
+    upd.set_time(0.0, 1e30)
+    upd.rk3_steps(3)
+    m3 = upd.total_mass()
+    for _ in range(3):
+        np.testing.assert_array_equal(upd.total_mass(), m3)
+    upd.close()
+
+
+# Relative mass drift bounds.  In a closed basin whose walls the waves have
+# not reached, the reference scheme conserves mass to rounding; the mixed
+# path's fluxes are FP32 numbers formed independently by the two rows of an
+# edge, so its mass moves by the FP32 rounding of the fluxes.
+MASS_DRIFT_TOL = {0: 1e-13, 1: 1e-7}
+
+
+def _circular_dam(prec):
+    mesh = M.lattice_mesh(101, 101)
+    x, y = mesh["rr"]
+    h = np.where((x - 0.5) ** 2 + (y - 0.5) ** 2 < 0.04, 1.0, 0.1)
+    u0 = np.asfortranarray(np.vstack([h, 0 * h, 0 * h]))
+    p = C.Params(gravity=9.81, cfl=0.25, max_water_h=1.0, htiny=1e-4, type_test=4, precision=prec)
+    return C.Case("circular_dam", mesh, p, np.zeros_like(h), u0, 1e30, C._walls(mesh, 3))
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_mass_conserved_in_a_closed_basin(prec):
+    """A circular dam (r = 0.2) in the walled unit square, 101x101 lattice,
+    100 SSP-RK3 steps (the wave stays clear of the walls): the total mass
+    sum m_i h_i, read on the device, stays within MASS_DRIFT_TOL."""
+    case = _circular_dam(prec)
+    upd = from_case(case)
+    upd.upload(case.u0)
+    m0 = upd.total_mass()[0]
+    upd.set_time(0.0, 1e30)
+    _, _, n = upd.rk3_steps(100)
+    u = upd.download()
+    m1 = upd.total_mass()[0]
+    upd.close()
+    assert n == 100
+    r2 = (case.mesh["rr"][0] - 0.5) ** 2 + (case.mesh["rr"][1] - 0.5) ** 2
+    assert np.abs(u[0][r2 > 0.45 ** 2] - 0.1).max() < 1e-12      # walls still at rest
+    drift = abs(m1 - m0) / m0
+    print(f"closed basin, relative mass drift over 100 steps, precision {prec}: {drift:.3e}")
+    assert drift <= MASS_DRIFT_TOL[prec], drift
+
+
+def test_mass_change_at_walls_follows_the_reference_scheme():
+    """C1 (101x101 dam break, reflective walls) for 200 steps.  The
+    reference's d_ij = |c_ij| lambda_max is not symmetric on boundary edges
+    (c_ij + c_ji is the boundary integral there), so where the depth varies
+    along a wall the scheme itself moves mass (here ~3e-7 relative).  The
+    FP64 path follows the oracle bit for bit (its mass change is the
+    reference scheme's); the mixed path's mass stays within 5e-8 of it."""
+    case = C.dam_break_case(n=101)
+    mass = {}
+    for prec in (0, 1):
+        upd = from_case(case, precision=prec)
+        upd.upload(case.u0)
+        m0 = upd.total_mass()[0]
+        upd.set_time(0.0, 1e30)
+        upd.rk3_steps(200)
+        mass[prec] = upd.total_mass()[0]
+        upd.close()
+    print(f"C1 mass change over 200 steps: FP64 {(mass[0] - m0) / m0:.3e}, mixed {(mass[1] - m0) / m0:.3e}")
+    assert abs(mass[1] - mass[0]) <= 5e-8 * m0
+
+
+def test_dam_break_full_size_against_oracle():
+    """C1 at its full size: the 101x101 lattice dam break run to t = 0.2 (the
+    dt of each step from the CFL condition, unclipped at t_final, as in the
+    reference).  FP64 equals the oracle bit for bit; mixed is within the
+    relative L1 tolerance of h, with h >= 0."""
+    case = C.dam_break_case(n=101, tfinal=0.2)
+    o = _oracle_for(case)
+    u = case.u0.copy(order="F")
+    t, n = 0.0, 0
+    while t < case.tfinal:
+        t = o.rk3_step(u, t)
+        n += 1
+    for prec in (0, 1):
+        upd = from_case(case, precision=prec)
+        upd.upload(case.u0)
+        upd.set_time(0.0, case.tfinal)
+        tg, _, ng = upd.rk3_steps(n + 10)
+        ug = upd.download()
+        lump = upd.lumped
+        upd.close()
+        assert ng == n
+        if prec == 0:
+            np.testing.assert_array_equal(ug, u)
+            assert tg[0] == t
+        else:
+            err = _rel_l1(ug[0], u[0], lump)
+            print(f"C1 mixed vs oracle after {n} steps: relative L1(h) {err:.3e}")
+            assert ug[0].min() >= 0.0
+            assert err <= MIXED_L1_TOL, err
 
 
 def test_set_bath_after_create_equals_create_with_bath(golden):
@@ -399,12 +495,12 @@ def test_lake_at_rest_is_preserved(prec):
     upd.set_time(0.0, 1e30)
     upd.rk3_steps(20)
     u = upd.download()
-    # FP32 holds h and z separately, so eta = h + z is constant only to
-    # 2^-24 relative; the resulting pressure imbalance g h d(eta) drives a
-    # momentum noise of ~1e-6 over 20 steps (q scale h sqrt(g h) ~ 2)
-    tol_h, tol_q = (1e-13, 1e-13) if prec == 0 else (2e-6, 5e-6)
+    # FP64 balances to rounding.  The mixed path carries eta = h + z rounded
+    # once per node, so every flux of a lake at rest is exactly 0: q stays 0
+    # and h moves only by the double-float RK combinations (~2^-48 relative)
+    tol_h, tol_q = (1e-13, 1e-13) if prec == 0 else (1e-13, 0.0)
     assert np.abs(u[0] - h).max() < tol_h
-    assert np.abs(u[1:]).max() < tol_q
+    assert np.abs(u[1:]).max() <= tol_q
 
 
 def test_sgn_fp64_bit_exact_and_mixed_close():
@@ -497,7 +593,9 @@ def test_chunked_transfers_round_trip(monkeypatch, chunks):
 
 
 def test_autotuned_variants_agree(monkeypatch):
-    """The autotuner only changes block sizes and entry batching."""
+    """The autotuner only changes launch shapes (block size, entry batch,
+    grid, register cap), all of which perform the same operations: the
+    autotuned run equals the default one bit for bit."""
     case = C.bump_basin_case(n=60)
     outs = []
     for env in ("0", "1"):
@@ -508,23 +606,16 @@ def test_autotuned_variants_agree(monkeypatch):
         upd.rk3_steps(20)
         outs.append(upd.download())
         assert ("autotuned" in upd.tuning) == (env == "1")
-    # variants are separate template instantiations: FMA contraction may
-    # differ, so they agree to FP32 rounding rather than bit for bit
-    lump = upd.lumped
-    assert _rel_l1(outs[1][0], outs[0][0], lump) <= 1e-6
-    scale = np.abs(outs[0]).max(axis=1, keepdims=True) + 1e-300
-    assert np.max(np.abs(outs[0] - outs[1]) / scale) <= 1e-5
+    np.testing.assert_array_equal(outs[1], outs[0])
 
 
 @pytest.mark.parametrize("tile", ["64", "256"])
 def test_tiled_kernels_match_global_gathers(golden, monkeypatch, tile):
     """The shared-memory tile variants (node records of a tile of rows and of
     its halo staged in shared memory, neighbours read by tile-local position)
-    against the kernels that gather from HBM by column index.  The autotuner
-    may pick other entry batches for the two, whose FMA contraction differs,
-    so they agree to FP32 rounding: one Euler stage on a Thacker state with
-    moving wet/dry fronts, and 20 RK3 steps (dt included) of the
-    well-conditioned bump basin (the Thacker film amplifies rounding)."""
+    against the kernels that gather from HBM by column index, bit for bit:
+    one Euler stage on a Thacker state with moving wet/dry fronts, and 20
+    RK3 steps (dt included) of the bump basin."""
     case = _thacker(golden, "0.1", periods=1.0, cfl=0.3)
     o = _oracle_for(case)
     u = case.u0.copy(order="F")
@@ -553,13 +644,10 @@ def test_tiled_kernels_match_global_gathers(golden, monkeypatch, tile):
         traj[tiled] = upd.download()
         lump = upd.lumped
         upd.close()
-    scale = np.abs(eul["0"]).max(axis=1, keepdims=True) + 1e-300
-    assert np.max(np.abs(eul["1"] - eul["0"]) / scale) <= 1e-6
-    assert dts["1"] == pytest.approx(dts["0"], rel=1e-6)
+    np.testing.assert_array_equal(eul["1"], eul["0"])
+    np.testing.assert_array_equal(dts["1"], dts["0"])
     assert traj["1"][0].min() >= 0.0
-    assert _rel_l1(traj["1"][0], traj["0"][0], lump) <= 1e-6
-    scale = np.abs(traj["0"]).max(axis=1, keepdims=True) + 1e-300
-    assert np.max(np.abs(traj["1"] - traj["0"]) / scale) <= 1e-5
+    np.testing.assert_array_equal(traj["1"], traj["0"])
 
 
 def test_fixed_tuning_reproduces_autotuned_variants(monkeypatch):
@@ -721,6 +809,8 @@ def test_checkpoint_resume_is_bit_exact(tmp_path, prec):
     upd.close()
     again = from_case(case, precision=prec)
     again.load_checkpoint(tmp_path / "ck.npz")
+    if prec == 1:          # the stored launch configuration, not a new tuning
+        assert "fixed " in again.tuning, again.tuning
     again.rk3_steps(7)
     np.testing.assert_array_equal(again.download(), want)
     assert again.get_time()[0][0] == t_want[0]
