@@ -46,8 +46,12 @@ enum {
 
 /* viscosity_type values (SOURCES/read_data.f90:57-58 marker) */
 enum { SWE_VISC_GALERKIN = 0, SWE_VISC_VISCOUS = 1, SWE_VISC_ENTROPY = 2, SWE_VISC_FCT = 3 };
-/* precision values */
-enum { SWE_PREC_FP64 = 0, SWE_PREC_MIXED = 1 };
+/* precision values.  SWE_PREC_MIXED: FP32 fluxes, viscosities, limiter and
+ * momenta with a double-float depth (no FP64 instruction per edge or row).
+ * SWE_PREC_MIXED_F64: the same FP32 fluxes, with the per-row low-order depth
+ * update, the limiter's Q^-, P^-, R^- (and its exact dry test) and the
+ * l_ij-weighted depth sum in FP64. */
+enum { SWE_PREC_FP64 = 0, SWE_PREC_MIXED = 1, SWE_PREC_MIXED_F64 = 2 };
 
 /* The subset of the reference's `inputs` record (SOURCES/read_data.f90:4-32)
  * and module constants the step reads.  Field order is part of the ABI. */
@@ -66,7 +70,7 @@ typedef struct swe_params {
   int if_alpha_limit;    /* inputs%if_alpha_limit                            */
   int if_lumped;         /* inputs%if_lumped (only lumped is supported)      */
   int if_roundoff_fix;   /* update.f90:15 module constant                    */
-  int precision;         /* SWE_PREC_FP64 or SWE_PREC_MIXED                  */
+  int precision;         /* SWE_PREC_FP64, SWE_PREC_MIXED or _MIXED_F64      */
 } swe_params;
 
 typedef struct swe_ctx swe_ctx;

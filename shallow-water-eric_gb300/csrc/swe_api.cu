@@ -156,6 +156,11 @@ static int cuda_check(swe_ctx* c, cudaError_t e, const char* where) {
     if (_rc) return _rc;                                           \
   } while (0)
 
+// mixed contexts: SWE_PREC_MIXED and its FP64 precision split share the
+// FP32 data layout and kernels
+static bool is_mixed(const swe_ctx* c) { return c->precision != SWE_PREC_FP64; }
+static bool is_split(const swe_ctx* c) { return c->precision == SWE_PREC_MIXED_F64; }
+
 static InstConst make_const(const swe_params& p) {
   InstConst k{};
   k.g = p.gravity; k.htiny = p.htiny; k.cfl = p.cfl; k.mannings = p.mannings; k.lambda_sgn = p.lambda_sgn;
@@ -173,6 +178,13 @@ static InstConst make_const(const swe_params& p) {
   k.lambda_sgnf = (float)k.lambda_sgn;
   k.rescale_floorf = (float)k.rescale_floor;
   return k;
+}
+
+// some instance runs 'viscous' with viscous_type 'type1' (the mixed path's k_low_type1)
+static bool has_type1(const swe_ctx* c) {
+  for (const auto& p : c->params)
+    if (p.viscous_type == 1 && p.viscosity_type == SWE_VISC_VISCOUS) return true;
+  return false;
 }
 
 static bool has_entropy(const swe_ctx* c) {
@@ -193,10 +205,11 @@ static int check_params(swe_ctx* c, const swe_params& p) {
     return fail(c, SWE_ERR_ARG, "Bug: entropy viscosity programmed only with type 2");
   if (p.viscous_type == 1 && p.viscosity_type == SWE_VISC_FCT)
     return fail(c, SWE_ERR_ARG, "BUG: FCT programmed with type2 only");
-  if (p.precision != SWE_PREC_FP64 && p.precision != SWE_PREC_MIXED) return fail(c, SWE_ERR_ARG, "bad precision");
-  if (p.precision == SWE_PREC_MIXED &&
-      (p.viscosity_type == SWE_VISC_ENTROPY || (p.viscous_type == 1 && p.viscosity_type != SWE_VISC_GALERKIN)))
-    return fail(c, SWE_ERR_ARG, "mixed precision builds 'galerkin', 'viscous' (type2) and 'fct'");
+  if (p.precision != SWE_PREC_FP64 && p.precision != SWE_PREC_MIXED && p.precision != SWE_PREC_MIXED_F64)
+    return fail(c, SWE_ERR_ARG, "bad precision");
+  if (p.precision != SWE_PREC_FP64 && p.viscous_type == 1 && p.viscosity_type == SWE_VISC_VISCOUS &&
+      p.syst_size != 3)
+    return fail(c, SWE_ERR_ARG, "mixed precision builds 'viscous' with 'type1' for 3-component systems");
   if (!(p.htiny >= 0.0) || !(p.gravity > 0.0)) return fail(c, SWE_ERR_ARG, "gravity must be > 0, htiny >= 0");
   return SWE_OK;
 }
@@ -245,7 +258,7 @@ static int build_device(swe_ctx* c, const std::vector<std::vector<double>>& bath
   std::vector<double> inv(L.n_rows);
   for (int64_t r = 0; r < L.n_rows; r++) inv[r] = 1.0 / L.lumped[r];
   G.inv_lumped = upload_vec(c, inv, st);
-  if (c->precision == SWE_PREC_MIXED) {
+  if (is_mixed(c)) {
     std::vector<float> lf(L.n_rows), ilf(L.n_rows);
     for (int64_t r = 0; r < L.n_rows; r++) { lf[r] = (float)L.lumped[r]; ilf[r] = (float)inv[r]; }
     G.lumpedf = upload_vec(c, lf, st);
@@ -272,11 +285,9 @@ static int build_device(swe_ctx* c, const std::vector<std::vector<double>>& bath
     G.cxii = upload_vec(c, L.cxii, st);
     G.cyii = upload_vec(c, L.cyii, st);
   } else {
-    std::vector<float> f(L.n_entries);
-    for (int64_t e = 0; e < L.n_entries; e++) f[e] = (float)L.cx[e];
-    G.cxf = upload_vec(c, f, st);
-    for (int64_t e = 0; e < L.n_entries; e++) f[e] = (float)L.cy[e];
-    G.cyf = upload_vec(c, f, st);
+    std::vector<float2> f(L.n_entries);
+    for (int64_t e = 0; e < L.n_entries; e++) f[e] = make_float2((float)L.cx[e], (float)L.cy[e]);
+    G.cf = upload_vec(c, f, st);
     std::vector<float> fr(L.n_rows);
     for (int64_t r = 0; r < L.n_rows; r++) fr[r] = (float)L.cxii[r];
     G.cxiif = upload_vec(c, fr, st);
@@ -339,6 +350,10 @@ static int build_device(swe_ctx* c, const std::vector<std::vector<double>>& bath
     w.dmu = c->buf.alloc<float2>(ne, st);
     w.dlam = c->buf.alloc<float>(ne, st);
     w.hL = c->buf.alloc<float2>(n, st);
+    if (is_split(c)) {     // FP64 low-order depth in hL's 8 bytes per row, FP64 R^-
+      w.hL64 = reinterpret_cast<double*>(w.hL);
+      w.rminus64 = c->buf.alloc<double>(n, st);
+    }
     w.qL = c->buf.alloc<float2>(n, st);
     if (c->S == 5) { w.q3L = c->buf.alloc<float>(n, st); w.q4L = c->buf.alloc<float>(n, st); }
     // row tiles of the shared-memory kernel variants (SWE_TILE rows, default
@@ -346,7 +361,9 @@ static int build_device(swe_ctx* c, const std::vector<std::vector<double>>& bath
     const char* ft = getenv("SWE_TILE");
     const int tile = ft ? atoi(ft) : 256;
     RowTiles F;
-    if (c->S == 3 && tile > 0 && build_row_tiles(L, tile, F) && (size_t)(F.tile + F.halo_cap) * 24 <= 48 * 1024) {
+    TileCtl probe{};
+    if (c->S == 3 && tile > 0 && build_row_tiles(L, tile, F) &&
+        (probe.tile_rows = F.tile, probe.halo_cap = F.halo_cap, tile_smem_bytes(probe, true) <= 48 * 1024)) {
       c->tiles.loc = upload_vec(c, F.loc, st);
       c->tiles.halo_ptr = upload_vec(c, F.halo_ptr, st);
       c->tiles.halo_rows = upload_vec(c, F.halo_rows, st);
@@ -404,7 +421,7 @@ __global__ void k_gather_out_mix(double* __restrict__ stage, const int* __restri
     if (S == 5) { stage[n * S + 3] = a.q3[r]; stage[n * S + 4] = a.q4[r]; }
   } else {
     const float2 v = w.qL[r];
-    stage[n * S] = df_to_double(w.hL[r]);
+    stage[n * S] = w.hL64 ? w.hL64[r] : df_to_double(w.hL[r]);
     stage[n * S + 1] = v.x;
     stage[n * S + 2] = v.y;
     if (S == 5) { stage[n * S + 3] = w.q3L[r]; stage[n * S + 4] = w.q4L[r]; }
@@ -626,6 +643,8 @@ static void enqueue_step(swe_ctx* c, const KernelEvents* kev = nullptr, double* 
     } else {
       StageArgsMix a{c->G, c->d_C, c->d_St, c->mA, c->mA, c->mB, c->wm, stage, c->d_err, c->block};
       a.tiles = c->tiles_ok ? &c->tiles : nullptr;
+      a.f64 = is_split(c);
+      a.type1 = has_type1(c);
       if (stage == 2) { a.u = c->mB; a.out = c->mC; }
       if (stage == 3) { a.u = c->mC; a.out = c->mA; }
       launch_stage_mix(a, s, kev, c->tune);
@@ -917,6 +936,8 @@ SWE_API int swe_euler(swe_ctx* c, int inst, const double* un, double* unext) {
   } else {
     StageArgsMix a{c->G, c->d_C, c->d_St, c->mA, c->mA, c->mB, c->wm, 0, c->d_err, c->block};
     a.tiles = c->tiles_ok ? &c->tiles : nullptr;
+    a.f64 = is_split(c);
+    a.type1 = has_type1(c);
     launch_stage_mix(a, c->stream, nullptr, c->tune);
   }
   CK(cudaGetLastError());
@@ -952,7 +973,8 @@ SWE_API int swe_euler_intermediates(swe_ctx* c, int inst, double* dij_low, doubl
     if (muij_low && (rc = entries_to_csr(c, inst, c->wm.dmu, muij_low, (const float*)nullptr, 1))) return rc;
     if (alpha && (rc = rows_to_nodes(c, inst, c->wm.alpha, alpha))) return rc;
     if (res && (rc = rows_to_nodes(c, inst, c->wm.res, res))) return rc;
-    if (rminus && (rc = rows_to_nodes(c, inst, c->wm.rminus, rminus))) return rc;
+    if (rminus && is_split(c) && (rc = rows_to_nodes(c, inst, c->wm.rminus64, rminus))) return rc;
+    if (rminus && !is_split(c) && (rc = rows_to_nodes(c, inst, c->wm.rminus, rminus))) return rc;
     if (u_low && (rc = from_device_state(c, u_low, false, c->node_off[inst], c->node_off[inst + 1], nullptr, nullptr,
                                          true)))
       return rc;
@@ -1199,7 +1221,7 @@ static int apply_tuning(swe_ctx* c, const char* spec, const char* what) {
 }
 
 static int autotune(swe_ctx* c) {
-  if (c->precision != SWE_PREC_MIXED) { c->tuned = true; return SWE_OK; }
+  if (!is_mixed(c)) { c->tuned = true; return SWE_OK; }
   if (const char* spec = getenv("SWE_TUNE")) return apply_tuning(c, spec, "SWE_TUNE");
   int rc;
   std::vector<InstState> saved;
@@ -1210,6 +1232,8 @@ static int autotune(swe_ctx* c) {
   const cudaStream_t s = c->stream;
   StageArgsMix a{c->G, c->d_C, c->d_St, c->mA, c->mA, c->mB, c->wm, 1, c->d_err, c->block};
   a.tiles = c->tiles_ok ? &c->tiles : nullptr;
+  a.f64 = is_split(c);
+  a.type1 = has_type1(c);
   KernelTune t = c->tune;
   launch_dt_mix(c->G, c->d_C, c->d_St, c->mA, c->wm.dlam, c->wm.alpha, c->d_err, t, a.tiles, s);   // populate every work array once
   launch_stage_mix(a, s, nullptr, t);
@@ -1290,7 +1314,7 @@ SWE_API int swe_autotune(swe_ctx* c) {
 
 SWE_API int swe_set_tuning(swe_ctx* c, const char* spec) {
   if (!c || !spec) return SWE_ERR_ARG;
-  if (c->precision != SWE_PREC_MIXED) { c->tuned = true; return SWE_OK; }
+  if (!is_mixed(c)) { c->tuned = true; return SWE_OK; }
   return apply_tuning(c, spec, "tuning");
 }
 
@@ -1515,7 +1539,7 @@ SWE_API int swe_rk3_steps(swe_ctx* c, int nsteps, double* time_out, double* dt_o
   CK(cudaEventRecord(c->t0, c->stream));
   // the mixed stage 1 takes alpha from k_dt_mix: one k_node launch fewer
   const long long per_step = 3LL * kLaunchesPerStage + kLaunchesPerStepExtra -
-                             (c->precision == SWE_PREC_MIXED ? 1 : 0) + (c->n_gauges ? 1 : 0);
+                             (is_mixed(c) ? 1 : 0) + (c->n_gauges ? 1 : 0);
   if (nsteps >= chunk && chunk > 1) {
     for (int k = 0; k + chunk <= nsteps; k += chunk) {
       CK(cudaGraphLaunch(c->gexec, c->stream));

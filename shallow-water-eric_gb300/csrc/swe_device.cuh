@@ -54,8 +54,7 @@ struct Graph {
   const double* __restrict__ cy;
   const double* __restrict__ cxii;
   const double* __restrict__ cyii;
-  const float* __restrict__ cxf;
-  const float* __restrict__ cyf;
+  const float2* __restrict__ cf;          // mixed path, per entry: c_ij in FP32, (x, y) interleaved
   const float* __restrict__ cxiif;
   const float* __restrict__ cyiif;
   const double* __restrict__ cnorm;       // FP64 path, per entry: |c_ij| and c_ij/|c_ij|

@@ -40,6 +40,8 @@ struct WorkMix {
   float2* dmu;                           // per entry: (d_ij, mu_ij), one 8-byte load
   float* dlam;                           // per entry: |c_ij| lambda_max from k_dt_mix (stage 1)
   float2* hL;                            // low-order depth (double-float)
+  double* hL64;                          // precision split: the FP64 low-order depth (hL's storage), or null
+  double* rminus64;                      // precision split: FP64 R^-_i, or null
   float2* qL;                            // low-order momenta
   float *q3L, *q4L;                      // low-order h*eta, h*w (type 13)
 };
@@ -82,6 +84,8 @@ struct StageArgsMix {
   unsigned* err;
   int block;
   const TileCtl* tiles = nullptr;  // row tiles of the shared-memory variants, or null
+  bool f64 = false;                 // precision split: h^L, R^- and the depth's limited sum in FP64
+  bool type1 = false;               // some instance runs 'viscous' with viscous_type 'type1'
 };
 
 // Optional per-kernel event timing: when non-null, ev[2k], ev[2k+1] bracket
@@ -121,6 +125,8 @@ struct KernelTune {
 };
 
 void launch_stage_mix(const StageArgsMix& a, cudaStream_t s, const KernelEvents* kev, const KernelTune& t);
+// dynamic shared memory of one tile block (d: with the FP64 R^- of the precision split)
+size_t tile_smem_bytes(const TileCtl& tc, bool d = false);
 void launch_kernel_mix(int kind, const StageArgsMix& a, const KernelTune& t, cudaStream_t s);
 bool kind_has_tiles(int kind);   // kernel kinds with a shared-memory tile variant
 void launch_dt_mix(const Graph& G, const InstConst* C, InstState* St, const StateMix& u, float* dlam, float* alpha,

@@ -188,24 +188,34 @@ __device__ __forceinline__ bool dlam_f(float cxe, float cye, float cvi, float cv
   return ok;
 }
 
-// Entry loops are processed in batches of B entries: every load of a batch is
-// issued before any of them is used, so a thread keeps B gathers in flight
-// (the kernels are latency-bound otherwise).  Sums keep the entry order, so
-// every batch size gives the same bits.  The autotuner picks B per kernel.
+// Entry loops are processed in batches of B entries: every global load of a
+// batch is issued before any of them is used, so a thread keeps B loads in
+// flight (the kernels are latency-bound otherwise); the tile variants read
+// neighbours from shared memory at the point of use (no registers held for
+// them).  Sums keep the entry order, so every batch size gives the same
+// bits.  The autotuner picks B per kernel.
 
 // Neighbour access of the entry loops: straight from HBM by column index
 // (NbGlobal), or from the block's shared-memory copy of its tile and halo
 // nodes by tile-local position (NbTile, rows of 3-component systems only).
 // aux is the per-node scalar the loop needs besides the node record (alpha
 // in k_low, the residual in k_fct and k_update); R is R^- (k_update).
+// Entry k of a row is read at row_index(base)[32 k]: a per-row pointer and a
+// 32-bit offset.  self(r) is the row's own position in nq / aux / R (the
+// tile variants read their own rows from shared memory too), len(r) and
+// base(r) its entry count and first entry (the tile variants read them from
+// shared memory, staged with the tile).
 struct NbGlobal {
   static constexpr bool kGlobal = true;
   const int* col;
   const float4* nq;
   const float* aux;
   const float* R;
-  __device__ __forceinline__ int index(int64_t e) const { return col[e]; }
+  const double* R64;          // FP64 R^- (precision split), or null
+  __device__ __forceinline__ const int* row_index(int64_t base) const { return col + base; }
   __device__ __forceinline__ int self(int64_t r) const { return (int)r; }
+  __device__ __forceinline__ int len(const Graph& G, int64_t r) const { return G.len[r]; }
+  __device__ __forceinline__ int64_t base(const Graph& G, int64_t r) const { return entry_base(G, r); }
 };
 struct NbTile {
   static constexpr bool kGlobal = false;
@@ -213,30 +223,44 @@ struct NbTile {
   const float4* nq;
   const float* aux;
   const float* R;
+  const double* R64;
   int64_t t0;
-  __device__ __forceinline__ int index(int64_t e) const { return loc[e]; }
+  const int64_t* sp;          // slice pointers of the tile's slices
+  const uint8_t* ln;          // entry counts of the tile's rows
+  __device__ __forceinline__ const int16_t* row_index(int64_t base) const { return loc + base; }
   __device__ __forceinline__ int self(int64_t r) const { return (int)(r - t0); }
+  __device__ __forceinline__ int len(const Graph&, int64_t r) const { return ln[r - t0]; }
+  __device__ __forceinline__ int64_t base(const Graph&, int64_t r) const { return sp[(r - t0) >> 5] + (r & 31); }
 };
 
-// Shared-memory tile of one block: node records, aux and R^- of the tile's
-// rows (positions 0 .. T-1) and of its halo rows (T .. T+nh-1).
+// Shared-memory tile of one block: node records, aux and R^- (and the FP64
+// R^- of the precision split) of the tile's rows (positions 0 .. T-1) and of
+// its halo rows (T .. T+nh-1), then the slice pointers and entry counts of
+// the tile's rows.  Layout: nq | R64 (split only) | aux | R | sp | ln.
 struct TileSmem {
   float4* nq;
+  double* R64;
   float* aux;
   float* R;
+  int64_t* sp;
+  uint8_t* ln;
 };
-__device__ __forceinline__ TileSmem tile_smem(void* base, int cap) {
+template <bool D>
+__device__ __forceinline__ TileSmem tile_smem(void* base, int cap, int T) {
   float4* nq = reinterpret_cast<float4*>(base);
-  float* aux = reinterpret_cast<float*>(nq + cap);
-  return TileSmem{nq, aux, aux + cap};
+  double* r64 = reinterpret_cast<double*>(nq + cap);
+  float* aux = reinterpret_cast<float*>(D ? (void*)(r64 + cap) : (void*)(nq + cap));
+  float* R = aux + cap;
+  int64_t* sp = reinterpret_cast<int64_t*>(R + cap);   // 24 or 32 bytes per position before it: 8-byte aligned
+  return TileSmem{nq, D ? r64 : nullptr, aux, R, sp, reinterpret_cast<uint8_t*>(sp + T / 32)};
 }
 
 // Copy the tile's and the halo's node data into shared memory (coalesced for
 // the tile rows, ascending gathers for the halo); returns the tile start.
-template <bool AUX, bool RM>
+template <bool AUX, bool RM, bool D = false>
 __device__ __forceinline__ int64_t stage_tile(const Graph& G, const TileCtl& tc, const StateMix& u,
                                               const float* __restrict__ aux, const float* __restrict__ rminus,
-                                              const TileSmem& sm) {
+                                              const TileSmem& sm, const double* __restrict__ rminus64 = nullptr) {
   const int T = tc.tile_rows;
   const int64_t t0 = (int64_t)blockIdx.x * T;
   const int h0 = tc.halo_ptr[blockIdx.x], nh = tc.halo_ptr[blockIdx.x + 1] - h0;
@@ -246,7 +270,11 @@ __device__ __forceinline__ int64_t stage_tile(const Graph& G, const TileCtl& tc,
       sm.nq[i] = u.nq[row];
       if (AUX) sm.aux[i] = aux[row];
       if (RM) sm.R[i] = rminus[row];
+      if (RM && D) sm.R64[i] = rminus64[row];
+      if (i < T) sm.ln[i] = G.len[row];
     }
+    // slices of the tile that exist (the last tile may be partial)
+    if (i < T / 32 && t0 + 32 * (int64_t)i < G.n_rows) sm.sp[i] = G.slice_ptr[(t0 >> 5) + i];
   }
   __syncthreads();
   return t0;
@@ -269,21 +297,22 @@ template <int B, class Nb>
 __device__ __forceinline__ void node_row(int64_t r, Graph G, const InstConst* __restrict__ C,
                                                   const InstState* __restrict__ St, StateMix u,
                                                   float* __restrict__ alpha_out, const Nb& nb) {
-  const int L = G.len[r];
+  const int L = nb.len(G, r);
   if (L == 0) return;
   const int b = G.slice_inst[r >> 5];
   if (St[b].done) return;
   const InstConst& c = C[b];
   const float* hs = reinterpret_cast<const float*>(nb.nq);
-  const float h = reinterpret_cast<const float*>(u.nq)[4 * r];
+  const int me = nb.self(r);
+  const float h = hs[4 * me];
   float alpha = 1.0f;
   if (c.alpha_limit && !(h <= c.htinyf)) {
-    const int64_t base = entry_base(G, r);
+    const auto ip = nb.row_index(nb.base(G, r));
     float num = 0.0f, denom = 0.0f;
     for (int k0 = 0; k0 < L; k0 += B) {
       int j[B];
 #pragma unroll
-      for (int q = 0; q < B; q++) j[q] = (k0 + q < L) ? nb.index(base + 32 * (k0 + q)) : nb.self(r);
+      for (int q = 0; q < B; q++) j[q] = (k0 + q < L) ? (int)ip[32 * (k0 + q)] : me;
       float hj[B];
 #pragma unroll
       for (int q = 0; q < B; q++) hj[q] = hs[4 * (int64_t)j[q]];
@@ -303,7 +332,7 @@ template <int B>
 __global__ void __launch_bounds__(256) k_node_mix(Graph G, const InstConst* __restrict__ C,
                                                   const InstState* __restrict__ St, StateMix u,
                                                   float* __restrict__ alpha_out) {
-  const NbGlobal nb{G.col, u.nq, nullptr, nullptr};
+  const NbGlobal nb{G.col, u.nq, nullptr, nullptr, nullptr};
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < G.n_rows; r += (int64_t)gridDim.x * blockDim.x)
     node_row<B>(r, G, C, St, u, alpha_out, nb);
 }
@@ -313,10 +342,10 @@ __global__ void __launch_bounds__(256) k_node_tile(Graph G, const InstConst* __r
                                                    const InstState* __restrict__ St, StateMix u,
                                                    float* __restrict__ alpha_out, TileCtl tc) {
   extern __shared__ float4 tile_mem[];
-  const TileSmem sm = tile_smem(tile_mem, tc.tile_rows + tc.halo_cap);
+  const TileSmem sm = tile_smem<false>(tile_mem, tc.tile_rows + tc.halo_cap, tc.tile_rows);
   const int64_t t0 = stage_tile<false, false>(G, tc, u, nullptr, nullptr, sm);
   const int64_t t1 = tile_end(G, tc, t0);
-  const NbTile nb{tc.loc, sm.nq, nullptr, nullptr, t0};
+  const NbTile nb{tc.loc, sm.nq, nullptr, nullptr, nullptr, t0, sm.sp, sm.ln};
   for (int64_t r = t0 + threadIdx.x; r < t1; r += blockDim.x) node_row<B>(r, G, C, St, u, alpha_out, nb);
 }
 
@@ -359,13 +388,13 @@ __device__ __forceinline__ float sgn_pressure(float lambda_sgn, float g, float m
 // (N <= h_i sum d, so a N <= CFL h_i): the reference's fix h + rk_1 with
 // rat_ij h_i = H*_ij.  At rest the two sums add equal terms in the same
 // order, so P - N is exactly 0.
-template <int B, bool LAMIN, int MINB, class Nb>
+template <int B, bool LAMIN, int MINB, bool D, class Nb>
 __device__ __forceinline__ void low_row(int64_t r, Graph G, const InstConst* __restrict__ C,
                                                        const InstState* __restrict__ St, StateMix u,
                                                        const float* __restrict__ alpha, float2* __restrict__ dmu,
                                                        WorkMix w, float* __restrict__ res, unsigned* __restrict__ err,
                                                        const Nb& nb) {
-  const int L = G.len[r];
+  const int L = nb.len(G, r);
   if (L == 0) return;
   const int b = G.slice_inst[r >> 5];
   const InstState& st = St[b];
@@ -381,11 +410,16 @@ __device__ __forceinline__ void low_row(int64_t r, Graph G, const InstConst* __r
   // tests (rat = 0 already where h <= 0) when the step is not roundoff-fixed
   const bool roundoff = c.roundoff_fix && !galerkin;
   const float hthr = roundoff ? htiny : 0.f;
-  const int64_t base = entry_base(G, r);
-  const NodeF ni = node_from(u.nq[r], htiny);
+  const int64_t base = nb.base(G, r);
+  const int me = nb.self(r);
+  const auto ip = nb.row_index(base);
+  const float2* cp = G.cf + base;
+  const float* dlp = w.dlam + base;
+  float2* dmp = dmu + base;
+  const NodeF ni = node_from(nb.nq[me], htiny);
   const float sqi = sqrtf(g * fabsf(ni.h));
   const float v2i_flux = sgn ? 0.f : ni.v2;          // flux() zeroes velocity(2) for type 13
-  const float ai = alpha[r];
+  const float ai = nb.aux[me];
   const float m = G.lumpedf[r];
   const float ghi = g * ni.h;
   const bool wet_i = !(ni.h <= hthr);
@@ -419,24 +453,28 @@ __device__ __forceinline__ void low_row(int64_t r, Graph G, const InstConst* __r
 #pragma unroll
    for (int q = 0; q < B; q++) {
      if (k0 + q < L) {
-       const int64_t e = base + 32 * (k0 + q);
-       jb[q] = nb.index(e); cxb[q] = G.cxf[e]; cyb[q] = G.cyf[e];
-       dlb[q] = LAMIN ? w.dlam[e] : 0.f;
+       const int off = 32 * (k0 + q);
+       const float2 cc = cp[off];
+       jb[q] = ip[off]; cxb[q] = cc.x; cyb[q] = cc.y;
+       dlb[q] = LAMIN ? dlp[off] : 0.f;
      } else {
-       jb[q] = nb.self(r); cxb[q] = 0.f; cyb[q] = 0.f; dlb[q] = 0.f;
+       jb[q] = me; cxb[q] = 0.f; cyb[q] = 0.f; dlb[q] = 0.f;
      }
    }
-   float4 nqb[B];
-   float alb[B];
+   float4 nqb[Nb::kGlobal ? B : 1];
+   float alb[Nb::kGlobal ? B : 1];
+   if constexpr (Nb::kGlobal) {
 #pragma unroll
-   for (int q = 0; q < B; q++) { nqb[q] = nb.nq[jb[q]]; alb[q] = nb.aux[jb[q]]; }
+     for (int q = 0; q < B; q++) { nqb[q] = nb.nq[jb[q]]; alb[q] = nb.aux[jb[q]]; }
+   }
 #pragma unroll
    for (int q = 0; q < B; q++) {
     if (k0 + q >= L) break;
-    const int64_t e = base + 32 * (k0 + q);
+    const int off = 32 * (k0 + q);
     const float cxe = cxb[q], cye = cyb[q];
     const int j = jb[q];
-    const NodeF nj = node_from(nqb[q], htiny);
+    const NodeF nj = node_from(Nb::kGlobal ? nqb[q] : nb.nq[j], htiny);
+    const float alj = Nb::kGlobal ? alb[q] : nb.aux[j];
     // --- viscosities: compute_dij, compute_muij, MAX, alpha_limit
     const float cvi = dotc(cxe, cye, ni.v1, ni.v2);                   // c.v_i (compute_muij)
     const float cvj = dotc(cxe, cye, nj.v1, nj.v2);                   // c.v_j
@@ -448,10 +486,10 @@ __device__ __forceinline__ void low_row(int64_t r, Graph G, const InstConst* __r
     }
     float mu = fmaxf(fmaxf(-cvi, 0.f), fmaxf(cvj, 0.f));
     float d = fmaxf(dlam, mu);
-    const float s = (c.alpha_limit ? fmaxf(ai, alb[q]) : 1.f) * vis;
+    const float s = (c.alpha_limit ? fmaxf(ai, alj) : 1.f) * vis;
     d *= s;
     mu *= s;
-    dmu[e] = make_float2(d, mu);
+    dmp[off] = make_float2(d, mu);
     // --- entropy stencil
     const float v2j_flux = sgn ? 0.f : nj.v2;
     const float Ej = entropy_f(g, nj.h, nj.v1, nj.q1, v2j_flux, nj.q2);
@@ -531,18 +569,34 @@ __device__ __forceinline__ void low_row(int64_t r, Graph G, const InstConst* __r
     rk3 = fma_(m, ui4, rk3); rk4 = fma_(-m, s_i, rk4);
     g3 = fma_(m, ui4, g3); g4 = fma_(-m, s_i, g4);
   }
-  // low-order state: double-float depth plus an FP32 increment
+  // low-order state: double-float depth plus an FP32 increment, or (precision
+  // split) the FP64 update h + (dt/m) (P - N - c_ii.v_i h) of the FP32 sums
   const float invm = G.inv_lumpedf[r];
   const float a = dtf * invm;
   const float2 h = u.h[r];
-  float2 hL;
-  if (roundoff) {
-    hL = df_add_f(h, a * fma_(-cvd, ni.h, P - N));   // h + a (fix h + rk_1), a N <= CFL h
-  } else {                                            // smb_2 and MAX(h + dt rk, 0)
-    hL = df_add_f(h, a * g0);
-    if (hL.x < 0.f) hL = make_float2(0.f, 0.f);
+  // ('entropy_visc' without the roundoff fix keeps h + dt rk unclipped: its
+  // k_update adds the high-order correction before MAX(., 0))
+  const bool clip = !(c.visc == VISC_ENTROPY);
+  if (D) {
+    const double hd = df_to_double(h), ad = st.dt * G.inv_lumped[r];
+    double hL;
+    if (roundoff) {
+      hL = fma(ad, fma(-(double)cvd, (double)ni.h, (double)P - (double)N), hd);
+    } else {
+      hL = fma(ad, (double)g0, hd);
+      if (clip && hL < 0.0) hL = 0.0;
+    }
+    w.hL64[r] = hL;
+  } else {
+    float2 hL;
+    if (roundoff) {
+      hL = df_add_f(h, a * fma_(-cvd, ni.h, P - N));   // h + a (fix h + rk_1), a N <= CFL h
+    } else {                                            // smb_2 and MAX(h + dt rk, 0)
+      hL = df_add_f(h, a * g0);
+      if (clip && hL.x < 0.f) hL = make_float2(0.f, 0.f);
+    }
+    w.hL[r] = hL;
   }
-  w.hL[r] = hL;
   w.qL[r] = make_float2(fma_(dtf, rk1 * invm, ni.q1), fma_(dtf, rk2_ * invm, ni.q2));
   if (S == 5) { w.q3L[r] = fma_(dtf, rk3 * invm, ui3); w.q4L[r] = fma_(dtf, rk4 * invm, ui4); }
   // entropy residual (update.f90:838-868), rescale once per node
@@ -559,29 +613,124 @@ __device__ __forceinline__ void low_row(int64_t r, Graph G, const InstConst* __r
   if (delta_bad) atomicOr(err, ERRB_DELTA);
 }
 
-template <int B, bool LAMIN, int MINB>
+template <int B, bool LAMIN, int MINB, bool D>
 __global__ void __launch_bounds__(256, MINB) k_low_mix(Graph G, const InstConst* __restrict__ C,
                                                        const InstState* __restrict__ St, StateMix u,
                                                        const float* __restrict__ alpha, float2* __restrict__ dmu,
                                                        WorkMix w, float* __restrict__ res, unsigned* __restrict__ err) {
-  const NbGlobal nb{G.col, u.nq, alpha, nullptr};
+  const NbGlobal nb{G.col, u.nq, alpha, nullptr, nullptr};
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < G.n_rows; r += (int64_t)gridDim.x * blockDim.x)
-    low_row<B, LAMIN, MINB>(r, G, C, St, u, alpha, dmu, w, res, err, nb);
+    low_row<B, LAMIN, MINB, D>(r, G, C, St, u, alpha, dmu, w, res, err, nb);
 }
 
-template <int B, bool LAMIN, int MINB>
+template <int B, bool LAMIN, int MINB, bool D>
 __global__ void __launch_bounds__(256, MINB) k_low_tile(Graph G, const InstConst* __restrict__ C,
                                                         const InstState* __restrict__ St, StateMix u,
                                                         const float* __restrict__ alpha, float2* __restrict__ dmu,
                                                         WorkMix w, float* __restrict__ res, unsigned* __restrict__ err,
                                                         TileCtl tc) {
   extern __shared__ float4 tile_mem[];
-  const TileSmem sm = tile_smem(tile_mem, tc.tile_rows + tc.halo_cap);
+  const TileSmem sm = tile_smem<false>(tile_mem, tc.tile_rows + tc.halo_cap, tc.tile_rows);
   const int64_t t0 = stage_tile<true, false>(G, tc, u, alpha, nullptr, sm);
   const int64_t t1 = tile_end(G, tc, t0);
-  const NbTile nb{tc.loc, sm.nq, sm.aux, nullptr, t0};
+  const NbTile nb{tc.loc, sm.nq, sm.aux, nullptr, nullptr, t0, sm.sp, sm.ln};
   for (int64_t r = t0 + threadIdx.x; r < t1; r += blockDim.x)
-    low_row<B, LAMIN, MINB>(r, G, C, St, u, alpha, dmu, w, res, err, nb);
+    low_row<B, LAMIN, MINB, D>(r, G, C, St, u, alpha, dmu, w, res, err, nb);
+}
+
+// 'viscous' with viscous_type 'type1' (update.f90:189-201, smb_1 :366-423):
+// d_ij as in low_row (lambda_max, MAX with mu_ij, alpha scaling), then the
+// RHS of smb_1 -- the centred flux -c.(v_j u_j rat_ji + v_i u_i rat_ij),
+// d_ij (u_j rat_ji - u_i rat_ij) and the pressure term
+// -g/2 (H*_ji^2 - H*_ij^2) c_ij, with the h <= htiny tests -- and the
+// low-order state u + dt rk / m (no clipping, as the reference).  Rows of
+// other instances of a batch run low_row.  3-component systems only.
+template <bool D>
+__device__ __forceinline__ void low_row_type1(int64_t r, const Graph& G, const InstConst& c, const InstState& st,
+                                              const StateMix& u, const float* __restrict__ alpha,
+                                              float2* __restrict__ dmu, const WorkMix& w, unsigned* __restrict__ err) {
+  const NbGlobal nb{G.col, u.nq, alpha, nullptr, nullptr};
+  const int L = nb.len(G, r);
+  const float g = c.gf, htiny = c.htinyf, dtf = st.dtf;
+  const LamK lk = lam_k(g, htiny);
+  const int64_t base = nb.base(G, r);
+  const int me = nb.self(r);
+  const int* ip = nb.row_index(base);
+  const float2* cp = G.cf + base;
+  float2* dmp = dmu + base;
+  const NodeF ni = node_from(nb.nq[me], htiny);
+  const float sqi = sqrtf(g * fabsf(ni.h));
+  const float ai = nb.aux[me];
+  const float invhi = inv_pos(ni.h);
+  const bool wet_i = !(ni.h <= htiny);
+  // diagonal: the centred flux -c_ii.v_i u_i (rat_ii = 1 for h_i > htiny)
+  const float cxd = G.cxiif[r], cyd = G.cyiif[r];
+  const float cvd = dotc(cxd, cyd, ni.v1, ni.v2);
+  const float rdd = wet_i ? 1.f : 0.f;
+  float rk0 = -2.f * cvd * ni.h * rdd, rk1 = -2.f * cvd * ni.q1 * rdd, rk2 = -2.f * cvd * ni.q2 * rdd;
+  bool delta_bad = false;
+  for (int k = 0; k < L; k++) {
+    const int off = 32 * k;
+    const float2 cc = cp[off];
+    const int j = ip[off];
+    const NodeF nj = node_from(nb.nq[j], htiny);
+    const float cxe = cc.x, cye = cc.y;
+    const float cvi = dotc(cxe, cye, ni.v1, ni.v2), cvj = dotc(cxe, cye, nj.v1, nj.v2);
+    float dlam;
+    if (!dlam_f(cxe, cye, cvi, cvj, ni.h, nj.h, ni.ovh, nj.ovh, sqi, sqrtf(g * fabsf(nj.h)), lk, &dlam))
+      delta_bad = true;
+    float mu = fmaxf(fmaxf(-cvi, 0.f), fmaxf(cvj, 0.f));
+    float d = fmaxf(dlam, mu);
+    const float s = c.alpha_limit ? fmaxf(ai, nb.aux[j]) : 1.f;
+    d *= s;
+    mu *= s;
+    dmp[off] = make_float2(d, mu);
+    const float deta = __fsub_rn(nj.eta, ni.eta);
+    const float dz = dz_of(deta, ni.h, nj.h);
+    const Recon R = recon(ni.h, nj.h, dz);
+    const float rij = wet_i ? rat_of(R.Hij, ni.h, dz <= 0.f, invhi) : 0.f;
+    const float rji = !(nj.h <= htiny) ? rat_of(R.Hji, nj.h, dz >= 0.f, inv_pos(nj.h)) : 0.f;
+    const float ai_ = cvi * rij, aj = cvj * rji;          // c.v_i rat_ij, c.v_j rat_ji
+    rk0 += fma_(d, fma_(nj.h, rji, -ni.h * rij), -fma_(aj, nj.h, ai_ * ni.h));
+    rk1 += fma_(d, fma_(nj.q1, rji, -ni.q1 * rij), -fma_(aj, nj.q1, ai_ * ni.q1));
+    rk2 += fma_(d, fma_(nj.q2, rji, -ni.q2 * rij), -fma_(aj, nj.q2, ai_ * ni.q2));
+    const float pr = 0.5f * g * fma_(R.Hji, R.Hji, -R.Hij * R.Hij);
+    rk1 = fma_(-pr, cxe, rk1);
+    rk2 = fma_(-pr, cye, rk2);
+  }
+  // source terms (update.f90:425-486)
+  const float m = G.lumpedf[r];
+  if (c.type_test == 9 || c.type_test == 10) {
+    const float hstar = __powf(fmaxf(ni.h, htiny), 4.0f / 3.0f);
+    const float vel = c.fricf * sqrtf(fma_(ni.v1, ni.v1, ni.v2 * ni.v2));
+    const float coef = fdiv(m * vel * 2.f, hstar + fmaxf(hstar, vel * dtf));
+    rk1 = fma_(-coef, ni.q1, rk1); rk2 = fma_(-coef, ni.q2, rk2);
+  } else if (c.type_test == 11) {
+    rk1 = fma_(-m * 0.2f, ni.q1, rk1); rk2 = fma_(-m * 0.2f, ni.q2, rk2);
+  } else if (c.type_test == 12) {
+    rk1 += m * 2.0f * ni.q2; rk2 -= m * 2.0f * ni.q1;
+  }
+  const float invm = G.inv_lumpedf[r];
+  if (D) w.hL64[r] = fma(st.dt * G.inv_lumped[r], (double)rk0, df_to_double(u.h[r]));
+  else w.hL[r] = df_add_f(u.h[r], (dtf * invm) * rk0);
+  w.qL[r] = make_float2(fma_(dtf, rk1 * invm, ni.q1), fma_(dtf, rk2 * invm, ni.q2));
+  if (delta_bad) atomicOr(err, ERRB_DELTA);
+}
+
+template <bool D>
+__global__ void __launch_bounds__(256) k_low_type1(Graph G, const InstConst* __restrict__ C,
+                                                   const InstState* __restrict__ St, StateMix u,
+                                                   const float* __restrict__ alpha, float2* __restrict__ dmu, WorkMix w,
+                                                   float* __restrict__ res, unsigned* __restrict__ err) {
+  const NbGlobal nb{G.col, u.nq, alpha, nullptr, nullptr};
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < G.n_rows; r += (int64_t)gridDim.x * blockDim.x) {
+    if (G.len[r] == 0) continue;
+    const int b = G.slice_inst[r >> 5];
+    if (St[b].done) continue;
+    const InstConst& c = C[b];
+    if (c.viscous_type == 1 && c.visc == VISC_VISCOUS) low_row_type1<D>(r, G, c, St[b], u, alpha, dmu, w, err);
+    else low_row<1, false, 3, D>(r, G, C, St, u, alpha, dmu, w, res, err, nb);
+  }
 }
 
 // Limiter margin: (1 - 2^-18) Q^-.  Between the limiter and the depth update
@@ -600,20 +749,23 @@ __device__ __forceinline__ float fct_entry(float d0, float m0, float rij, float 
 
 // k_fct_mix: f_ij and the limiter R^-_i (fct.f90:15-30): P^- = sum f^- - 1e-15,
 // Q^- = -m h^L/dt, R^- = min(Q^-/P^-, 1), 0 where m h^L/dt <= htiny.
-template <int B, class Nb>
+template <int B, bool D, class Nb>
 __device__ __forceinline__ void fct_row(int64_t r, Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St, StateMix u,
                           const float2* __restrict__ dmu, WorkMix w, const float* __restrict__ res,
                           unsigned* __restrict__ err, const Nb& nb) {
-  const int L = G.len[r];
+  const int L = nb.len(G, r);
   if (L == 0) return;
   const int b = G.slice_inst[r >> 5];
   const InstState& st = St[b];
   if (st.done) return;
   const InstConst& c = C[b];
   if (c.visc != VISC_FCT) return;
-  const int64_t base = entry_base(G, r);
-  const float4 ni = u.nq[r];
-  const float hi = ni.x, etai = ni.w, resi = res[r];
+  const int64_t base = nb.base(G, r);
+  const int me = nb.self(r);
+  const auto ip = nb.row_index(base);
+  const float2* dmp = dmu + base;
+  const float4 ni = nb.nq[me];
+  const float hi = ni.x, etai = ni.w, resi = nb.aux[me];
   float neg = 0.f;                       // f_ii = 0 adds nothing
   for (int k0 = 0; k0 < L; k0 += B) {
     int jb[B];
@@ -621,24 +773,40 @@ __device__ __forceinline__ void fct_row(int64_t r, Graph G, const InstConst* __r
 #pragma unroll
     for (int q = 0; q < B; q++) {
       if (k0 + q < L) {
-        const int64_t e = base + 32 * (k0 + q);
-        jb[q] = nb.index(e); const float2 v = dmu[e]; d0b[q] = v.x; m0b[q] = v.y;
+        const int off = 32 * (k0 + q);
+        jb[q] = ip[off]; const float2 v = dmp[off]; d0b[q] = v.x; m0b[q] = v.y;
       } else {
-        jb[q] = nb.self(r); d0b[q] = 0.f; m0b[q] = 0.f;
+        jb[q] = me; d0b[q] = 0.f; m0b[q] = 0.f;
       }
     }
-    float4 njb[B];
-    float rsb[B];
+    float4 njb[Nb::kGlobal ? B : 1];
+    float rsb[Nb::kGlobal ? B : 1];
+    if constexpr (Nb::kGlobal) {
 #pragma unroll
-    for (int q = 0; q < B; q++) { njb[q] = nb.nq[jb[q]]; rsb[q] = nb.aux[jb[q]]; }
+      for (int q = 0; q < B; q++) { njb[q] = nb.nq[jb[q]]; rsb[q] = nb.aux[jb[q]]; }
+    }
 #pragma unroll
     for (int q = 0; q < B; q++) {
       if (k0 + q >= L) break;
-      const float4 nj = njb[q];
+      const float4 nj = Nb::kGlobal ? njb[q] : nb.nq[jb[q]];
+      const float rsj = Nb::kGlobal ? rsb[q] : nb.aux[jb[q]];
       const Recon R = recon(hi, nj.x, dz_of(__fsub_rn(nj.w, etai), hi, nj.x));
-      const float f = fct_entry(d0b[q], m0b[q], fmaxf(resi, rsb[q]), hi, nj.x, R);
+      const float f = fct_entry(d0b[q], m0b[q], fmaxf(resi, rsj), hi, nj.x, R);
       if (f < 0.f) neg = __fadd_rn(neg, f);
     }
+  }
+  if (D) {   // precision split: Q^-, P^-, R^- and the dry test in FP64, as the reference
+    const double hL = w.hL64[r];
+    if (hL < 0.0) atomicOr(err, ERRB_NEG_H);
+    const double scaled = (G.lumped[r] / st.dt) * hL;                           // (lumped/dt) h^L
+    double R = 0.0;
+    if (!(scaled <= c.htiny)) {
+      const double Pm = -1.e-15 + (double)neg;
+      R = fmin((0.0 - scaled) / Pm, 1.0);
+    }
+    w.rminus64[r] = R;
+    w.rminus[r] = (float)R;
+    return;
   }
   const float2 hL = w.hL[r];
   if (hL.x < 0.f) atomicOr(err, ERRB_NEG_H);
@@ -655,26 +823,26 @@ __device__ __forceinline__ void fct_row(int64_t r, Graph G, const InstConst* __r
   w.rminus[r] = R;
 }
 
-template <int B>
+template <int B, bool D>
 __global__ void __launch_bounds__(256) k_fct_mix(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St,
                                                  StateMix u, const float2* __restrict__ dmu, WorkMix w,
                                                  const float* __restrict__ res, unsigned* __restrict__ err) {
-  const NbGlobal nb{G.col, u.nq, res, nullptr};
+  const NbGlobal nb{G.col, u.nq, res, nullptr, nullptr};
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < G.n_rows; r += (int64_t)gridDim.x * blockDim.x)
-    fct_row<B>(r, G, C, St, u, dmu, w, res, err, nb);
+    fct_row<B, D>(r, G, C, St, u, dmu, w, res, err, nb);
 }
 
-template <int B>
+template <int B, bool D>
 __global__ void __launch_bounds__(256) k_fct_tile(Graph G, const InstConst* __restrict__ C,
                                                   const InstState* __restrict__ St, StateMix u,
                                                   const float2* __restrict__ dmu, WorkMix w,
                                                   const float* __restrict__ res, unsigned* __restrict__ err, TileCtl tc) {
   extern __shared__ float4 tile_mem[];
-  const TileSmem sm = tile_smem(tile_mem, tc.tile_rows + tc.halo_cap);
+  const TileSmem sm = tile_smem<false>(tile_mem, tc.tile_rows + tc.halo_cap, tc.tile_rows);
   const int64_t t0 = stage_tile<true, false>(G, tc, u, res, nullptr, sm);
   const int64_t t1 = tile_end(G, tc, t0);
-  const NbTile nb{tc.loc, sm.nq, sm.aux, nullptr, t0};
-  for (int64_t r = t0 + threadIdx.x; r < t1; r += blockDim.x) fct_row<B>(r, G, C, St, u, dmu, w, res, err, nb);
+  const NbTile nb{tc.loc, sm.nq, sm.aux, nullptr, nullptr, t0, sm.sp, sm.ln};
+  for (int64_t r = t0 + threadIdx.x; r < t1; r += blockDim.x) fct_row<B, D>(r, G, C, St, u, dmu, w, res, err, nb);
 }
 
 // End of a stage for one row: non-finite check, the SSP-RK combination and
@@ -719,32 +887,48 @@ __device__ __forceinline__ void finish_mix(const Graph& G, const InstConst& c, i
 // sum is R^-_i P_i plus sum_{f_ij >= 0} R^-_j f_ij, with P_i = sum_{f_ij < 0}
 // f_ij formed in the entry order of k_fct_mix (the same value, bit for bit,
 // as the one the limiter saw).
-template <int B, class Nb>
+//
+// 'entropy_visc' (update.f90:241-269) recomputes the RHS with the
+// high-order viscosities d^H = MIN(d, res_ij), mu^H = MIN(mu, res_ij).  That
+// RHS is linear in (d, mu), so u^H = u^L + (dt/m) sum_j [dm (u_j - u_i) +
+// (dd - dm) (u_j rat_ji - u_i rat_ij)] with dd = d^H - d, dm = mu^H - mu:
+// this kernel's antidiffusion with every l_ij = 1, and the rats of the RHS
+// the stage uses (smb_2_roundoff: the htiny tests, the mass row testing
+// only h_i; smb_2: the h <= 0 tests, then MAX(h, 0)).
+template <int B, bool D, class Nb>
 __device__ __forceinline__ void update_row(int64_t r, Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St,
                              StateMix u, const float2* __restrict__ dmu, WorkMix w,
                              const float* __restrict__ res, StateMix u0, StateMix out, int rk_stage,
                              unsigned* __restrict__ err, const Nb& nb) {
-  const int L = G.len[r];
+  const int L = nb.len(G, r);
   if (L == 0) return;
   const int b = G.slice_inst[r >> 5];
   const InstState& st = St[b];
   if (st.done) return;
   const InstConst& c = C[b];
   const int S = Nb::kGlobal ? c.S : 3;
-  const float4 ni = u.nq[r];
-  if (c.visc != VISC_FCT) {                     // 'galerkin' / 'viscous': u^L is the result
+  const int me = nb.self(r);
+  const float4 ni = nb.nq[me];
+  const bool ent = c.visc == VISC_ENTROPY;
+  if (c.visc != VISC_FCT && !ent) {             // 'galerkin' / 'viscous': u^L is the result
     const float2 qL = w.qL[r];
-    finish_mix(G, c, r, S, w.hL[r], qL.x, qL.y, S == 5 ? w.q3L[r] : 0.f, S == 5 ? w.q4L[r] : 0.f, rk_stage, u0,
-               out, err);
+    finish_mix(G, c, r, S, D ? df_from_double(w.hL64[r]) : w.hL[r], qL.x, qL.y, S == 5 ? w.q3L[r] : 0.f,
+               S == 5 ? w.q4L[r] : 0.f, rk_stage, u0, out, err);
     return;
   }
-  const int64_t base = entry_base(G, r);
-  const float hi = ni.x, etai = ni.w, resi = res[r];
+  const int64_t base = nb.base(G, r);
+  const auto ip = nb.row_index(base);
+  const float2* dmp = dmu + base;
+  const float hi = ni.x, etai = ni.w, resi = nb.aux[me];
   const float invhi = inv_pos(hi);
-  const float Ri = w.rminus[r];
+  const float Ri = ent ? 1.f : nb.R[me];
+  // entropy_visc with the roundoff fix: smb_2_roundoff's h <= htiny tests
+  const float hthr = (ent && c.roundoff_fix) ? c.htinyf : 0.f;
+  const bool wet_i = !(hi <= hthr);
   float ui3 = 0.f, ui4 = 0.f;
   if (S == 5) { ui3 = u.q3[r]; ui4 = u.q4[r]; }
   float neg = 0.f, pos = 0.f;            // sum_{f < 0} f_ij, sum_{f >= 0} R_j f_ij
+  double pos64 = 0.0;                    // precision split: sum_{f >= 0} R_j f_ij in FP64
   float x1 = 0.f, x2 = 0.f, x3 = 0.f, x4 = 0.f;
   for (int k0 = 0; k0 < L; k0 += B) {    // the diagonal's terms vanish: u_i rat_ii - u_i rat_ii = 0
    int jb[B];
@@ -752,31 +936,42 @@ __device__ __forceinline__ void update_row(int64_t r, Graph G, const InstConst* 
 #pragma unroll
    for (int q = 0; q < B; q++) {
      if (k0 + q < L) {
-       const int64_t e = base + 32 * (k0 + q);
-       jb[q] = nb.index(e); const float2 v = dmu[e]; d0b[q] = v.x; m0b[q] = v.y;
+       const int off = 32 * (k0 + q);
+       jb[q] = ip[off]; const float2 v = dmp[off]; d0b[q] = v.x; m0b[q] = v.y;
      } else {
-       jb[q] = nb.self(r); d0b[q] = 0.f; m0b[q] = 0.f;
+       jb[q] = me; d0b[q] = 0.f; m0b[q] = 0.f;
      }
    }
-   float4 njb[B];
-   float rsb[B], Rjb[B];
+   float4 njb[Nb::kGlobal ? B : 1];
+   float rsb[Nb::kGlobal ? B : 1], Rjb[Nb::kGlobal ? B : 1];
+   if constexpr (Nb::kGlobal) {
 #pragma unroll
-   for (int q = 0; q < B; q++) { njb[q] = nb.nq[jb[q]]; rsb[q] = nb.aux[jb[q]]; Rjb[q] = nb.R[jb[q]]; }
+     for (int q = 0; q < B; q++) { njb[q] = nb.nq[jb[q]]; rsb[q] = nb.aux[jb[q]]; Rjb[q] = ent ? 1.f : nb.R[jb[q]]; }
+   }
 #pragma unroll
    for (int q = 0; q < B; q++) {
     if (k0 + q >= L) break;
-    const float4 nj = njb[q];
+    const float4 nj = Nb::kGlobal ? njb[q] : nb.nq[jb[q]];
     const float d0 = d0b[q], m0 = m0b[q];
-    const float rij = fmaxf(resi, rsb[q]);
+    const float rij = fmaxf(resi, Nb::kGlobal ? rsb[q] : nb.aux[jb[q]]);
     const float ddr = fminf(d0, rij) - d0, dmr = fminf(m0, rij) - m0;
     const float dz = dz_of(__fsub_rn(nj.w, etai), hi, nj.x);
-    const Recon R = recon(hi, nj.x, dz);
+    Recon R = recon(hi, nj.x, dz);
+    float rij_ = rat_of(R.Hij, hi, dz <= 0.f, invhi);
+    float rji_ = rat_of(R.Hji, nj.x, dz >= 0.f, inv_pos(nj.x));
+    if (ent) {           // the rats and the mass row's H*_ij of the stage's RHS
+      if (!wet_i) { rij_ = 0.f; R.Hij = 0.f; }
+      if (nj.x <= hthr) rji_ = 0.f;
+    }
     const float f = fct_from(ddr, dmr, hi, nj.x, R);
     float lf = Ri;
-    if (f >= 0.f) { lf = Rjb[q]; pos = __fmaf_rn(lf, f, pos); }
-    else neg = __fadd_rn(neg, f);
-    const float rij_ = rat_of(R.Hij, hi, dz <= 0.f, invhi);
-    const float rji_ = rat_of(R.Hji, nj.x, dz >= 0.f, inv_pos(nj.x));
+    if (f >= 0.f) {
+      lf = ent ? 1.f : (Nb::kGlobal ? Rjb[q] : nb.R[jb[q]]);
+      if (D && !ent) pos64 = fma(nb.R64[jb[q]], (double)f, pos64);
+      else pos = __fmaf_rn(lf, f, pos);
+    } else {
+      neg = __fadd_rn(neg, f);
+    }
     // l (dd (u_j rat_ji - u_i rat_ij) + dm (u_j (1 - rat_ji) - u_i (1 - rat_ij)))
     // = l (dm (u_j - u_i) + (dd - dm) (u_j rat_ji - u_i rat_ij))
     const float dm = dmr * lf, dx = (ddr - dmr) * lf;
@@ -793,8 +988,17 @@ __device__ __forceinline__ void update_row(int64_t r, Graph G, const InstConst* 
    }
   }
   const float invm = G.inv_lumpedf[r], dtf = st.dtf;
-  const float sh = __fadd_rn(__fmul_rn(Ri, neg), pos);
-  const float2 hn = df_add_f(w.hL[r], __fmul_rn(__fmul_rn(dtf, invm), sh));
+  float2 hn;
+  if (D) {       // u^L + dt/m sum l_ij f_ij for the depth, in FP64
+    const double sh = ent ? (double)__fadd_rn(neg, pos) : fma(nb.R64[me], (double)neg, pos64);
+    double h64 = fma(st.dt * G.inv_lumped[r], sh, w.hL64[r]);
+    if (ent && !c.roundoff_fix && h64 < 0.0) h64 = 0.0;       // smb_2: MAX(h + dt rk, 0)
+    hn = df_from_double(h64);
+  } else {
+    const float sh = __fadd_rn(__fmul_rn(Ri, neg), pos);
+    hn = df_add_f(w.hL[r], __fmul_rn(__fmul_rn(dtf, invm), sh));
+    if (ent && !c.roundoff_fix && hn.x < 0.f) hn = make_float2(0.f, 0.f);
+  }
   const float2 qL = w.qL[r];
   const float q1 = fma_(dtf, x1 * invm, qL.x);
   const float q2 = fma_(dtf, x2 * invm, qL.y);
@@ -804,29 +1008,29 @@ __device__ __forceinline__ void update_row(int64_t r, Graph G, const InstConst* 
   finish_mix(G, c, r, S, hn, q1, q2, q3, q4, rk_stage, u0, out, err);
 }
 
-template <int B>
+template <int B, bool D>
 __global__ void __launch_bounds__(256) k_update_mix(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St,
                                                     StateMix u, const float2* __restrict__ dmu, WorkMix w,
                                                     const float* __restrict__ res, StateMix u0, StateMix out,
                                                     int rk_stage, unsigned* __restrict__ err) {
-  const NbGlobal nb{G.col, u.nq, res, w.rminus};
+  const NbGlobal nb{G.col, u.nq, res, w.rminus, w.rminus64};
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < G.n_rows; r += (int64_t)gridDim.x * blockDim.x)
-    update_row<B>(r, G, C, St, u, dmu, w, res, u0, out, rk_stage, err, nb);
+    update_row<B, D>(r, G, C, St, u, dmu, w, res, u0, out, rk_stage, err, nb);
 }
 
-template <int B>
+template <int B, bool D>
 __global__ void __launch_bounds__(256) k_update_tile(Graph G, const InstConst* __restrict__ C,
                                                      const InstState* __restrict__ St, StateMix u,
                                                      const float2* __restrict__ dmu, WorkMix w,
                                                      const float* __restrict__ res, StateMix u0, StateMix out,
                                                      int rk_stage, unsigned* __restrict__ err, TileCtl tc) {
   extern __shared__ float4 tile_mem[];
-  const TileSmem sm = tile_smem(tile_mem, tc.tile_rows + tc.halo_cap);
-  const int64_t t0 = stage_tile<true, true>(G, tc, u, res, w.rminus, sm);
+  const TileSmem sm = tile_smem<D>(tile_mem, tc.tile_rows + tc.halo_cap, tc.tile_rows);
+  const int64_t t0 = stage_tile<true, true, D>(G, tc, u, res, w.rminus, sm, w.rminus64);
   const int64_t t1 = tile_end(G, tc, t0);
-  const NbTile nb{tc.loc, sm.nq, sm.aux, sm.R, t0};
+  const NbTile nb{tc.loc, sm.nq, sm.aux, sm.R, sm.R64, t0, sm.sp, sm.ln};
   for (int64_t r = t0 + threadIdx.x; r < t1; r += blockDim.x)
-    update_row<B>(r, G, C, St, u, dmu, w, res, u0, out, rk_stage, err, nb);
+    update_row<B, D>(r, G, C, St, u, dmu, w, res, u0, out, rk_stage, err, nb);
 }
 
 // One row of k_dt_mix: FP32 lambda_max, |d_ii| / m_i (main.f90:166-174; 0 for
@@ -838,15 +1042,18 @@ template <int B, class Nb>
 __device__ __forceinline__ float dt_row(int64_t r, const Graph& G, const InstConst* __restrict__ C,
                                         const InstState* __restrict__ St, const StateMix& u, float* __restrict__ dlam,
                                         float* __restrict__ alpha_out, unsigned* __restrict__ err, const Nb& nb) {
-  if (r >= G.n_rows || G.len[r] == 0) return 0.f;
+  if (r >= G.n_rows || nb.len(G, r) == 0) return 0.f;
   const int b = G.slice_inst[r >> 5];
   if (St[b].done) return 0.f;
   const InstConst& c = C[b];
   const float g = c.gf, htiny = c.htinyf;
   const LamK lk = lam_k(g, htiny);
-  const int L = G.len[r];
-  const int64_t base = entry_base(G, r);
-  const NodeF ni = node_from(u.nq[r], htiny);
+  const int L = nb.len(G, r);
+  const int64_t base = nb.base(G, r);
+  const int me = nb.self(r);
+  const auto ip = nb.row_index(base);
+  const float2* cp = G.cf + base;
+  const NodeF ni = node_from(nb.nq[me], htiny);
   const float sqi = sqrtf(g * fabsf(ni.h));
   float s = 0.f;
   float num = 0.f, denom = 0.f;          // alpha_limit stencil (as k_node_mix)
@@ -857,10 +1064,11 @@ __device__ __forceinline__ float dt_row(int64_t r, const Graph& G, const InstCon
 #pragma unroll
     for (int q = 0; q < B; q++) {
       if (k0 + q < L) {
-        const int64_t e = base + 32 * (k0 + q);
-        jb[q] = nb.index(e); cxb[q] = G.cxf[e]; cyb[q] = G.cyf[e];
+        const int off = 32 * (k0 + q);
+        const float2 cc = cp[off];
+        jb[q] = ip[off]; cxb[q] = cc.x; cyb[q] = cc.y;
       } else {
-        jb[q] = nb.self(r); cxb[q] = 1.f; cyb[q] = 0.f;
+        jb[q] = me; cxb[q] = 1.f; cyb[q] = 0.f;
       }
     }
     float4 njb[B];
@@ -904,7 +1112,7 @@ __global__ void __launch_bounds__(256) k_dt_mix(Graph G, const InstConst* __rest
                          float* __restrict__ dlam, float* __restrict__ alpha_out, unsigned* __restrict__ err) {
   // grid-stride over block-sized row ranges: every lane of a warp runs the
   // same iterations (the warp reduction needs all 32)
-  const NbGlobal nb{G.col, u.nq, nullptr, nullptr};
+  const NbGlobal nb{G.col, u.nq, nullptr, nullptr, nullptr};
   for (int64_t rb = blockIdx.x * (int64_t)blockDim.x; rb < G.n_rows; rb += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = rb + threadIdx.x;
     dt_reduce(dt_row<B>(r, G, C, St, u, dlam, alpha_out, err, nb), r, G, St);
@@ -916,9 +1124,9 @@ __global__ void __launch_bounds__(256) k_dt_tile(Graph G, const InstConst* __res
                                                  StateMix u, float* __restrict__ dlam, float* __restrict__ alpha_out,
                                                  unsigned* __restrict__ err, TileCtl tc) {
   extern __shared__ float4 tile_mem[];
-  const TileSmem sm = tile_smem(tile_mem, tc.tile_rows + tc.halo_cap);
+  const TileSmem sm = tile_smem<false>(tile_mem, tc.tile_rows + tc.halo_cap, tc.tile_rows);
   const int64_t t0 = stage_tile<false, false>(G, tc, u, nullptr, nullptr, sm);
-  const NbTile nb{tc.loc, sm.nq, nullptr, nullptr, t0};
+  const NbTile nb{tc.loc, sm.nq, nullptr, nullptr, nullptr, t0, sm.sp, sm.ln};
   // tile_rows is a multiple of 32: every lane of a warp runs the same iterations
   for (int64_t rb = t0; rb < t0 + tc.tile_rows; rb += blockDim.x) {
     const int64_t r = rb + threadIdx.x;
@@ -969,10 +1177,22 @@ static unsigned row_grid(K kern, int64_t n, int block, int mode) {
     case 2: KERNEL<2><<<row_grid(KERNEL<2>, N, BS, MODE), BS, 0, s>>>(__VA_ARGS__); break;      \
     default: KERNEL<1><<<row_grid(KERNEL<1>, N, BS, MODE), BS, 0, s>>>(__VA_ARGS__); break;     \
   }
+// the same for kernels with a second template argument D
+#define SWE_DISPATCH_BD(b, KERNEL, D, N, BS, MODE, ...)                                                         \
+  switch (b) {                                                                                                 \
+    case 8: KERNEL<8, D><<<row_grid(KERNEL<8, D>, N, BS, MODE), BS, 0, s>>>(__VA_ARGS__); break;               \
+    case 4: KERNEL<4, D><<<row_grid(KERNEL<4, D>, N, BS, MODE), BS, 0, s>>>(__VA_ARGS__); break;               \
+    case 2: KERNEL<2, D><<<row_grid(KERNEL<2, D>, N, BS, MODE), BS, 0, s>>>(__VA_ARGS__); break;               \
+    default: KERNEL<1, D><<<row_grid(KERNEL<1, D>, N, BS, MODE), BS, 0, s>>>(__VA_ARGS__); break;              \
+  }
 
 // Tile variants: one block per tile, shared memory for the tile's and the
-// halo's node records, residuals and R^- (24 B per row)
-inline size_t tile_smem_bytes(const TileCtl& tc) { return (size_t)(tc.tile_rows + tc.halo_cap) * 24; }
+// halo's node records, residuals and R^- (24 B per row; 32 B with the FP64
+// R^- of the precision split)
+size_t tile_smem_bytes(const TileCtl& tc, bool d) {
+  const size_t cap = tc.tile_rows + tc.halo_cap;
+  return cap * (d ? 32 : 24) + (size_t)tc.tile_rows / 32 * 8 + tc.tile_rows;
+}
 #define SWE_DISPATCH_TILE(b, KERNEL, BS, TC, NROWS, ...)                                                \
   do {                                                                                                \
     const TileCtl& tc_ = (TC);                                                                        \
@@ -985,25 +1205,37 @@ inline size_t tile_smem_bytes(const TileCtl& tc) { return (size_t)(tc.tile_rows 
       default: KERNEL<1><<<g_, BS, sm_, s>>>(__VA_ARGS__); break;                                     \
     }                                                                                                 \
   } while (0)
+#define SWE_DISPATCH_TILE_D(b, KERNEL, BS, TC, NROWS, D, SMEM, ...)                                     \
+  do {                                                                                                \
+    const TileCtl& tc_ = (TC);                                                                        \
+    const unsigned g_ = (unsigned)(((NROWS) + tc_.tile_rows - 1) / tc_.tile_rows);                    \
+    const size_t sm_ = (SMEM);                                                                        \
+    switch (b) {                                                                                      \
+      case 8: KERNEL<8, D><<<g_, BS, sm_, s>>>(__VA_ARGS__); break;                                   \
+      case 4: KERNEL<4, D><<<g_, BS, sm_, s>>>(__VA_ARGS__); break;                                   \
+      case 2: KERNEL<2, D><<<g_, BS, sm_, s>>>(__VA_ARGS__); break;                                   \
+      default: KERNEL<1, D><<<g_, BS, sm_, s>>>(__VA_ARGS__); break;                                  \
+    }                                                                                                 \
+  } while (0)
 
 // k_low variants: entry batch 1 or 2, lambda_max computed or taken from
 // k_dt_mix (stage 1), registers capped at 85, 64 or 51 (3, 4 or 5 resident
 // blocks of 256 threads per SM; the compiler would take ~106 with no cap)
-template <bool LAMIN>
+template <bool LAMIN, bool D>
 static void launch_low(const StageArgsMix& a, int batch, int cap, int mode, int block, bool tiled, cudaStream_t s) {
   if (tiled && a.tiles) {
     const TileCtl& tc = *a.tiles;
     const unsigned g = (unsigned)((a.G.n_rows + tc.tile_rows - 1) / tc.tile_rows);
     const size_t sm = tile_smem_bytes(tc);
 #define SWE_LOWT(BB, MB) \
-    k_low_tile<BB, LAMIN, MB><<<g, block, sm, s>>>(a.G, a.C, a.St, a.u, a.w.alpha, a.w.dmu, a.w, a.w.res, a.err, tc)
+    k_low_tile<BB, LAMIN, MB, D><<<g, block, sm, s>>>(a.G, a.C, a.St, a.u, a.w.alpha, a.w.dmu, a.w, a.w.res, a.err, tc)
     if (batch >= 2) { if (cap == 2) SWE_LOWT(2, 5); else if (cap) SWE_LOWT(2, 4); else SWE_LOWT(2, 3); }
     else { if (cap == 2) SWE_LOWT(1, 5); else if (cap) SWE_LOWT(1, 4); else SWE_LOWT(1, 3); }
 #undef SWE_LOWT
     return;
   }
 #define SWE_LOW(BB, MB)                                                                                  \
-  k_low_mix<BB, LAMIN, MB><<<row_grid(k_low_mix<BB, LAMIN, MB>, a.G.n_rows, block, mode), block, 0, s>>>( \
+  k_low_mix<BB, LAMIN, MB, D><<<row_grid(k_low_mix<BB, LAMIN, MB, D>, a.G.n_rows, block, mode), block, 0, s>>>( \
       a.G, a.C, a.St, a.u, a.w.alpha, a.w.dmu, a.w, a.w.res, a.err)
   if (batch >= 2) { if (cap == 2) SWE_LOW(2, 5); else if (cap) SWE_LOW(2, 4); else SWE_LOW(2, 3); }
   else { if (cap == 2) SWE_LOW(1, 5); else if (cap) SWE_LOW(1, 4); else SWE_LOW(1, 3); }
@@ -1012,7 +1244,8 @@ static void launch_low(const StageArgsMix& a, int batch, int cap, int mode, int 
 
 bool kind_has_tiles(int kind) { return kind >= 0 && kind <= 4; }
 
-void launch_kernel_mix(int kind, const StageArgsMix& a, const KernelTune& t, cudaStream_t s) {
+template <bool D>
+static void launch_kernel_mix_d(int kind, const StageArgsMix& a, const KernelTune& t, cudaStream_t s) {
   const int64_t n = a.G.n_rows;
   switch (kind) {
     case 1: if (t.tiled[1] && a.tiles) {
@@ -1021,29 +1254,37 @@ void launch_kernel_mix(int kind, const StageArgsMix& a, const KernelTune& t, cud
               SWE_DISPATCH_B(t.batch[1], k_node_mix, n, t.block[1], t.grid[1], a.G, a.C, a.St, a.u, a.w.alpha)
             }
             break;
-    case 2: if (a.rk_stage == 1 && a.w.dlam)   // stage 1 follows k_dt_mix on the same state
-              launch_low<true>(a, t.batch[2], t.cap_low, t.grid[2], t.block[2], t.tiled[2], s);
+    case 2: if (a.type1)                       // some instance runs 'viscous' with 'type1'
+              k_low_type1<D><<<nblk(n, 128), 128, 0, s>>>(a.G, a.C, a.St, a.u, a.w.alpha, a.w.dmu, a.w, a.w.res,
+                                                         a.err);
+            else if (a.rk_stage == 1 && a.w.dlam)   // stage 1 follows k_dt_mix on the same state
+              launch_low<true, D>(a, t.batch[2], t.cap_low, t.grid[2], t.block[2], t.tiled[2], s);
             else
-              launch_low<false>(a, t.batch[2], t.cap_low, t.grid[2], t.block[2], t.tiled[2], s);
+              launch_low<false, D>(a, t.batch[2], t.cap_low, t.grid[2], t.block[2], t.tiled[2], s);
             break;
     case 3: if (t.tiled[3] && a.tiles) {
-              SWE_DISPATCH_TILE(t.batch[3], k_fct_tile, t.block[3], *a.tiles, n, a.G, a.C, a.St, a.u, a.w.dmu, a.w, a.w.res, a.err,
-                                *a.tiles);
+              SWE_DISPATCH_TILE_D(t.batch[3], k_fct_tile, t.block[3], *a.tiles, n, D, tile_smem_bytes(*a.tiles), a.G, a.C, a.St, a.u, a.w.dmu, a.w,
+                                  a.w.res, a.err, *a.tiles);
             } else {
-              SWE_DISPATCH_B(t.batch[3], k_fct_mix, n, t.block[3], t.grid[3], a.G, a.C, a.St, a.u, a.w.dmu, a.w,
-                             a.w.res, a.err)
+              SWE_DISPATCH_BD(t.batch[3], k_fct_mix, D, n, t.block[3], t.grid[3], a.G, a.C, a.St, a.u, a.w.dmu, a.w,
+                              a.w.res, a.err)
             }
             break;
     case 4: if (t.tiled[4] && a.tiles) {
-              SWE_DISPATCH_TILE(t.batch[4], k_update_tile, t.block[4], *a.tiles, n, a.G, a.C, a.St, a.u, a.w.dmu, a.w, a.w.res,
-                                a.u0, a.out, a.rk_stage, a.err, *a.tiles);
+              SWE_DISPATCH_TILE_D(t.batch[4], k_update_tile, t.block[4], *a.tiles, n, D, tile_smem_bytes(*a.tiles, D), a.G, a.C, a.St, a.u,
+                                  a.w.dmu, a.w, a.w.res, a.u0, a.out, a.rk_stage, a.err, *a.tiles);
             } else {
-              SWE_DISPATCH_B(t.batch[4], k_update_mix, n, t.block[4], t.grid[4], a.G, a.C, a.St, a.u, a.w.dmu, a.w,
-                             a.w.res, a.u0, a.out, a.rk_stage, a.err)
+              SWE_DISPATCH_BD(t.batch[4], k_update_mix, D, n, t.block[4], t.grid[4], a.G, a.C, a.St, a.u, a.w.dmu,
+                              a.w, a.w.res, a.u0, a.out, a.rk_stage, a.err)
             }
             break;
     default: break;
   }
+}
+
+void launch_kernel_mix(int kind, const StageArgsMix& a, const KernelTune& t, cudaStream_t s) {
+  if (a.f64) launch_kernel_mix_d<true>(kind, a, t, s);
+  else launch_kernel_mix_d<false>(kind, a, t, s);
 }
 
 void launch_stage_mix(const StageArgsMix& a, cudaStream_t s, const KernelEvents* kev, const KernelTune& t) {

@@ -1,8 +1,8 @@
 """ctypes binding of libswe_gpu.so (include/swe_gpu.h).
 
-This is the binding a Python caller of the C ABI writes; the Fortran-side
-equivalent (iso_c_binding) is given in INTEGRATION.md.  Loading fails loudly
-when the library is missing: there is no CPU fallback.
+This is the binding a Python caller of the C ABI writes (a Fortran caller
+binds the same symbols through iso_c_binding).  Loading fails loudly when the
+library is missing: there is no CPU fallback.
 """
 from __future__ import annotations
 

@@ -1,7 +1,7 @@
 """Generate the committed golden fixtures of tests/golden/.
 
-Run in a container that has the reference checkout (read-only) at
-/root/reference:   python tests/golden/make_golden.py
+Run where a checkout of the reference exists (read-only is enough), giving
+its root directory:   python tests/golden/make_golden.py REFERENCE_ROOT
 
 Fixtures written (all small, numpy .npz):
   mesh_cav_{0.2,0.1,0.05}.npz  MESHES/PARABOLOID/cav_*.FEM read and renumbered
@@ -39,7 +39,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parent.parent
-REF = Path("/root/reference")
+REF = Path(sys.argv[1]) if len(sys.argv) > 1 else None
 sys.path.insert(0, str(REPO / "shallow-water-eric_gb300"))
 sys.path.insert(0, str(REPO))
 
@@ -62,6 +62,8 @@ def parse_plt(path):
 
 
 def main():
+    if REF is None or not (REF / "SOURCES" / "update.f90").exists():
+        sys.exit("usage: python tests/golden/make_golden.py REFERENCE_ROOT (the reference checkout's root)")
     for h in ("0.2", "0.1", "0.05"):
         m = M.load_mesh_free_format(REF / "MESHES/PARABOLOID" / f"cav_{h}.FEM")
         np.savez_compressed(HERE / f"mesh_cav_{h}.npz", jj=m["jj"], rr=m["rr"], jjs=m["jjs"], sides=m["sides"])

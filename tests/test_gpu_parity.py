@@ -116,14 +116,35 @@ def test_viscosity_modes_fp64_bit_exact(visc, vtype, roundoff):
     np.testing.assert_array_equal(upd.download(), u)
 
 
-@pytest.mark.parametrize("visc", ["galerkin", "viscous"])
-def test_viscosity_modes_mixed(visc):
-    """'galerkin' and 'viscous' in mixed precision against the FP64 oracle."""
-    base = C.dam_break_case(n=41, tfinal=0.05)
-    p = replace(base.params, viscosity_type=C.VISC[visc], precision=1)
-    case = replace(base, params=p)
-    u, ug, n, ng, lump = _mixed_vs_oracle(case, nsteps=5)
-    assert _rel_l1(ug[0], u[0], lump) <= MIXED_L1_TOL
+@pytest.mark.parametrize("roundoff", [1, 0])
+@pytest.mark.parametrize("prec", [1, 2])
+@pytest.mark.parametrize("visc", ["galerkin", "viscous", "entropy_visc"])
+def test_viscosity_modes_mixed(visc, prec, roundoff):
+    """'galerkin', 'viscous' and 'entropy_visc' ('type2', with and without the
+    roundoff fix) in mixed precision and its FP64 split against the FP64
+    oracle, on the dam break and on the wet/dry Gaussian-bump basin ('entropy_visc'
+    has no positivity limiter: on the wet/dry basin the reference scheme itself
+    STOPs with Min h<0, so that mode runs the dam break only)."""
+    cases = [(C.dam_break_case(n=41, tfinal=0.05), 5)]
+    if visc != "entropy_visc":
+        cases.append((C.bump_basin_case(n=40), 10))
+    for base, k in cases:
+        p = replace(base.params, viscosity_type=C.VISC[visc], precision=prec, if_roundoff_fix=roundoff)
+        case = replace(base, params=p)
+        u, ug, n, ng, lump = _mixed_vs_oracle(case, nsteps=k, prec=prec)
+        assert ug[0].min() >= 0.0
+        assert _rel_l1(ug[0], u[0], lump) <= MIXED_L1_TOL, (base.name, _rel_l1(ug[0], u[0], lump))
+
+
+@pytest.mark.parametrize("prec", [1, 2])
+def test_viscous_type1_mixed(prec):
+    """'viscous' with 'type1' (smb_1's centred flux and pressure term) in
+    mixed precision and its FP64 split against the FP64 oracle."""
+    for base, k in ((C.dam_break_case(n=41, tfinal=0.05), 5), (C.bump_basin_case(n=40), 10)):
+        p = replace(base.params, viscosity_type=C.VISC["viscous"], viscous_type=1, precision=prec)
+        case = replace(base, params=p)
+        u, ug, n, ng, lump = _mixed_vs_oracle(case, nsteps=k, prec=prec)
+        assert _rel_l1(ug[0], u[0], lump) <= MIXED_L1_TOL, (base.name, _rel_l1(ug[0], u[0], lump))
 
 
 def test_mode_combinations_the_reference_stops_on():
@@ -133,9 +154,10 @@ def test_mode_combinations_the_reference_stops_on():
         with pytest.raises(L.SweError) as ei:
             from_case(replace(base, params=p))
         assert ei.value.code == L.SWE_ERR_ARG
-    p = replace(base.params, viscosity_type=C.VISC["entropy_visc"], precision=1)
-    with pytest.raises(L.SweError):
-        from_case(replace(base, params=p))
+    sgn = C.sgn_case(nx=41, ny=3, nsteps=1)
+    p = replace(sgn.params, viscosity_type=C.VISC["viscous"], viscous_type=1, precision=1)
+    with pytest.raises(L.SweError):      # mixed 'type1' is built for 3-component systems
+        from_case(replace(sgn, params=p))
 
 
 def test_device_norms_match_oracle(golden):
@@ -304,7 +326,7 @@ def test_negative_depth_is_reported_not_trapped():
     upd.euler(u)
 
 
-def _mixed_vs_oracle(case, nsteps=None):
+def _mixed_vs_oracle(case, nsteps=None, prec=1):
     o = _oracle_for(case)
     u = case.u0.copy(order="F")
     if nsteps is None:
@@ -314,7 +336,7 @@ def _mixed_vs_oracle(case, nsteps=None):
         for _ in range(nsteps):
             t = o.rk3_step(u, t)
         n = nsteps
-    upd = from_case(case, precision=1)
+    upd = from_case(case, precision=prec)
     upd.upload(case.u0)
     upd.set_time(0.0, case.tfinal if nsteps is None else 1e30)
     tg, _, ng = upd.rk3_steps(n + 50 if nsteps is None else n)
@@ -322,14 +344,16 @@ def _mixed_vs_oracle(case, nsteps=None):
     return u, ug, n, ng, upd.lumped
 
 
+@pytest.mark.parametrize("prec", [1, 2])
 @pytest.mark.parametrize("which", ["dam", "bump"])
-def test_mixed_precision_within_tolerance(which):
-    """Well-conditioned workloads: relative L1(h) vs the FP64 oracle <= 1e-5."""
+def test_mixed_precision_within_tolerance(which, prec):
+    """Well-conditioned workloads: relative L1(h) vs the FP64 oracle <= 1e-5,
+    for the mixed path and its FP64 precision split (precision 2)."""
     if which == "dam":
         case, nsteps = C.dam_break_case(n=41, tfinal=0.05), None
     else:
         case, nsteps = C.bump_basin_case(n=60), 60
-    u, ug, n, ng, lump = _mixed_vs_oracle(case, nsteps)
+    u, ug, n, ng, lump = _mixed_vs_oracle(case, nsteps, prec)
     err = _rel_l1(ug[0], u[0], lump)
     assert ug[0].min() >= 0.0
     assert abs(ng - n) <= 1
@@ -443,7 +467,7 @@ def test_dam_break_full_size_against_oracle():
     while t < case.tfinal:
         t = o.rk3_step(u, t)
         n += 1
-    for prec in (0, 1):
+    for prec in (0, 1, 2):
         upd = from_case(case, precision=prec)
         upd.upload(case.u0)
         upd.set_time(0.0, case.tfinal)
@@ -457,7 +481,7 @@ def test_dam_break_full_size_against_oracle():
             assert tg[0] == t
         else:
             err = _rel_l1(ug[0], u[0], lump)
-            print(f"C1 mixed vs oracle after {n} steps: relative L1(h) {err:.3e}")
+            print(f"C1 precision {prec} vs oracle after {n} steps: relative L1(h) {err:.3e}")
             assert ug[0].min() >= 0.0
             assert err <= MIXED_L1_TOL, err
 
@@ -477,7 +501,7 @@ def test_set_bath_after_create_equals_create_with_bath(golden):
     np.testing.assert_array_equal(a.download(), b.download())
 
 
-@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("prec", [0, 1, 2])
 def test_lake_at_rest_is_preserved(prec):
     """Well-balancing: eta = const over random bathymetry, q = 0, all wet.
     (The reference's type2 topography term g h_i (eta_j - eta_i) c_ij is not
@@ -592,7 +616,8 @@ def test_chunked_transfers_round_trip(monkeypatch, chunks):
     ref.close()
 
 
-def test_autotuned_variants_agree(monkeypatch):
+@pytest.mark.parametrize("prec", [1, 2])
+def test_autotuned_variants_agree(monkeypatch, prec):
     """The autotuner only changes launch shapes (block size, entry batch,
     grid, register cap), all of which perform the same operations: the
     autotuned run equals the default one bit for bit."""
@@ -600,7 +625,7 @@ def test_autotuned_variants_agree(monkeypatch):
     outs = []
     for env in ("0", "1"):
         monkeypatch.setenv("SWE_AUTOTUNE", env)
-        upd = from_case(case, precision=1)
+        upd = from_case(case, precision=prec)
         upd.upload(case.u0)
         upd.set_time(0.0, 1e30)
         upd.rk3_steps(20)
@@ -794,7 +819,7 @@ def test_malpasset_time_loop_fixed_dt_and_htiny():
     upd.close()
 
 
-@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("prec", [0, 1, 2])
 def test_checkpoint_resume_is_bit_exact(tmp_path, prec):
     """A run stopped after 5 steps, saved, and resumed in a new context
     continues bit for bit like the uninterrupted run."""
@@ -809,7 +834,7 @@ def test_checkpoint_resume_is_bit_exact(tmp_path, prec):
     upd.close()
     again = from_case(case, precision=prec)
     again.load_checkpoint(tmp_path / "ck.npz")
-    if prec == 1:          # the stored launch configuration, not a new tuning
+    if prec != 0:          # the stored launch configuration, not a new tuning
         assert "fixed " in again.tuning, again.tuning
     again.rk3_steps(7)
     np.testing.assert_array_equal(again.download(), want)
@@ -818,6 +843,49 @@ def test_checkpoint_resume_is_bit_exact(tmp_path, prec):
     with pytest.raises(ValueError):
         other.load_checkpoint(tmp_path / "ck.npz")
     again.close(); other.close()
+
+
+def _thacker_converging(spacing, prec):
+    """Thacker's planar oscillation (type 5), one period, film-free initial
+    state, with htiny = 4e-4 (spacing / 0.05)^2: proportional to the lumped
+    mass, as the reference's own commented-out choice htiny ~ MINVAL(lumped)
+    (SOURCES/main.f90:64-65), and equal to the reference's type-5 value
+    1e-4 max_water_h = 4e-4 at spacing 0.05.  With the reference's fixed
+    htiny the htiny-regularised shoreline layer keeps the error near 0.02
+    under refinement (on any of the meshes tried); a fixed htiny 10x smaller
+    makes the scheme itself STOP (Min h<0) on the coarse meshes."""
+    mesh = C.thacker_mesh(spacing)
+    case = C.thacker_case(mesh, periods=1.0, cfl=0.3, film=False)
+    ht = 4e-4 * (spacing / 0.05) ** 2
+    rr = mesh["rr"]
+    u0 = np.asfortranarray(np.vstack([C.thacker_sol(k, rr, 0.0, ht, 9.81, False) for k in (1, 2, 3)]))
+    js = M.dirichlet_nodes(mesh["jjs"], mesh["sides"], [1, 2, 3, 4])
+    bc = [(k - 1, js, C.thacker_sol(k, rr[:, js - 1], 0.0, ht, 9.81, False)) for k in (1, 2, 3)]
+    case = replace(case, params=replace(case.params, htiny=ht, precision=prec), u0=u0, dirichlet=bc)
+    o = oracle.Oracle(mesh["jj"], rr)
+    rj, rg = o.gauss()
+    upd = from_case(case)
+    upd.upload(case.u0)
+    upd.set_time(0.0, case.tfinal)
+    while True:
+        t, _, k = upd.rk3_steps(4000)
+        if k < 4000:
+            break
+    u = upd.download()
+    upd.close()
+    ex = C.thacker_sol(1, rg, float(t[0]), ht, 9.81, False)
+    return o.norms(u[0], ex)[0] / o.norms(np.zeros(o.np), ex)[0]
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_thacker_converges_under_refinement(prec):
+    """C2's analytic L1 error of h after one period falls on each halving of
+    the mesh spacing (0.1, 0.05, 0.025), in FP64 and in mixed precision
+    (measured rates ~1.6 and ~1.4)."""
+    errs = [_thacker_converging(hs, prec) for hs in (0.1, 0.05, 0.025)]
+    rates = [math.log2(errs[k] / errs[k + 1]) for k in range(2)]
+    print(f"Thacker precision {prec}: L1 {errs}, rates {rates}")
+    assert all(r > 1.0 for r in rates), (errs, rates)
 
 
 def _fan(k, closed=True):
