@@ -284,6 +284,42 @@ __device__ __forceinline__ int64_t tile_end(const Graph& G, const TileCtl& tc, i
   return t0 + tc.tile_rows < G.n_rows ? t0 + tc.tile_rows : G.n_rows;
 }
 
+// L2 prefetch of a byte range with the TMA unit (cp.async.bulk.prefetch):
+// no registers or shared memory are held while the data comes in.  The range
+// is widened to the 16-byte granule the instruction requires; every array
+// passed here starts 256-byte aligned and is a multiple of 16 bytes long
+// (per-row and per-entry arrays of a multiple of 32 elements), so the
+// widened range stays inside it.
+__device__ __forceinline__ void prefetch_l2(const void* p, int64_t bytes) {
+  if (bytes <= 0) return;
+  const uint64_t a = reinterpret_cast<uint64_t>(p);
+  const uint64_t lo = a & ~uint64_t(15), hi = (a + (uint64_t)bytes + 15) & ~uint64_t(15);
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lo), "r"((unsigned)(hi - lo)) : "memory");
+}
+
+// The tile's per-entry arrays are one contiguous range (its slices are
+// consecutive): one thread of the block prefetches it into L2, with the
+// per-row arrays the rows read after their entry loops, while the block
+// stages its nodes.  e0/e1: the tile's first and one-past-last entry.
+struct TilePrefetch {
+  const void* ent[3];   // per-entry arrays
+  int esz[3];           // their element sizes (0: unused)
+  const void* row[6];   // per-row arrays
+  int rsz[6];
+};
+__device__ __forceinline__ void tile_prefetch(const Graph& G, const TileCtl& tc, const TilePrefetch& pf) {
+  if (threadIdx.x != 0) return;
+  const int64_t t0 = (int64_t)blockIdx.x * tc.tile_rows;
+  const int64_t t1 = tile_end(G, tc, t0);
+  const int64_t e0 = G.slice_ptr[t0 >> 5], e1 = G.slice_ptr[(t1 + 31) >> 5];
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+    if (pf.esz[k]) prefetch_l2(static_cast<const char*>(pf.ent[k]) + e0 * pf.esz[k], (e1 - e0) * pf.esz[k]);
+#pragma unroll
+  for (int k = 0; k < 6; k++)
+    if (pf.rsz[k]) prefetch_l2(static_cast<const char*>(pf.row[k]) + t0 * pf.rsz[k], (t1 - t0) * pf.rsz[k]);
+}
+
 // alpha_i (SOURCES/update.f90:758-781) from the stencil sums of the FP32
 // depth: |num| / denom, 1 where denom <= |num|, to the 8th power.
 __device__ __forceinline__ float alpha_from(float num, float denom) {
@@ -630,6 +666,8 @@ __global__ void __launch_bounds__(256, MINB) k_low_tile(Graph G, const InstConst
                                                         WorkMix w, float* __restrict__ res, unsigned* __restrict__ err,
                                                         TileCtl tc) {
   extern __shared__ float4 tile_mem[];
+  tile_prefetch(G, tc, TilePrefetch{{tc.loc, G.cf, w.dlam}, {2, 8, LAMIN ? 4 : 0},
+                                    {u.h, G.lumpedf, G.inv_lumpedf, G.cxiif, G.cyiif, nullptr}, {8, 4, 4, 4, 4, 0}});
   const TileSmem sm = tile_smem<false>(tile_mem, tc.tile_rows + tc.halo_cap, tc.tile_rows);
   const int64_t t0 = stage_tile<true, false>(G, tc, u, alpha, nullptr, sm);
   const int64_t t1 = tile_end(G, tc, t0);
@@ -838,6 +876,9 @@ __global__ void __launch_bounds__(256) k_fct_tile(Graph G, const InstConst* __re
                                                   const float2* __restrict__ dmu, WorkMix w,
                                                   const float* __restrict__ res, unsigned* __restrict__ err, TileCtl tc) {
   extern __shared__ float4 tile_mem[];
+  tile_prefetch(G, tc, TilePrefetch{{tc.loc, dmu, nullptr}, {2, 8, 0},
+                                    {D ? (const void*)w.hL64 : (const void*)w.hL, G.lumpedf, nullptr, nullptr,
+                                     nullptr, nullptr}, {8, 4, 0, 0, 0, 0}});
   const TileSmem sm = tile_smem<false>(tile_mem, tc.tile_rows + tc.halo_cap, tc.tile_rows);
   const int64_t t0 = stage_tile<true, false>(G, tc, u, res, nullptr, sm);
   const int64_t t1 = tile_end(G, tc, t0);
@@ -1025,6 +1066,10 @@ __global__ void __launch_bounds__(256) k_update_tile(Graph G, const InstConst* _
                                                      const float* __restrict__ res, StateMix u0, StateMix out,
                                                      int rk_stage, unsigned* __restrict__ err, TileCtl tc) {
   extern __shared__ float4 tile_mem[];
+  tile_prefetch(G, tc, TilePrefetch{{tc.loc, dmu, nullptr}, {2, 8, 0},
+                                    {w.hL, w.qL, G.inv_lumpedf, G.bathdf, rk_stage >= 2 ? (const void*)u0.nq : nullptr,
+                                     rk_stage >= 2 ? (const void*)u0.h : nullptr},
+                                    {8, 8, 4, 8, rk_stage >= 2 ? 16 : 0, rk_stage >= 2 ? 8 : 0}});
   const TileSmem sm = tile_smem<D>(tile_mem, tc.tile_rows + tc.halo_cap, tc.tile_rows);
   const int64_t t0 = stage_tile<true, true, D>(G, tc, u, res, w.rminus, sm, w.rminus64);
   const int64_t t1 = tile_end(G, tc, t0);
@@ -1124,6 +1169,8 @@ __global__ void __launch_bounds__(256) k_dt_tile(Graph G, const InstConst* __res
                                                  StateMix u, float* __restrict__ dlam, float* __restrict__ alpha_out,
                                                  unsigned* __restrict__ err, TileCtl tc) {
   extern __shared__ float4 tile_mem[];
+  tile_prefetch(G, tc, TilePrefetch{{tc.loc, G.cf, nullptr}, {2, 8, 0},
+                                    {G.inv_lumpedf, nullptr, nullptr, nullptr, nullptr, nullptr}, {4, 0, 0, 0, 0, 0}});
   const TileSmem sm = tile_smem<false>(tile_mem, tc.tile_rows + tc.halo_cap, tc.tile_rows);
   const int64_t t0 = stage_tile<false, false>(G, tc, u, nullptr, nullptr, sm);
   const NbTile nb{tc.loc, sm.nq, nullptr, nullptr, nullptr, t0, sm.sp, sm.ln};
