@@ -413,6 +413,24 @@ def run_ours(args, rank, world, dist):
         u64.close()
         log(f"fp64 timed run: {r64['dev_ms']:.1f} ms")
 
+    # the spec precision split (FP64 depth update, limiter and limited
+    # depth sum over the same FP32 fluxes) on the same workload and steps
+    split = None
+    if not args.no_fp64:
+        us = from_case(case, precision=2)
+        rs = timed_run(us, u0, args.steps, min(args.warmup, 3), dist)
+        u_s = us.download()
+        prof_s = us.profile_kernels(1)
+        vs = world * N * 3 * rs["steps"] / (rs["dev_ms"] / 1e3)
+        split = {"value": vs, "ms_per_step": rs["dev_ms"] / rs["steps"], "steps": rs["steps"],
+                 "stage_kernels_ms": {k: round(v, 4) for k, v in prof_s.items()},
+                 "speed_vs_default_mixed": vs / value}
+        if fp64:
+            w = lump
+            split["l1_rel_h_vs_fp64"] = float(np.sum(w * np.abs(u_s[0] - u_ref[0])) / np.sum(w * np.abs(u_ref[0])))
+        us.close()
+        log(f"precision split timed run: {rs['dev_ms']:.1f} ms")
+
     if rank != 0:
         return
     parity, cpu = None, None
@@ -441,6 +459,7 @@ def run_ours(args, rank, world, dist):
         "gpu_launches": r["launches"],
         "fp64": fp64,
         "speedup_mixed_vs_fp64": (value / fp64["value"]) if fp64 else None,
+        "precision_split": split,
         "parity_vs_oracle": parity,
         "batched": batched,
         "mass_rel_drift_mixed": (mass_mix - mass0) / mass0,

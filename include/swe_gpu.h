@@ -110,6 +110,16 @@ int swe_set_bath(swe_ctx* ctx, int inst, const double* bath);
  * `inst`, vals the values (NULL = zeros).  Replaces earlier data for comp. */
 int swe_set_dirichlet(swe_ctx* ctx, int inst, int comp, int n, const int* js, const double* vals);
 
+/* Time-dependent Dirichlet data on the device loop, like bdy
+ * (SOURCES/main.f90:176-188) with sol_anal (SOURCES/condlim.f90:311-831):
+ * after every RK stage swe_rk3_steps writes sol_anal(comp+1, rr(js), t) of
+ * the instance's type_test into component comp of nodes js, with t the
+ * reference's bdy time of that stage (to + dt, then (to + dt) + dt/2, then
+ * (to + dt/2) + dt; main.f90:78, 84, 90).  Built for type_test 5 and 13 and
+ * the components h, qx, qy (0-2); others -> SWE_ERR_ARG.  Replaces earlier
+ * data for comp, as swe_set_dirichlet does (and is replaced by it). */
+int swe_set_dirichlet_anal(swe_ctx* ctx, int inst, int comp, int n, const int* js);
+
 /* Sizes and the assembled matrices in the reference numbering and CSR order
  * (1-based ia/ja, like mass%ia/ja).  Any output pointer may be NULL. */
 int swe_sizes(const swe_ctx* ctx, int inst, int* np, int* nnz);

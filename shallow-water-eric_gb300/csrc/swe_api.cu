@@ -66,6 +66,9 @@ struct swe_ctx {
   double* d_dir_val = nullptr;
   std::vector<uint8_t> h_dir_mask;
   std::vector<double> h_dir_val;
+  uint8_t* d_dir_anal = nullptr;         // analytic Dirichlet components per row (on first use)
+  double* d_rr_row = nullptr;            // node coordinates per row (with d_dir_anal)
+  std::vector<uint8_t> h_dir_anal;
   // FP64 path
   StateF64 A{}, B{}, Cs{};
   WorkF64 w{};
@@ -816,18 +819,66 @@ SWE_API int swe_set_bath(swe_ctx* c, int inst, const double* bath) {
   return SWE_OK;
 }
 
+SWE_API int swe_set_dirichlet_anal(swe_ctx* c, int inst, int comp, int n, const int* js) {
+  if (!c || inst < 0 || inst >= c->n_inst || comp < 0 || comp >= c->S || n < 0 || (n > 0 && !js))
+    return fail(c, SWE_ERR_ARG, "bad Dirichlet arguments");
+  const int tt = c->params[inst].type_test;
+  if (tt != 5 && tt != 13) return fail(c, SWE_ERR_ARG, "analytic Dirichlet data are built for type_test 5 and 13");
+  if (comp > 2)   // sol_anal leaves type 13's components 4 and 5 undefined for t > 0 (condlim.f90:803-823)
+    return fail(c, SWE_ERR_ARG, "analytic Dirichlet data are built for components h, qx, qy");
+  const Layout& L = c->L;
+  for (int q = 0; q < n; q++)
+    if (js[q] < 1 || js[q] > c->meshes[inst].np) return fail(c, SWE_ERR_ARG, "Dirichlet node out of range");
+  if (!c->d_dir_anal) {   // on first use: the per-row flags and node coordinates
+    cudaError_t st = cudaSuccess;
+    c->h_dir_anal.assign(L.n_rows, 0);
+    std::vector<double> rr(2 * (size_t)L.n_rows, 0.0);
+    for (int b = 0; b < c->n_inst; b++)
+      for (int i = 0; i < c->meshes[b].np; i++) {
+        const int64_t r = L.new_of_old[b][i];
+        rr[2 * r] = c->meshes[b].rr[2 * (size_t)i];
+        rr[2 * r + 1] = c->meshes[b].rr[2 * (size_t)i + 1];
+      }
+    c->d_dir_anal = c->buf.alloc<uint8_t>(L.n_rows, st);
+    c->d_rr_row = upload_vec(c, rr, st);
+    if (st != cudaSuccess) return fail(c, SWE_ERR_CUDA, std::string("device allocation: ") + cudaGetErrorString(st));
+    c->G.dir_anal = c->d_dir_anal;
+    c->G.rr_row = c->d_rr_row;
+    drop_graphs(c);       // captured launches carry the graph's pointers
+  }
+  for (int64_t r = L.row_off[inst]; r < L.row_off[inst + 1]; r++) {
+    c->h_dir_mask[r] &= (uint8_t)~(1u << comp);
+    c->h_dir_anal[r] &= (uint8_t)~(1u << comp);
+  }
+  for (int q = 0; q < n; q++) {
+    const int64_t r = L.new_of_old[inst][js[q] - 1];
+    c->h_dir_mask[r] |= (uint8_t)(1u << comp);
+    c->h_dir_anal[r] |= (uint8_t)(1u << comp);
+  }
+  CK(cudaMemcpyAsync(c->d_dir_mask, c->h_dir_mask.data(), L.n_rows, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->d_dir_anal, c->h_dir_anal.data(), L.n_rows, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return SWE_OK;
+}
+
 SWE_API int swe_set_dirichlet(swe_ctx* c, int inst, int comp, int n, const int* js, const double* vals) {
   if (!c || inst < 0 || inst >= c->n_inst || comp < 0 || comp >= c->S || n < 0 || (n > 0 && !js))
     return fail(c, SWE_ERR_ARG, "bad Dirichlet arguments");
   const Layout& L = c->L;
   // clear the component on this instance, then set
-  for (int64_t r = L.row_off[inst]; r < L.row_off[inst + 1]; r++) c->h_dir_mask[r] &= (uint8_t)~(1u << comp);
-  for (int q = 0; q < n; q++) {
+  for (int q = 0; q < n; q++)
     if (js[q] < 1 || js[q] > c->meshes[inst].np) return fail(c, SWE_ERR_ARG, "Dirichlet node out of range");
+  for (int64_t r = L.row_off[inst]; r < L.row_off[inst + 1]; r++) {
+    c->h_dir_mask[r] &= (uint8_t)~(1u << comp);
+    if (!c->h_dir_anal.empty()) c->h_dir_anal[r] &= (uint8_t)~(1u << comp);
+  }
+  for (int q = 0; q < n; q++) {
     const int64_t r = L.new_of_old[inst][js[q] - 1];
     c->h_dir_mask[r] |= (uint8_t)(1u << comp);
     c->h_dir_val[(size_t)comp * L.n_rows + r] = vals ? vals[q] : 0.0;
   }
+  if (c->d_dir_anal)
+    CK(cudaMemcpyAsync(c->d_dir_anal, c->h_dir_anal.data(), L.n_rows, cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(c->d_dir_mask, c->h_dir_mask.data(), L.n_rows, cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(c->d_dir_val, c->h_dir_val.data(), c->h_dir_val.size() * sizeof(double), cudaMemcpyHostToDevice,
                      c->stream));

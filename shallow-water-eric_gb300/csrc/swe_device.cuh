@@ -68,7 +68,53 @@ struct Graph {
   const float2* __restrict__ bathdf;     // mixed path: bathymetry as a double-float pair
   const uint8_t* __restrict__ dir_mask;   // bit k: component k is Dirichlet
   const double* __restrict__ dir_val;     // (S, n_rows) SoA, read where masked
+  const uint8_t* __restrict__ dir_anal;   // bit k: component k's value is sol_anal(t) (or null)
+  const double* __restrict__ rr_row;      // node coordinates (x, y) per row, where dir_anal is set
 };
+
+// sol_anal(k, rr, t) (SOURCES/condlim.f90:421-456, 751-791) of the analytic
+// cases whose boundary data change with time, components 1-3 (h, qx, qy):
+// type 5 (Thacker's planar oscillation, with the current reference's +htiny
+// film) and type 13 (the SGN solitary wave).  The operations follow the
+// reference's expressions in its order; cos, sin and cosh are CUDA's.
+__device__ inline double sol_anal_dev(int type_test, int k, double x, double y, double t, double g, double htiny) {
+  if (type_test == 5) {
+    const double a = 1.0, h0 = 0.1, hL = 4.0, eta = 0.5;
+    const double omega = sqrt(2 * g * h0) / a;
+    const double dx = x - hL / 2.0, dy = y - hL / 2.0;
+    const double bathi = -h0 * (1.0 - (dx * dx + dy * dy) / (a * a));
+    const double v = (eta * h0 / (a * a)) * (2.0 * dx * cos(omega * t) + 2.0 * dy * sin(omega * t)) - bathi;
+    const double base = v > 0.0 ? v : 0.0;
+    if (k == 1) return base + htiny;
+    if (k == 2) return -eta * omega * sin(omega * t) * base;
+    return eta * omega * cos(omega * t) * base;
+  }
+  // type 13
+  const double h1 = 10.0 / 100.0, h2 = 11.0 / 100.0, x0 = 2.75;
+  const double D = sqrt(g * h2);
+  const double z = sqrt((3.0 * (h2 - h1)) / (h2 * (h1 * h1)));
+  const double arg = 1.0 / 2.0 * z * (x - x0 - D * t);
+  const double se = 1.0 / cosh(arg);
+  const double hv = h1 + (h2 - h1) * (se * se);
+  const double ht = hv > 0.0 ? hv : 0.0;
+  if (k == 1) return ht;
+  if (k == 2) return ht * D - h1 * D;
+  return ht * 0.0;
+}
+
+// Value bdy (main.f90:176-188) writes into component q of row r after RK
+// stage rk_stage of the device loop: the fixed value, or sol_anal at the
+// reference's bdy time of that stage (main.f90:78, 84, 90: to + dt, then
+// (to + dt) + dt/2, then (to + dt/2) + dt).
+__device__ inline double dirichlet_value(const Graph& G, const InstConst& c, const InstState& st, int rk_stage, int q,
+                                         int64_t r) {
+  if (G.dir_anal && ((G.dir_anal[r] >> q) & 1u)) {
+    const double to = st.time, dt = st.dt;
+    const double t = rk_stage == 1 ? to + dt : (rk_stage == 2 ? (to + dt) + dt / 2 : (to + dt / 2) + dt);
+    return sol_anal_dev(c.type_test, q + 1, G.rr_row[2 * r], G.rr_row[2 * r + 1], t, c.g, c.htiny);
+  }
+  return G.dir_val[(int64_t)q * G.n_rows + r];
+}
 
 __device__ __forceinline__ int64_t entry_base(const Graph& G, int64_t r) {
   return G.slice_ptr[r >> 5] + (r & 31);

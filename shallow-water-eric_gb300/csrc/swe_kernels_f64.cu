@@ -489,9 +489,9 @@ __device__ __forceinline__ void store_f64(const StateF64& s, int q, int64_t r, d
 // End of a stage for one row: check_hmin (when the mode has it), non-finite
 // check, the SSP-RK combination and bdy of the time loop (main.f90:77-90)
 // when rk_stage > 0, and the store.
-__device__ __forceinline__ void finish_row_f64(const Graph& G, int64_t r, int S, double (&un)[5], bool check_hmin,
-                                               int rk_stage, const StateF64& u0, const StateF64& out,
-                                               unsigned* err) {
+__device__ __forceinline__ void finish_row_f64(const Graph& G, const InstConst& c, const InstState& st, int64_t r,
+                                               int S, double (&un)[5], bool check_hmin, int rk_stage,
+                                               const StateF64& u0, const StateF64& out, unsigned* err) {
   if (check_hmin && un[0] < 0.0) atomicOr(err, ERRB_NEG_H);
   if (!(un[0] == un[0]) || !(un[1] == un[1]) || !(un[2] == un[2])) atomicOr(err, ERRB_NAN);
   const unsigned msk = (rk_stage >= 1 && G.dir_mask) ? G.dir_mask[r] : 0u;
@@ -501,7 +501,7 @@ __device__ __forceinline__ void finish_row_f64(const Graph& G, int64_t r, int S,
     double v = un[q];
     if (rk_stage == 2) v = (3 * comp_f64(u0, q, r) + v) / 4;
     else if (rk_stage == 3) v = (comp_f64(u0, q, r) + 2 * v) / 3;
-    if (msk & (1u << q)) v = G.dir_val[(int64_t)q * G.n_rows + r];
+    if (msk & (1u << q)) v = dirichlet_value(G, c, st, rk_stage, q, r);
     store_f64(out, q, r, v);
   }
 }
@@ -566,7 +566,7 @@ __global__ void k_update_f64(Graph G, const InstConst* __restrict__ C, const Ins
   for (int q = 0; q < S; q++) un[q] = ulp[q][r] + dt * (xx[q] / m);
   // check_hmin follows 'fct' (update.f90:285); 'viscous' and 'galerkin' return
   // before it (:219-222, :155-176)
-  finish_row_f64(G, r, S, un, fct_mode, rk_stage, u0, out, err);
+  finish_row_f64(G, c, st, r, S, un, fct_mode, rk_stage, u0, out, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -607,7 +607,7 @@ __global__ void k_entropy_f64(Graph G, const InstConst* __restrict__ C, const In
     un[0] = tmax(ui[0] + dt * (rs.rk2[0] / m), 0.0);
     for (int q = 1; q < S; q++) un[q] = ui[q] + dt * (rs.rk2[q] / m);
   }
-  finish_row_f64(G, r, S, un, true, rk_stage, u0, out, err);
+  finish_row_f64(G, c, st, r, S, un, true, rk_stage, u0, out, err);
 }
 
 // ---------------------------------------------------------------------------

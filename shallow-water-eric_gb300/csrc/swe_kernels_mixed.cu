@@ -889,9 +889,9 @@ __global__ void __launch_bounds__(256) k_fct_tile(Graph G, const InstConst* __re
 // End of a stage for one row: non-finite check, the SSP-RK combination and
 // bdy of the time loop (main.f90:77-90) when rk_stage > 0, and the store of
 // the double-float depth and the node record with its free surface.
-__device__ __forceinline__ void finish_mix(const Graph& G, const InstConst& c, int64_t r, int S, float2 hn, float q1,
-                                           float q2, float q3, float q4, int rk_stage, const StateMix& u0,
-                                           const StateMix& out, unsigned* err) {
+__device__ __forceinline__ void finish_mix(const Graph& G, const InstConst& c, const InstState& st, int64_t r, int S,
+                                           float2 hn, float q1, float q2, float q3, float q4, int rk_stage,
+                                           const StateMix& u0, const StateMix& out, unsigned* err) {
   if (!(hn.x == hn.x) || !(q1 == q1) || !(q2 == q2)) atomicOr(err, ERRB_NAN);
   if (rk_stage >= 2) {
     const float4 a0 = u0.nq[r];
@@ -911,9 +911,9 @@ __device__ __forceinline__ void finish_mix(const Graph& G, const InstConst& c, i
   if (rk_stage >= 1 && G.dir_mask) {
     const unsigned msk = G.dir_mask[r];
     if (msk) {
-      if (msk & 1u) hn = df_from_double(G.dir_val[r]);
-      if (msk & 2u) q1 = (float)G.dir_val[G.n_rows + r];
-      if (msk & 4u) q2 = (float)G.dir_val[2 * G.n_rows + r];
+      if (msk & 1u) hn = df_from_double(dirichlet_value(G, c, st, rk_stage, 0, r));
+      if (msk & 2u) q1 = (float)dirichlet_value(G, c, st, rk_stage, 1, r);
+      if (msk & 4u) q2 = (float)dirichlet_value(G, c, st, rk_stage, 2, r);
       if (S == 5 && (msk & 8u)) q3 = (float)G.dir_val[3 * G.n_rows + r];
       if (S == 5 && (msk & 16u)) q4 = (float)G.dir_val[4 * G.n_rows + r];
     }
@@ -953,7 +953,7 @@ __device__ __forceinline__ void update_row(int64_t r, Graph G, const InstConst* 
   const bool ent = c.visc == VISC_ENTROPY;
   if (c.visc != VISC_FCT && !ent) {             // 'galerkin' / 'viscous': u^L is the result
     const float2 qL = w.qL[r];
-    finish_mix(G, c, r, S, D ? df_from_double(w.hL64[r]) : w.hL[r], qL.x, qL.y, S == 5 ? w.q3L[r] : 0.f,
+    finish_mix(G, c, st, r, S, D ? df_from_double(w.hL64[r]) : w.hL[r], qL.x, qL.y, S == 5 ? w.q3L[r] : 0.f,
                S == 5 ? w.q4L[r] : 0.f, rk_stage, u0, out, err);
     return;
   }
@@ -1046,7 +1046,7 @@ __device__ __forceinline__ void update_row(int64_t r, Graph G, const InstConst* 
   float q3 = 0.f, q4 = 0.f;
   if (S == 5) { q3 = fma_(dtf, x3 * invm, w.q3L[r]); q4 = fma_(dtf, x4 * invm, w.q4L[r]); }
   if (hn.x < 0.f) atomicOr(err, ERRB_NEG_H);   // check_hmin (update.f90:285)
-  finish_mix(G, c, r, S, hn, q1, q2, q3, q4, rk_stage, u0, out, err);
+  finish_mix(G, c, st, r, S, hn, q1, q2, q3, q4, rk_stage, u0, out, err);
 }
 
 template <int B, bool D>

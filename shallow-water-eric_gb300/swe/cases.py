@@ -60,6 +60,7 @@ class Case:
     t0: float = 0.0                  # inputs%time at the start (1 for the reference's type 4)
     bdy: object = None               # callable(un, t): bdy (main.f90:176-188) on the host, when known
     bdy_fixed: bool = True           # Dirichlet values independent of t: the device loop can run it
+    dirichlet_anal: list = field(default_factory=list)   # [(comp0, js)] of sol_anal(t), evaluated on the device
 
 
 def _walls(mesh, S):

@@ -38,7 +38,7 @@ EXPORTS = [
     "swe_set_time", "swe_rk3_steps", "swe_mass", "swe_last_launch_count", "swe_tuning",
     "swe_last_device_ms", "swe_profile_kernels", "swe_fct_positivity_noalloc", "swe_autotune",
     "swe_write_vtk_2d", "swe_frame_fields", "swe_frame_async", "swe_frames_wait", "swe_gauges_set",
-    "swe_gauges_read", "swe_get_time", "swe_set_tuning",
+    "swe_gauges_read", "swe_get_time", "swe_set_tuning", "swe_set_dirichlet_anal",
 ]
 NOALLOC_MAX_NODES = 1 << 20   # SWE_NOALLOC_MAX_NODES
 KERNEL_KINDS = ("dt", "node", "low", "fct", "update")
@@ -75,6 +75,7 @@ def load(build: bool = True):
         "swe_set_params": ([vp, ctypes.c_int, pp], ctypes.c_int),
         "swe_set_bath": ([vp, ctypes.c_int, dp], ctypes.c_int),
         "swe_set_dirichlet": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ip, dp], ctypes.c_int),
+        "swe_set_dirichlet_anal": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ip], ctypes.c_int),
         "swe_sizes": ([vp, ctypes.c_int, ip, ip], ctypes.c_int),
         "swe_get_matrices": ([vp, ctypes.c_int, ip, ip, dp, dp, ip, dp, dp], ctypes.c_int),
         "swe_compute_dij": ([vp, ctypes.c_int, dp, dp, dp], ctypes.c_int),

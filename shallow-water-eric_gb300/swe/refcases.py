@@ -466,6 +466,11 @@ def case_from_data(d, mesh, precision=0, tfinal=None):
                                       for k in range(1, p.syst_size + 1)]))
     lists = dirichlet_lists(d, mesh)
     bc = bdy_data(tt, lists, rr, ini["bath"], ini["gravity"], ini["htiny"], t0, tf)
+    # values that change with time: the device evaluates sol_anal for types 5
+    # and 13 (components h, qx, qy; swe_set_dirichlet_anal)
+    comps = _bdy_comps(tt, lists)
+    anal = comps if bc is None and tt in (5, 13) and all(comp <= 2 for comp, _ in comps) else []
     return C.Case(f"type{tt}", mesh, p, ini["bath"], u0, tf, bc or [], t0=t0,
                   exact=lambda k, r, t: sol_anal(tt, k, r, t, ini["bath"], ini["gravity"], ini["htiny"]),
-                  bdy=make_bdy(tt, lists, rr, ini["bath"], ini["gravity"], ini["htiny"]), bdy_fixed=bc is not None)
+                  bdy=make_bdy(tt, lists, rr, ini["bath"], ini["gravity"], ini["htiny"]), bdy_fixed=bc is not None,
+                  dirichlet_anal=anal)

@@ -109,6 +109,12 @@ class Update:
         v = None if vals is None else np.ascontiguousarray(vals, np.float64)
         self._check(self._L.swe_set_dirichlet(self.h, inst, comp, len(js), _L.ip(js), _L.dp(v)))
 
+    def set_dirichlet_anal(self, comp, js, inst=0):
+        """Dirichlet data sol_anal(comp+1, rr(js), t) evaluated on the device
+        at every stage's bdy time (type_test 5 and 13, components 0-2)."""
+        js = np.ascontiguousarray(js, np.int32)
+        self._check(self._L.swe_set_dirichlet_anal(self.h, inst, comp, len(js), _L.ip(js)))
+
     # ---- per-call operators (reference-shaped) ----------------------------
     def compute_dij(self, un, inst=0):
         u = np.asfortranarray(un, np.float64)
@@ -315,10 +321,12 @@ class Update:
 
 def from_case(case, precision=None, per_call=False):
     """Build an Update for a cases.Case (bath, params and Dirichlet data).
-    A case whose Dirichlet values change with time cannot run in the device
-    loop (rk3_steps imposes fixed values): it needs ``per_call=True`` and a
-    host loop that calls euler and the case's bdy per stage."""
-    if not getattr(case, "bdy_fixed", True) and not per_call:
+    Dirichlet values that change with time run in the device loop when the
+    case lists them as analytic (``dirichlet_anal``: the device evaluates
+    sol_anal at every stage's bdy time); otherwise the case needs
+    ``per_call=True`` and a host loop that calls euler and bdy per stage."""
+    anal = getattr(case, "dirichlet_anal", None) or []
+    if not getattr(case, "bdy_fixed", True) and not per_call and not anal:
         raise ValueError(f"case {case.name}: Dirichlet values change with time; build it with per_call=True "
                          "and run it through the per-call operators")
     p = case.params
@@ -328,6 +336,9 @@ def from_case(case, precision=None, per_call=False):
     upd = Update(case.mesh, case.bath, p)
     for comp, js, vals in case.dirichlet:
         upd.set_dirichlet(comp, js, vals)
+    if not per_call:
+        for comp, js in anal:
+            upd.set_dirichlet_anal(comp, js)
     return upd
 
 

@@ -998,6 +998,61 @@ def test_time_dependent_dirichlet_through_per_call_euler(golden):
     upd.close()
 
 
+def _device_vs_host_anal(case, comps, steps, prec=0):
+    """case with analytic Dirichlet data comps [(comp, js)]: the device loop
+    (swe_set_dirichlet_anal) against main.f90's loop on the host over the
+    per-call euler with bdy = sol_anal at the reference's stage times."""
+    from swe import refcases as R
+
+    def bdy(uu, t):
+        for comp, js in comps:
+            uu[comp, js - 1] = case.exact(comp + 1, case.mesh["rr"][:, js - 1], t)
+
+    host = from_case(replace(case, dirichlet=[], dirichlet_anal=[]), precision=0, per_call=True)
+    want, tw, nw = R.host_time_loop(R.PerCall(host), bdy, case.u0, case.t0, 1e30, steps)
+    host.close()
+    dev = from_case(replace(case, dirichlet=[], dirichlet_anal=comps, bdy_fixed=False), precision=prec)
+    dev.upload(case.u0)
+    dev.set_time(case.t0, 1e30)
+    tg, _, ng = dev.rk3_steps(steps)
+    got = dev.download()
+    lump = dev.lumped
+    dev.close()
+    assert ng == nw == steps
+    return got, want, lump
+
+
+def test_time_dependent_dirichlet_on_the_device_loop(golden):
+    """SOURCES/data (type 13 solitary wave, 'entropy_visc', h imposed at both
+    channel ends from sol_anal(t)) on MESHES/SGN_CANAL/rectangle.1 through
+    the device loop, sol_anal evaluated on the device at every stage's bdy
+    time, against the host loop over the per-call euler: FP64 within 1e-12
+    (CUDA's cosh against the C library's), mixed within the L1 tolerance."""
+    from swe import data as D, refcases as R
+    d = D.read_my_data(golden / "ref_data_sources.txt")
+    mesh = M.load_mesh_free_format(golden / "ref_rectangle.1.FEM.gz")
+    case = R.case_from_data(d, mesh)
+    assert case.dirichlet_anal and not case.bdy_fixed
+    got, want, lump = _device_vs_host_anal(case, case.dirichlet_anal, 8)
+    scale = np.abs(want).max(axis=1, keepdims=True) + 1e-300
+    assert np.max(np.abs(got - want) / scale) < 1e-12
+    got1, _, _ = _device_vs_host_anal(case, case.dirichlet_anal, 8, prec=1)
+    assert _rel_l1(got1[0], want[0], lump) <= MIXED_L1_TOL
+
+
+def test_thacker_analytic_dirichlet_on_wet_nodes(golden):
+    """Type 5 with h, qx and qy imposed from sol_anal(t) on wet nodes (a disk
+    inside the moving water): the device loop against the host loop, FP64
+    within 1e-12."""
+    case = _thacker(golden, "0.2", periods=1.0, cfl=0.3)
+    rr = case.mesh["rr"]
+    js = (np.nonzero((rr[0] - 2.0) ** 2 + (rr[1] - 2.0) ** 2 < 0.3 ** 2)[0] + 1).astype(np.int32)
+    assert len(js) >= 5
+    got, want, _ = _device_vs_host_anal(case, [(0, js), (1, js), (2, js)], 6)
+    scale = np.abs(want).max(axis=1, keepdims=True) + 1e-300
+    assert np.max(np.abs(got - want) / scale) < 1e-12
+
+
 def test_degenerate_meshes_are_refused():
     """An empty mesh, an element node number out of range, a node that no
     element touches (zero lumped mass, which the reference would divide by)

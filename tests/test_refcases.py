@@ -155,18 +155,26 @@ def test_cases_the_reference_cannot_run_are_refused():
 def test_reference_data_files_set_up_their_runs():
     """SOURCES/data: type 13 ('entropy_visc', CFL 0.08, lambdaSGN 9, h
     imposed on sides 1 and 3 of the SGN channel); the solitary wave moves,
-    so the values at the channel ends change with time and the case must run
-    through the per-call loop.  PARABOLOID/data: type 12 on the disk with
-    h, qx, qy imposed on its one side; the rim is dry, so the values are
-    fixed (zero) and the device loop runs it."""
+    so the values at the channel ends change with time: the case lists them
+    as analytic data, which the device loop evaluates at every stage (or the
+    per-call loop imposes on the host).  With qx imposed too, type 13's bdy
+    writes its fourth unknown, which sol_anal leaves undefined for t > 0:
+    no analytic data, the per-call loop only.  PARABOLOID/data: type 12 on
+    the disk with h, qx, qy imposed on its one side; the rim is dry, so the
+    values are fixed (zero) and the device loop runs it."""
     d = D.read_my_data(GOLDEN / "ref_data_sources.txt")
     mesh = M.load_mesh_free_format(GOLDEN / "ref_rectangle.1.FEM.gz")
     case = R.case_from_data(d, mesh)
     assert case.params.syst_size == 5 and case.params.viscosity_type == 2 and case.params.lambda_sgn == 9.0
     assert not case.bdy_fixed and case.dirichlet == [] and case.tfinal == 5.0
-    with pytest.raises(ValueError, match="per_call"):
-        from_case(case)
     ends = M.dirichlet_nodes(mesh["jjs"], mesh["sides"], [1, 3])
+    assert len(case.dirichlet_anal) == 1 and case.dirichlet_anal[0][0] == 0
+    np.testing.assert_array_equal(np.sort(case.dirichlet_anal[0][1]), np.sort(ends))
+    d2 = dict(d, ux_nb_Dir_bdy=1, ux_Dir_list=[1])
+    case2 = R.case_from_data(d2, mesh)
+    assert not case2.bdy_fixed and case2.dirichlet_anal == []
+    with pytest.raises(ValueError, match="per_call"):
+        from_case(case2)
     u = case.u0.copy(order="F")
     case.bdy(u, 0.5)
     np.testing.assert_array_equal(u[0, ends - 1], R.sol_anal(13, 1, mesh["rr"][:, ends - 1], 0.5, None, 9.81,
