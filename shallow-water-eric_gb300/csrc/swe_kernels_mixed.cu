@@ -49,6 +49,18 @@ namespace swe {
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
 __device__ __forceinline__ float fma_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 
+// Programmatic dependent launch: the stage kernels are launched so that a
+// kernel's blocks may start while the previous kernel's last blocks still
+// run.  Each kernel lets its dependents launch at once (pdl_trigger), may
+// prefetch data no kernel writes (the graph), then waits in pdl_wait until
+// the previous grid has completed and its writes are visible, before it
+// reads anything a kernel produced or writes anything.  Completion is
+// transitive (every kernel waits before it can exit), so outputs of any
+// earlier kernel are visible after the wait.  Without the launch attribute
+// both instructions do nothing.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" :::); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // c . v with an explicit rounding sequence.  The low-order mass flux
 // (mu_ij - c.v_j) h_j is non-negative only if mu_ij >= c.v_j holds bit for
 // bit, so c.v_j is formed once per entry with a fixed rounding.
@@ -368,6 +380,8 @@ template <int B>
 __global__ void __launch_bounds__(256) k_node_mix(Graph G, const InstConst* __restrict__ C,
                                                   const InstState* __restrict__ St, StateMix u,
                                                   float* __restrict__ alpha_out) {
+  pdl_trigger();
+  pdl_wait();
   const NbGlobal nb{G.col, u.nq, nullptr, nullptr, nullptr};
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < G.n_rows; r += (int64_t)gridDim.x * blockDim.x)
     node_row<B>(r, G, C, St, u, alpha_out, nb);
@@ -378,6 +392,9 @@ __global__ void __launch_bounds__(256) k_node_tile(Graph G, const InstConst* __r
                                                    const InstState* __restrict__ St, StateMix u,
                                                    float* __restrict__ alpha_out, TileCtl tc) {
   extern __shared__ float4 tile_mem[];
+  pdl_trigger();
+  tile_prefetch(G, tc, TilePrefetch{{tc.loc, nullptr, nullptr}, {2, 0, 0}, {}, {}});
+  pdl_wait();
   const TileSmem sm = tile_smem<false>(tile_mem, tc.tile_rows + tc.halo_cap, tc.tile_rows);
   const int64_t t0 = stage_tile<false, false>(G, tc, u, nullptr, nullptr, sm);
   const int64_t t1 = tile_end(G, tc, t0);
@@ -654,6 +671,8 @@ __global__ void __launch_bounds__(256, MINB) k_low_mix(Graph G, const InstConst*
                                                        const InstState* __restrict__ St, StateMix u,
                                                        const float* __restrict__ alpha, float2* __restrict__ dmu,
                                                        WorkMix w, float* __restrict__ res, unsigned* __restrict__ err) {
+  pdl_trigger();
+  pdl_wait();
   const NbGlobal nb{G.col, u.nq, alpha, nullptr, nullptr};
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < G.n_rows; r += (int64_t)gridDim.x * blockDim.x)
     low_row<B, LAMIN, MINB, D>(r, G, C, St, u, alpha, dmu, w, res, err, nb);
@@ -666,8 +685,11 @@ __global__ void __launch_bounds__(256, MINB) k_low_tile(Graph G, const InstConst
                                                         WorkMix w, float* __restrict__ res, unsigned* __restrict__ err,
                                                         TileCtl tc) {
   extern __shared__ float4 tile_mem[];
-  tile_prefetch(G, tc, TilePrefetch{{tc.loc, G.cf, w.dlam}, {2, 8, LAMIN ? 4 : 0},
-                                    {u.h, G.lumpedf, G.inv_lumpedf, G.cxiif, G.cyiif, nullptr}, {8, 4, 4, 4, 4, 0}});
+  pdl_trigger();
+  tile_prefetch(G, tc, TilePrefetch{{tc.loc, G.cf, nullptr}, {2, 8, 0},
+                                    {G.lumpedf, G.inv_lumpedf, G.cxiif, G.cyiif, nullptr, nullptr}, {4, 4, 4, 4, 0, 0}});
+  pdl_wait();
+  tile_prefetch(G, tc, TilePrefetch{{w.dlam, nullptr, nullptr}, {LAMIN ? 4 : 0, 0, 0}, {u.h}, {8}});
   const TileSmem sm = tile_smem<false>(tile_mem, tc.tile_rows + tc.halo_cap, tc.tile_rows);
   const int64_t t0 = stage_tile<true, false>(G, tc, u, alpha, nullptr, sm);
   const int64_t t1 = tile_end(G, tc, t0);
@@ -760,6 +782,8 @@ __global__ void __launch_bounds__(256) k_low_type1(Graph G, const InstConst* __r
                                                    const InstState* __restrict__ St, StateMix u,
                                                    const float* __restrict__ alpha, float2* __restrict__ dmu, WorkMix w,
                                                    float* __restrict__ res, unsigned* __restrict__ err) {
+  pdl_trigger();
+  pdl_wait();
   const NbGlobal nb{G.col, u.nq, alpha, nullptr, nullptr};
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < G.n_rows; r += (int64_t)gridDim.x * blockDim.x) {
     if (G.len[r] == 0) continue;
@@ -865,6 +889,8 @@ template <int B, bool D>
 __global__ void __launch_bounds__(256) k_fct_mix(Graph G, const InstConst* __restrict__ C, const InstState* __restrict__ St,
                                                  StateMix u, const float2* __restrict__ dmu, WorkMix w,
                                                  const float* __restrict__ res, unsigned* __restrict__ err) {
+  pdl_trigger();
+  pdl_wait();
   const NbGlobal nb{G.col, u.nq, res, nullptr, nullptr};
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < G.n_rows; r += (int64_t)gridDim.x * blockDim.x)
     fct_row<B, D>(r, G, C, St, u, dmu, w, res, err, nb);
@@ -876,9 +902,11 @@ __global__ void __launch_bounds__(256) k_fct_tile(Graph G, const InstConst* __re
                                                   const float2* __restrict__ dmu, WorkMix w,
                                                   const float* __restrict__ res, unsigned* __restrict__ err, TileCtl tc) {
   extern __shared__ float4 tile_mem[];
-  tile_prefetch(G, tc, TilePrefetch{{tc.loc, dmu, nullptr}, {2, 8, 0},
-                                    {D ? (const void*)w.hL64 : (const void*)w.hL, G.lumpedf, nullptr, nullptr,
-                                     nullptr, nullptr}, {8, 4, 0, 0, 0, 0}});
+  pdl_trigger();
+  tile_prefetch(G, tc, TilePrefetch{{tc.loc, nullptr, nullptr}, {2, 0, 0}, {G.lumpedf}, {4}});
+  pdl_wait();
+  tile_prefetch(G, tc, TilePrefetch{{dmu, nullptr, nullptr}, {8, 0, 0},
+                                    {D ? (const void*)w.hL64 : (const void*)w.hL}, {8}});
   const TileSmem sm = tile_smem<false>(tile_mem, tc.tile_rows + tc.halo_cap, tc.tile_rows);
   const int64_t t0 = stage_tile<true, false>(G, tc, u, res, nullptr, sm);
   const int64_t t1 = tile_end(G, tc, t0);
@@ -1054,6 +1082,8 @@ __global__ void __launch_bounds__(256) k_update_mix(Graph G, const InstConst* __
                                                     StateMix u, const float2* __restrict__ dmu, WorkMix w,
                                                     const float* __restrict__ res, StateMix u0, StateMix out,
                                                     int rk_stage, unsigned* __restrict__ err) {
+  pdl_trigger();
+  pdl_wait();
   const NbGlobal nb{G.col, u.nq, res, w.rminus, w.rminus64};
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < G.n_rows; r += (int64_t)gridDim.x * blockDim.x)
     update_row<B, D>(r, G, C, St, u, dmu, w, res, u0, out, rk_stage, err, nb);
@@ -1066,10 +1096,13 @@ __global__ void __launch_bounds__(256) k_update_tile(Graph G, const InstConst* _
                                                      const float* __restrict__ res, StateMix u0, StateMix out,
                                                      int rk_stage, unsigned* __restrict__ err, TileCtl tc) {
   extern __shared__ float4 tile_mem[];
-  tile_prefetch(G, tc, TilePrefetch{{tc.loc, dmu, nullptr}, {2, 8, 0},
-                                    {w.hL, w.qL, G.inv_lumpedf, G.bathdf, rk_stage >= 2 ? (const void*)u0.nq : nullptr,
+  pdl_trigger();
+  tile_prefetch(G, tc, TilePrefetch{{tc.loc, nullptr, nullptr}, {2, 0, 0}, {G.inv_lumpedf, G.bathdf}, {4, 8}});
+  pdl_wait();
+  tile_prefetch(G, tc, TilePrefetch{{dmu, nullptr, nullptr}, {8, 0, 0},
+                                    {w.hL, w.qL, rk_stage >= 2 ? (const void*)u0.nq : nullptr,
                                      rk_stage >= 2 ? (const void*)u0.h : nullptr},
-                                    {8, 8, 4, 8, rk_stage >= 2 ? 16 : 0, rk_stage >= 2 ? 8 : 0}});
+                                    {8, 8, rk_stage >= 2 ? 16 : 0, rk_stage >= 2 ? 8 : 0}});
   const TileSmem sm = tile_smem<D>(tile_mem, tc.tile_rows + tc.halo_cap, tc.tile_rows);
   const int64_t t0 = stage_tile<true, true, D>(G, tc, u, res, w.rminus, sm, w.rminus64);
   const int64_t t1 = tile_end(G, tc, t0);
@@ -1155,6 +1188,8 @@ __device__ __forceinline__ void dt_reduce(float val, int64_t r, const Graph& G, 
 template <int B>
 __global__ void __launch_bounds__(256) k_dt_mix(Graph G, const InstConst* __restrict__ C, InstState* __restrict__ St, StateMix u,
                          float* __restrict__ dlam, float* __restrict__ alpha_out, unsigned* __restrict__ err) {
+  pdl_trigger();
+  pdl_wait();
   // grid-stride over block-sized row ranges: every lane of a warp runs the
   // same iterations (the warp reduction needs all 32)
   const NbGlobal nb{G.col, u.nq, nullptr, nullptr, nullptr};
@@ -1169,8 +1204,9 @@ __global__ void __launch_bounds__(256) k_dt_tile(Graph G, const InstConst* __res
                                                  StateMix u, float* __restrict__ dlam, float* __restrict__ alpha_out,
                                                  unsigned* __restrict__ err, TileCtl tc) {
   extern __shared__ float4 tile_mem[];
-  tile_prefetch(G, tc, TilePrefetch{{tc.loc, G.cf, nullptr}, {2, 8, 0},
-                                    {G.inv_lumpedf, nullptr, nullptr, nullptr, nullptr, nullptr}, {4, 0, 0, 0, 0, 0}});
+  pdl_trigger();
+  tile_prefetch(G, tc, TilePrefetch{{tc.loc, G.cf, nullptr}, {2, 8, 0}, {G.inv_lumpedf}, {4}});
+  pdl_wait();
   const TileSmem sm = tile_smem<false>(tile_mem, tc.tile_rows + tc.halo_cap, tc.tile_rows);
   const int64_t t0 = stage_tile<false, false>(G, tc, u, nullptr, nullptr, sm);
   const NbTile nb{tc.loc, sm.nq, nullptr, nullptr, nullptr, t0, sm.sp, sm.ln};
@@ -1190,6 +1226,31 @@ __global__ void k_refresh_eta(Graph G, StateMix u) {
 }
 
 static inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+// Launch of a stage kernel with programmatic stream serialization (the
+// kernels wait for their predecessor themselves, pdl_wait); SWE_PDL=0 makes
+// it an ordinary launch.
+static bool pdl_enabled() {
+  static const int on = [] {
+    const char* e = getenv("SWE_PDL");
+    return (e && e[0] == '0') ? 0 : 1;
+  }();
+  return on != 0;
+}
+template <typename... KArgs, typename... Args>
+static void launch_k(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
 
 // Grid of a row kernel: one thread per row (mode 0), or a resident grid of
 // mode x (blocks per SM at full occupancy) x SMs whose threads stride over
@@ -1219,18 +1280,18 @@ static unsigned row_grid(K kern, int64_t n, int block, int mode) {
 
 #define SWE_DISPATCH_B(b, KERNEL, N, BS, MODE, ...)                                              \
   switch (b) {                                                                                  \
-    case 8: KERNEL<8><<<row_grid(KERNEL<8>, N, BS, MODE), BS, 0, s>>>(__VA_ARGS__); break;      \
-    case 4: KERNEL<4><<<row_grid(KERNEL<4>, N, BS, MODE), BS, 0, s>>>(__VA_ARGS__); break;      \
-    case 2: KERNEL<2><<<row_grid(KERNEL<2>, N, BS, MODE), BS, 0, s>>>(__VA_ARGS__); break;      \
-    default: KERNEL<1><<<row_grid(KERNEL<1>, N, BS, MODE), BS, 0, s>>>(__VA_ARGS__); break;     \
+    case 8: launch_k(KERNEL<8>, row_grid(KERNEL<8>, N, BS, MODE), BS, 0, s, __VA_ARGS__); break;      \
+    case 4: launch_k(KERNEL<4>, row_grid(KERNEL<4>, N, BS, MODE), BS, 0, s, __VA_ARGS__); break;      \
+    case 2: launch_k(KERNEL<2>, row_grid(KERNEL<2>, N, BS, MODE), BS, 0, s, __VA_ARGS__); break;      \
+    default: launch_k(KERNEL<1>, row_grid(KERNEL<1>, N, BS, MODE), BS, 0, s, __VA_ARGS__); break;     \
   }
 // the same for kernels with a second template argument D
 #define SWE_DISPATCH_BD(b, KERNEL, D, N, BS, MODE, ...)                                                         \
   switch (b) {                                                                                                 \
-    case 8: KERNEL<8, D><<<row_grid(KERNEL<8, D>, N, BS, MODE), BS, 0, s>>>(__VA_ARGS__); break;               \
-    case 4: KERNEL<4, D><<<row_grid(KERNEL<4, D>, N, BS, MODE), BS, 0, s>>>(__VA_ARGS__); break;               \
-    case 2: KERNEL<2, D><<<row_grid(KERNEL<2, D>, N, BS, MODE), BS, 0, s>>>(__VA_ARGS__); break;               \
-    default: KERNEL<1, D><<<row_grid(KERNEL<1, D>, N, BS, MODE), BS, 0, s>>>(__VA_ARGS__); break;              \
+    case 8: launch_k(KERNEL<8, D>, row_grid(KERNEL<8, D>, N, BS, MODE), BS, 0, s, __VA_ARGS__); break;         \
+    case 4: launch_k(KERNEL<4, D>, row_grid(KERNEL<4, D>, N, BS, MODE), BS, 0, s, __VA_ARGS__); break;         \
+    case 2: launch_k(KERNEL<2, D>, row_grid(KERNEL<2, D>, N, BS, MODE), BS, 0, s, __VA_ARGS__); break;         \
+    default: launch_k(KERNEL<1, D>, row_grid(KERNEL<1, D>, N, BS, MODE), BS, 0, s, __VA_ARGS__); break;        \
   }
 
 // Tile variants: one block per tile, shared memory for the tile's and the
@@ -1246,10 +1307,10 @@ size_t tile_smem_bytes(const TileCtl& tc, bool d) {
     const unsigned g_ = (unsigned)(((NROWS) + tc_.tile_rows - 1) / tc_.tile_rows);                    \
     const size_t sm_ = tile_smem_bytes(tc_);                                                          \
     switch (b) {                                                                                      \
-      case 8: KERNEL<8><<<g_, BS, sm_, s>>>(__VA_ARGS__); break;                                      \
-      case 4: KERNEL<4><<<g_, BS, sm_, s>>>(__VA_ARGS__); break;                                      \
-      case 2: KERNEL<2><<<g_, BS, sm_, s>>>(__VA_ARGS__); break;                                      \
-      default: KERNEL<1><<<g_, BS, sm_, s>>>(__VA_ARGS__); break;                                     \
+      case 8: launch_k(KERNEL<8>, g_, BS, sm_, s, __VA_ARGS__); break;                                \
+      case 4: launch_k(KERNEL<4>, g_, BS, sm_, s, __VA_ARGS__); break;                                \
+      case 2: launch_k(KERNEL<2>, g_, BS, sm_, s, __VA_ARGS__); break;                                \
+      default: launch_k(KERNEL<1>, g_, BS, sm_, s, __VA_ARGS__); break;                               \
     }                                                                                                 \
   } while (0)
 #define SWE_DISPATCH_TILE_D(b, KERNEL, BS, TC, NROWS, D, SMEM, ...)                                     \
@@ -1258,10 +1319,10 @@ size_t tile_smem_bytes(const TileCtl& tc, bool d) {
     const unsigned g_ = (unsigned)(((NROWS) + tc_.tile_rows - 1) / tc_.tile_rows);                    \
     const size_t sm_ = (SMEM);                                                                        \
     switch (b) {                                                                                      \
-      case 8: KERNEL<8, D><<<g_, BS, sm_, s>>>(__VA_ARGS__); break;                                   \
-      case 4: KERNEL<4, D><<<g_, BS, sm_, s>>>(__VA_ARGS__); break;                                   \
-      case 2: KERNEL<2, D><<<g_, BS, sm_, s>>>(__VA_ARGS__); break;                                   \
-      default: KERNEL<1, D><<<g_, BS, sm_, s>>>(__VA_ARGS__); break;                                  \
+      case 8: launch_k(KERNEL<8, D>, g_, BS, sm_, s, __VA_ARGS__); break;                             \
+      case 4: launch_k(KERNEL<4, D>, g_, BS, sm_, s, __VA_ARGS__); break;                             \
+      case 2: launch_k(KERNEL<2, D>, g_, BS, sm_, s, __VA_ARGS__); break;                             \
+      default: launch_k(KERNEL<1, D>, g_, BS, sm_, s, __VA_ARGS__); break;                            \
     }                                                                                                 \
   } while (0)
 
@@ -1275,15 +1336,16 @@ static void launch_low(const StageArgsMix& a, int batch, int cap, int mode, int 
     const unsigned g = (unsigned)((a.G.n_rows + tc.tile_rows - 1) / tc.tile_rows);
     const size_t sm = tile_smem_bytes(tc);
 #define SWE_LOWT(BB, MB) \
-    k_low_tile<BB, LAMIN, MB, D><<<g, block, sm, s>>>(a.G, a.C, a.St, a.u, a.w.alpha, a.w.dmu, a.w, a.w.res, a.err, tc)
+    launch_k(k_low_tile<BB, LAMIN, MB, D>, g, block, sm, s, a.G, a.C, a.St, a.u, a.w.alpha, a.w.dmu, a.w, a.w.res, \
+             a.err, tc)
     if (batch >= 2) { if (cap == 2) SWE_LOWT(2, 5); else if (cap) SWE_LOWT(2, 4); else SWE_LOWT(2, 3); }
     else { if (cap == 2) SWE_LOWT(1, 5); else if (cap) SWE_LOWT(1, 4); else SWE_LOWT(1, 3); }
 #undef SWE_LOWT
     return;
   }
 #define SWE_LOW(BB, MB)                                                                                  \
-  k_low_mix<BB, LAMIN, MB, D><<<row_grid(k_low_mix<BB, LAMIN, MB, D>, a.G.n_rows, block, mode), block, 0, s>>>( \
-      a.G, a.C, a.St, a.u, a.w.alpha, a.w.dmu, a.w, a.w.res, a.err)
+  launch_k(k_low_mix<BB, LAMIN, MB, D>, row_grid(k_low_mix<BB, LAMIN, MB, D>, a.G.n_rows, block, mode), block, 0, s, \
+           a.G, a.C, a.St, a.u, a.w.alpha, a.w.dmu, a.w, a.w.res, a.err)
   if (batch >= 2) { if (cap == 2) SWE_LOW(2, 5); else if (cap) SWE_LOW(2, 4); else SWE_LOW(2, 3); }
   else { if (cap == 2) SWE_LOW(1, 5); else if (cap) SWE_LOW(1, 4); else SWE_LOW(1, 3); }
 #undef SWE_LOW
@@ -1302,8 +1364,8 @@ static void launch_kernel_mix_d(int kind, const StageArgsMix& a, const KernelTun
             }
             break;
     case 2: if (a.type1)                       // some instance runs 'viscous' with 'type1'
-              k_low_type1<D><<<nblk(n, 128), 128, 0, s>>>(a.G, a.C, a.St, a.u, a.w.alpha, a.w.dmu, a.w, a.w.res,
-                                                         a.err);
+              launch_k(k_low_type1<D>, nblk(n, 128), 128, 0, s, a.G, a.C, a.St, a.u, a.w.alpha, a.w.dmu, a.w, a.w.res,
+                       a.err);
             else if (a.rk_stage == 1 && a.w.dlam)   // stage 1 follows k_dt_mix on the same state
               launch_low<true, D>(a, t.batch[2], t.cap_low, t.grid[2], t.block[2], t.tiled[2], s);
             else
