@@ -139,7 +139,8 @@ void launch_norms(int field, int precision, const StateF64& a, const StateMix& m
 // ---- total mass sum_i m_i h_i per instance (main.f90:94-99 monitors it),
 // added in a fixed order so that every call gives the same bits: one
 // double-double partial per 32-row slice (a slice belongs to one instance),
-// then one block per instance adds its slices like k_norms_final.
+// then one block per instance adds its slices like k_norms_final, with
+// 1024 threads (an instance may hold 10^5 slices).
 __global__ void k_mass_part(Graph G, const double* __restrict__ h64, const float2* __restrict__ hdf,
                             double* __restrict__ part) {
   const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -152,21 +153,23 @@ __global__ void k_mass_part(Graph G, const double* __restrict__ h64, const float
   }
 }
 
-__global__ void __launch_bounds__(kNormThreads) k_mass_final(const double* __restrict__ part,
+constexpr int kMassThreads = 1024;
+
+__global__ void __launch_bounds__(kMassThreads) k_mass_final(const double* __restrict__ part,
                                                              const int64_t* __restrict__ inst_slice,
                                                              double* __restrict__ acc) {
   const int b = blockIdx.x;
   double v = 0.0, c = 0.0;
-  for (int64_t w = inst_slice[b] + threadIdx.x; w < inst_slice[b + 1]; w += kNormThreads)
+  for (int64_t w = inst_slice[b] + threadIdx.x; w < inst_slice[b + 1]; w += kMassThreads)
     dd_add(v, c, part[2 * w], part[2 * w + 1]);
   dd_warp_sum(v, c);
-  __shared__ double sw[kNormThreads / 32][2];
+  __shared__ double sw[kMassThreads / 32][2];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0) { sw[warp][0] = v; sw[warp][1] = c; }
   __syncthreads();
   if (threadIdx.x == 0) {
     double a = 0.0, e = 0.0;
-    for (int k = 0; k < kNormThreads / 32; k++) dd_add(a, e, sw[k][0], sw[k][1]);
+    for (int k = 0; k < kMassThreads / 32; k++) dd_add(a, e, sw[k][0], sw[k][1]);
     acc[2 * b] = a;
     acc[2 * b + 1] = e;
   }
@@ -175,7 +178,7 @@ __global__ void __launch_bounds__(kNormThreads) k_mass_final(const double* __res
 void launch_mass(const Graph& G, int n_inst, const double* h64, const float2* hdf, const int64_t* inst_slice,
                  double* part, double* acc, cudaStream_t s) {
   k_mass_part<<<(unsigned)((G.n_rows + 255) / 256), 256, 0, s>>>(G, h64, hdf, part);
-  k_mass_final<<<n_inst, kNormThreads, 0, s>>>(part, inst_slice, acc);
+  k_mass_final<<<n_inst, kMassThreads, 0, s>>>(part, inst_slice, acc);
 }
 
 }  // namespace swe
