@@ -198,6 +198,17 @@ int swe_get_time(swe_ctx* ctx, double* time, double* t_final, double* dt);
  * time and last dt; steps_done (nullable) the number of steps instance 0 ran. */
 int swe_rk3_steps(swe_ctx* ctx, int nsteps, double* time_out, double* dt_out, int* steps_done);
 
+/* swe_upload(un), swe_rk3_steps(nsteps), swe_download(unext) as one call with
+ * one synchronisation: the host-buffer form of the reference's time loop
+ * (SOURCES/main.f90:61-91 around euler, SOURCES/update.f90:134-289), where
+ * un and unext are host arrays.  The state goes up in chunks on several copy
+ * streams, the steps run as the captured graph, and the new state comes back
+ * in chunks while the next chunk is permuted.  un == NULL keeps the device
+ * state, unext == NULL skips the download; un == unext is allowed.  Results
+ * are bit-identical to the three separate calls. */
+int swe_rk3_steps_host(swe_ctx* ctx, const double* un, double* unext, int nsteps, double* time_out,
+                       double* dt_out, int* steps_done);
+
 /* Total water mass sum_i m_i h_i per instance: double-double sums added in a
  * fixed order, so every call on the same state gives the same bits. */
 int swe_mass(swe_ctx* ctx, double* mass_out);

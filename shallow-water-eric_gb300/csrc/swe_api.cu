@@ -1573,9 +1573,10 @@ SWE_API int swe_gauges_read(swe_ctx* c, int max_rows, double* out, int* rows, lo
   return SWE_OK;
 }
 
-SWE_API int swe_rk3_steps(swe_ctx* c, int nsteps, double* time_out, double* dt_out, int* steps_done) {
-  NvtxRange nvtx("swe_rk3_steps");
-  if (!c || nsteps < 0) return fail(c, SWE_ERR_ARG, "bad arguments");
+// The steps of swe_rk3_steps enqueued on the context's stream (the autotuner
+// runs on the first call, on the state the stream holds by then), between the
+// t0 / t1 events.
+static int enqueue_rk3_steps(swe_ctx* c, int nsteps) {
   int rc;
   if (!c->tuned) {
     const char* env = getenv("SWE_AUTOTUNE");
@@ -1607,10 +1608,15 @@ SWE_API int swe_rk3_steps(swe_ctx* c, int nsteps, double* time_out, double* dt_o
   CK(cudaGetLastError());
   c->last_launches = launches;
   c->euler_done = false;
-  // the instances' state and the error word in one synchronisation
+  return SWE_OK;
+}
+
+// The instances' clocks and the error word after everything enqueued, in one
+// synchronisation.
+static int finish_rk3_steps(swe_ctx* c, double* time_out, double* dt_out, int* steps_done) {
   std::vector<InstState> out(c->n_inst);
   CK(cudaMemcpyAsync(out.data(), c->d_St, sizeof(InstState) * c->n_inst, cudaMemcpyDeviceToHost, c->stream));
-  rc = read_errors(c);
+  const int rc = read_errors(c);
   for (int b = 0; b < c->n_inst; b++) {
     if (time_out) time_out[b] = out[b].time;
     if (dt_out) dt_out[b] = out[b].dt;
@@ -1620,6 +1626,28 @@ SWE_API int swe_rk3_steps(swe_ctx* c, int nsteps, double* time_out, double* dt_o
   CK(cudaEventElapsedTime(&ms, c->t0, c->t1));
   c->last_ms = ms;
   return rc;
+}
+
+SWE_API int swe_rk3_steps(swe_ctx* c, int nsteps, double* time_out, double* dt_out, int* steps_done) {
+  NvtxRange nvtx("swe_rk3_steps");
+  if (!c || nsteps < 0) return fail(c, SWE_ERR_ARG, "bad arguments");
+  const int rc = enqueue_rk3_steps(c, nsteps);
+  if (rc) return rc;
+  return finish_rk3_steps(c, time_out, dt_out, steps_done);
+}
+
+SWE_API int swe_rk3_steps_host(swe_ctx* c, const double* un, double* unext, int nsteps, double* time_out,
+                               double* dt_out, int* steps_done) {
+  NvtxRange nvtx("swe_rk3_steps_host");
+  if (!c || nsteps < 0) return fail(c, SWE_ERR_ARG, "bad arguments");
+  const int64_t nn = c->node_off[c->n_inst];
+  int rc;
+  if (un && (rc = to_device(c, un, false, 0, nn))) return rc;
+  if ((rc = enqueue_rk3_steps(c, nsteps))) return rc;
+  if (unext && (rc = from_device_state(c, unext, false, 0, nn, c->precision == SWE_PREC_FP64 ? &c->A : nullptr,
+                                       c->precision == SWE_PREC_FP64 ? nullptr : &c->mA)))
+    return rc;
+  return finish_rk3_steps(c, time_out, dt_out, steps_done);
 }
 
 SWE_API double swe_last_device_ms(const swe_ctx* c) { return c ? c->last_ms : 0.0; }

@@ -39,6 +39,7 @@ EXPORTS = [
     "swe_last_device_ms", "swe_profile_kernels", "swe_fct_positivity_noalloc", "swe_autotune",
     "swe_write_vtk_2d", "swe_frame_fields", "swe_frame_async", "swe_frames_wait", "swe_gauges_set",
     "swe_gauges_read", "swe_get_time", "swe_set_tuning", "swe_set_dirichlet_anal",
+    "swe_rk3_steps_host",
 ]
 NOALLOC_MAX_NODES = 1 << 20   # SWE_NOALLOC_MAX_NODES
 KERNEL_KINDS = ("dt", "node", "low", "fct", "update")
@@ -92,6 +93,7 @@ def load(build: bool = True):
         "swe_set_time": ([vp, dp, dp], ctypes.c_int),
         "swe_get_time": ([vp, dp, dp, dp], ctypes.c_int),
         "swe_rk3_steps": ([vp, ctypes.c_int, dp, dp, ip], ctypes.c_int),
+        "swe_rk3_steps_host": ([vp, dp, dp, ctypes.c_int, dp, dp, ip], ctypes.c_int),
         "swe_mass": ([vp, dp], ctypes.c_int),
         "swe_last_launch_count": ([vp], ctypes.c_longlong),
         "swe_tuning": ([vp], ctypes.c_char_p),

@@ -290,6 +290,25 @@ class Update:
         self._check(self._L.swe_rk3_steps(self.h, nsteps, _L.dp(t), _L.dp(dt), ctypes.byref(n)))
         return t, dt, n.value
 
+    def rk3_steps_host_ptr(self, in_ptr, out_ptr, nsteps):
+        """Upload from host pointer in_ptr (reference layout; 0 keeps the device
+        state), nsteps steps, download to out_ptr (0 skips it): one call, one
+        synchronisation."""
+        t = np.zeros(self.n_inst); dt = np.zeros(self.n_inst); n = ctypes.c_int()
+        cast = lambda p: ctypes.cast(p, ctypes.POINTER(ctypes.c_double)) if p else None
+        self._check(self._L.swe_rk3_steps_host(self.h, cast(in_ptr), cast(out_ptr), nsteps, _L.dp(t), _L.dp(dt),
+                                               ctypes.byref(n)))
+        return t, dt, n.value
+
+    def rk3_steps_host(self, un, nsteps):
+        """rk3_steps_host_ptr on numpy arrays: returns the new state (S, np)."""
+        u = np.asfortranarray(np.asarray(un, dtype=np.float64))
+        if u.shape != (self.S, int(self.node_off[-1])):
+            raise ValueError(f"state of shape {u.shape}, expected {(self.S, int(self.node_off[-1]))}")
+        out = np.zeros_like(u, order="F")
+        self.rk3_steps_host_ptr(u.ctypes.data, out.ctypes.data, nsteps)
+        return out
+
     def total_mass(self):
         m = np.zeros(self.n_inst)
         self._check(self._L.swe_mass(self.h, _L.dp(m)))

@@ -845,6 +845,36 @@ def test_checkpoint_resume_is_bit_exact(tmp_path, prec):
     again.close(); other.close()
 
 
+@pytest.mark.parametrize("prec", [0, 1, 2])
+def test_rk3_steps_host_equals_the_three_calls(prec):
+    """swe_rk3_steps_host (upload, steps, download in one call) gives the bits
+    of swe_upload + swe_rk3_steps + swe_download, also in place (un == unext)
+    and with either transfer skipped."""
+    case = C.dam_break_case(n=41)
+    a = from_case(case, precision=prec)
+    b = from_case(case, precision=prec)
+    for u in (a, b):
+        u.set_time(0.0, 0.2)
+    a.upload(case.u0)
+    ta, dta, na = a.rk3_steps(3)
+    want = a.download()
+    got = b.rk3_steps_host(case.u0, 3)
+    np.testing.assert_array_equal(got, want)
+    tb, _, dtb = b.get_time()
+    assert tb[0] == ta[0] and dtb[0] == dta[0]
+    # in place: the same buffer in and out, then a run with no upload
+    buf = np.asfortranarray(want.copy())
+    b.rk3_steps_host_ptr(buf.ctypes.data, buf.ctypes.data, 2)
+    a.rk3_steps(2)
+    np.testing.assert_array_equal(buf, a.download())
+    b.rk3_steps_host_ptr(0, 0, 1)
+    a.rk3_steps(1)
+    np.testing.assert_array_equal(b.download(), a.download())
+    with pytest.raises(ValueError):
+        b.rk3_steps_host(case.u0[:, :-1], 1)
+    a.close(); b.close()
+
+
 def _thacker_converging(spacing, prec):
     """Thacker's planar oscillation (type 5), one period, film-free initial
     state, with htiny = 4e-4 (spacing / 0.05)^2: proportional to the lumped
