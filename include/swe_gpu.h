@@ -263,12 +263,13 @@ int swe_set_tuning(swe_ctx* ctx, const char* spec);
  *   htiny     inputs%htiny
  *   d_lij     l_ij per CSR entry (output)
  *   stream    cudaStream_t to launch on (NULL = default stream); the call
- *             synchronises that stream before returning.
+ *             synchronises that stream before returning, so it cannot be
+ *             recorded into a CUDA graph (stream capture).
  * The scratch array (SWE_NOALLOC_MAX_NODES doubles, 8 MiB) is held by every
  * GPU that loads the library until the process exits and is shared by all
  * calls: calls that overlap on the GPU race, so serialise them.  The first
  * call on a device looks up the array's address for that device (with it
- * current); make that first call before any stream capture. */
+ * current). */
 #define SWE_NOALLOC_MAX_NODES (1 << 20)
 int swe_fct_positivity_noalloc(int np, const int* d_ia, const int* d_ja, const double* d_unext,
                                const double* d_mat, double htiny, double* d_lij, void* stream);

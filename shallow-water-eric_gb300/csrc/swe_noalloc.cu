@@ -20,8 +20,9 @@
 //    them.  The array keeps the previous call's contents; nothing in it needs
 //    to start at zero because every R^-_i is written before it is read.
 //  * The first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress while that device is current, once per device.  Make
-//    that first call before any stream capture.
+//    cudaGetSymbolAddress while that device is current, once per device.
+//  * Every call synchronises the caller's stream before it returns (to read
+//    the column-check flag), so no call can be recorded into a CUDA graph.
 //  * d_ia and d_ja must form a valid 1-based CSR structure of the caller's
 //    d_mat / d_lij arrays (ia(1) = 1, non-decreasing).  Column indices are
 //    checked on the device: a column outside 1..np is not read through, and
