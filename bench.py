@@ -135,6 +135,19 @@ def b_alg(n, nnz, precision, S=3):
     return n * (3 * 8 * S + 8 + 8 + 4) + nnz * (4 + 2 * 8)
 
 
+def design_bytes(n, nnz):
+    """Bytes per node that each mixed stage kernel reads and writes once per
+    launch in the four-sweep design (3-component systems), with e the
+    off-diagonal entries per row (16-bit position, c_ij or (d, mu), |c|lambda
+    per entry): k_dt 25 + 14e; k_low 65 + 18e, plus 4e in stage 1 (it reads
+    k_dt's |c|lambda); k_fct 37 + 10e; k_update 78 + 10e, plus 24 in stages 2
+    and 3 (u0); k_node 21 + 4e in stages 2 and 3.  Averaged per stage like
+    swe_profile_kernels' times."""
+    e = (nnz - n) / n
+    return {"dt": 25 + 14 * e, "node": (21 + 4 * e) * 2 / 3, "low": 65 + 18 * e + 4 * e / 3,
+            "fct": 37 + 10 * e, "update": 78 + 10 * e + 16}
+
+
 def make_case(n):
     from swe import cases as C
     return C.bump_basin_case(n=n, nsteps=200)
@@ -361,6 +374,9 @@ def run_ours(args, rank, world, dist):
     peak, peak_kind = peaks()
     balg = b_alg(N, nnz, 1)
     achieved = balg / (stage_ms / 1e3) / 1e9
+    kernel_bw = {k: {"ms": round(prof[k], 4), "design_bytes_per_node": round(b, 1),
+                     "gbs": round(b * N / (prof[k] / 1e3) / 1e9, 1)}
+                 for k, b in design_bytes(N, nnz).items() if prof.get(k)}
     traffic = None
     tf = ROOT / "profiles" / "traffic_per_node_stage.json"
     if tf.exists():
@@ -463,6 +479,7 @@ def run_ours(args, rank, world, dist):
                      "unit_of_work": "one RK stage (k_node+k_low+k_fct+k_update), algorithmic bytes "
                                      f"{balg / N:.1f} B/node"},
         "stage_kernels_ms": {k: round(v, 4) for k, v in prof.items()},
+        "kernel_design_bandwidth": kernel_bw,
         "setup_s": round(setup_s, 3),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": S * N * 8, "d2h_bytes_per_step": S * N * 8,
                 "api": "swe_rk3_steps_host (one call per step)", "three_calls_value": e2e3_value},
