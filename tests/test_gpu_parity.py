@@ -455,6 +455,41 @@ def test_mass_change_at_walls_follows_the_reference_scheme():
     assert abs(mass[1] - mass[0]) <= 5e-8 * m0
 
 
+def test_wetdry_basin_full_size_against_oracle():
+    """C3 at its full size: the 4M-node wet/dry basin (2000 x 2000 jittered
+    lattice on [0, 10]^2, Gaussian-bump bathymetry, Manning friction, dry
+    shores), two SSP-RK3 steps from the workload's own initial state, the
+    oracle on every host core beside it.  FP64 equals the oracle to 1e-13
+    relative (Manning's pow is the one libm call whose last bit may differ
+    from the host's); the mixed path and its precision split are within
+    1e-8 relative L1(h) (1.6e-9 after 15 steps in bench.py), with h >= 0
+    and the same dt as the oracle to FP32 rounding."""
+    case = C.bump_basin_case(n=2000, nsteps=200)
+    steps = 2
+    o = _oracle_for(case)
+    u = case.u0.copy(order="F")
+    t = 0.0
+    for _ in range(steps):
+        t = o.rk3_step(u, t)
+    del o
+    for prec in (0, 1, 2):
+        upd = from_case(case, precision=prec)
+        upd.set_time(0.0, 1e30)
+        ug = upd.rk3_steps_host(case.u0, steps)
+        tg = upd.get_time()[0][0]
+        lump = upd.lumped
+        upd.close()
+        if prec == 0:
+            assert np.max(np.abs(ug - u)) <= 1e-13 * np.max(np.abs(u)), np.max(np.abs(ug - u))
+            assert abs(tg - t) <= 1e-13 * t
+        else:
+            err = _rel_l1(ug[0], u[0], lump)
+            print(f"C3 precision {prec} vs oracle after {steps} steps: relative L1(h) {err:.3e}")
+            assert ug[0].min() >= 0.0
+            assert err <= 1e-8, err
+            assert abs(tg - t) <= 1e-6 * t
+
+
 def test_dam_break_full_size_against_oracle():
     """C1 at its full size: the 101x101 lattice dam break run to t = 0.2 (the
     dt of each step from the CFL condition, unclipped at t_final, as in the
