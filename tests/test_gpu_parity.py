@@ -490,6 +490,43 @@ def test_wetdry_basin_full_size_against_oracle():
             assert abs(tg - t) <= 1e-6 * t
 
 
+def test_sgn_channel_full_size_against_oracle():
+    """C5 at its full size: the 10001 x 201 SGN channel (2,010,201 nodes, five
+    unknowns, mSGN_RHS source, walls on the long sides), the solitary wave,
+    three SSP-RK3 steps.  FP64 equals the oracle bit for bit.  The mixed
+    path is held to 3x the oracle's own sensitivity over the same steps (the
+    oracle from the initial state perturbed by 1e-7 relative, seeded), plus
+    1e-9: the stiff relaxation makes the case ill-conditioned over long
+    runs."""
+    case = C.sgn_case()
+    steps = 3
+    o = _oracle_for(case)
+    u = case.u0.copy(order="F")
+    t = 0.0
+    for _ in range(steps):
+        t = o.rk3_step(u, t)
+    up = case.u0.copy(order="F")
+    up *= 1 + 1e-7 * np.random.default_rng(0).uniform(-1, 1, up.shape)
+    tp = 0.0
+    for _ in range(steps):
+        tp = o.rk3_step(up, tp)
+    del o
+    for prec in (0, 1):
+        upd = from_case(case, precision=prec)
+        upd.set_time(0.0, 1e30)
+        ug = upd.rk3_steps_host(case.u0, steps)
+        lump = upd.lumped
+        upd.close()
+        if prec == 0:
+            np.testing.assert_array_equal(ug, u)
+        else:
+            err = _rel_l1(ug[0], u[0], lump)
+            sens = _rel_l1(up[0], u[0], lump)
+            print(f"C5 mixed vs oracle after {steps} steps: relative L1(h) {err:.3e} (oracle sensitivity {sens:.3e})")
+            assert ug[0].min() >= 0.0
+            assert err <= 3 * sens + 1e-9, (err, sens)
+
+
 def test_dam_break_full_size_against_oracle():
     """C1 at its full size: the 101x101 lattice dam break run to t = 0.2 (the
     dt of each step from the CFL condition, unclipped at t_final, as in the
