@@ -645,6 +645,9 @@ def run_single(args, which):
         res[prec] = u
         out[("fp64" if prec == 0 else "mixed") + "_node_stage_per_s"] = v
         out["steps"] = n
+        if prec == 1:
+            out["mixed_tuning"] = upd.tuning
+            out["mixed_stage_kernels_ms"] = {k: round(v, 4) for k, v in upd.profile_kernels(3).items()}
         lump = upd.lumped
         upd.close()
     out["mixed_vs_fp64_l1_h"] = float(np.sum(lump * np.abs(res[1][0] - res[0][0])) / np.sum(lump * np.abs(res[0][0])))
