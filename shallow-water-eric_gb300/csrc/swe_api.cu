@@ -449,6 +449,14 @@ static int copy_setup(swe_ctx* c) {
   return SWE_OK;
 }
 
+// Waits for every copy stream and the context's stream: after an error, so
+// that no transfer still reads or writes a caller's buffer once the call has
+// returned.
+static void drain(swe_ctx* c) {
+  for (int k = 0; k < c->copy_chunks; k++) cudaStreamSynchronize(c->copy_stream[k]);
+  cudaStreamSynchronize(c->stream);
+}
+
 static int to_device(swe_ctx* c, const double* un, bool device_src, int64_t node_begin, int64_t node_end) {
   const int64_t nn = node_end - node_begin;
   if (nn <= 0) return SWE_OK;
@@ -1148,7 +1156,7 @@ SWE_API int swe_upload(swe_ctx* c, const double* un) {
   NvtxRange nvtx("swe_upload");
   if (!c || !un) return fail(c, SWE_ERR_ARG, "bad arguments");
   int rc = to_device(c, un, false, 0, c->node_off[c->n_inst]);
-  if (rc) return rc;
+  if (rc) { drain(c); return rc; }
   CK(cudaStreamSynchronize(c->stream));
   return SWE_OK;
 }
@@ -1158,7 +1166,7 @@ SWE_API int swe_download(swe_ctx* c, double* un) {
   if (!c || !un) return fail(c, SWE_ERR_ARG, "bad arguments");
   int rc = from_device_state(c, un, false, 0, c->node_off[c->n_inst], c->precision == SWE_PREC_FP64 ? &c->A : nullptr,
                              c->precision == SWE_PREC_FP64 ? nullptr : &c->mA);
-  if (rc) return rc;
+  if (rc) { drain(c); return rc; }
   CK(cudaStreamSynchronize(c->stream));
   return SWE_OK;
 }
@@ -1642,11 +1650,12 @@ SWE_API int swe_rk3_steps_host(swe_ctx* c, const double* un, double* unext, int 
   if (!c || nsteps < 0) return fail(c, SWE_ERR_ARG, "bad arguments");
   const int64_t nn = c->node_off[c->n_inst];
   int rc;
-  if (un && (rc = to_device(c, un, false, 0, nn))) return rc;
-  if ((rc = enqueue_rk3_steps(c, nsteps))) return rc;
-  if (unext && (rc = from_device_state(c, unext, false, 0, nn, c->precision == SWE_PREC_FP64 ? &c->A : nullptr,
-                                       c->precision == SWE_PREC_FP64 ? nullptr : &c->mA)))
+  if ((un && (rc = to_device(c, un, false, 0, nn))) || (rc = enqueue_rk3_steps(c, nsteps)) ||
+      (unext && (rc = from_device_state(c, unext, false, 0, nn, c->precision == SWE_PREC_FP64 ? &c->A : nullptr,
+                                        c->precision == SWE_PREC_FP64 ? nullptr : &c->mA)))) {
+    drain(c);
     return rc;
+  }
   return finish_rk3_steps(c, time_out, dt_out, steps_done);
 }
 
