@@ -959,7 +959,7 @@ SWE_API int swe_compute_dij(swe_ctx* c, int inst, const double* un, double* dij,
   if (!c || inst < 0 || inst >= c->n_inst || !un) return fail(c, SWE_ERR_ARG, "bad arguments");
   if (c->precision != SWE_PREC_FP64) return fail(c, SWE_ERR_ARG, "swe_compute_dij is an FP64 operator");
   int rc = to_device(c, un, false, c->node_off[inst], c->node_off[inst + 1]);
-  if (rc) return rc;
+  if (rc) { drain(c); return rc; }
   std::vector<InstState> saved;
   if ((rc = save_state(c, saved))) return rc;
   if ((rc = set_inst_state_dt(c, inst, c->params[inst].dt > 0 ? c->params[inst].dt : 1.0, 1))) return rc;
@@ -984,7 +984,7 @@ SWE_API int swe_euler(swe_ctx* c, int inst, const double* un, double* unext) {
   if (!c || inst < 0 || inst >= c->n_inst || !un || !unext) return fail(c, SWE_ERR_ARG, "bad arguments");
   if (!(c->params[inst].dt > 0)) return fail(c, SWE_ERR_ARG, "params.dt must be > 0 for swe_euler");
   int rc = to_device(c, un, false, c->node_off[inst], c->node_off[inst + 1]);
-  if (rc) return rc;
+  if (rc) { drain(c); return rc; }
   std::vector<InstState> saved;
   if ((rc = save_state(c, saved))) return rc;
   if ((rc = set_inst_state_dt(c, inst, c->params[inst].dt, 1))) return rc;
@@ -1006,8 +1006,10 @@ SWE_API int swe_euler(swe_ctx* c, int inst, const double* un, double* unext) {
   c->euler_inst = inst;
   if ((rc = from_device_state(c, unext, false, c->node_off[inst], c->node_off[inst + 1],
                               c->precision == SWE_PREC_FP64 ? &c->B : nullptr,
-                              c->precision == SWE_PREC_FP64 ? nullptr : &c->mB)))
+                              c->precision == SWE_PREC_FP64 ? nullptr : &c->mB))) {
+    drain(c);
     return rc;
+  }
   CK(cudaStreamSynchronize(c->stream));
   return erc;
 }
@@ -1025,8 +1027,10 @@ SWE_API int swe_euler_intermediates(swe_ctx* c, int inst, double* dij_low, doubl
     if (alpha && (rc = rows_to_nodes(c, inst, c->w.alpha, alpha))) return rc;
     if (res && (rc = rows_to_nodes(c, inst, c->w.res, res))) return rc;
     if (rminus && (rc = rows_to_nodes(c, inst, c->w.rminus, rminus))) return rc;
-    if (u_low && (rc = from_device_state(c, u_low, false, c->node_off[inst], c->node_off[inst + 1], &c->w.uL, nullptr)))
+    if (u_low && (rc = from_device_state(c, u_low, false, c->node_off[inst], c->node_off[inst + 1], &c->w.uL, nullptr))) {
+      drain(c);
       return rc;
+    }
   } else {
     if (dij_low && (rc = entries_to_csr(c, inst, c->wm.dmu, dij_low, (const float*)nullptr, 0))) return rc;
     if (muij_low && (rc = entries_to_csr(c, inst, c->wm.dmu, muij_low, (const float*)nullptr, 1))) return rc;
@@ -1035,8 +1039,10 @@ SWE_API int swe_euler_intermediates(swe_ctx* c, int inst, double* dij_low, doubl
     if (rminus && is_split(c) && (rc = rows_to_nodes(c, inst, c->wm.rminus64, rminus))) return rc;
     if (rminus && !is_split(c) && (rc = rows_to_nodes(c, inst, c->wm.rminus, rminus))) return rc;
     if (u_low && (rc = from_device_state(c, u_low, false, c->node_off[inst], c->node_off[inst + 1], nullptr, nullptr,
-                                         true)))
+                                         true))) {
+      drain(c);
       return rc;
+    }
   }
   CK(cudaStreamSynchronize(c->stream));
   return SWE_OK;
