@@ -87,14 +87,13 @@ class Update {
   }
 
   // the time loop on the device: un uploaded, DO WHILE(time < t_final) for at
-  // most max_steps steps, un downloaded; returns the steps taken
+  // most max_steps steps, un downloaded (one swe_rk3_steps_host call); returns
+  // the steps taken
   int rk3(double* un, double& time, double t_final, int max_steps, double* dt_last = nullptr) {
-    check(swe_upload(ctx_, un), "upload");
     check(swe_set_time(ctx_, &time, &t_final), "set_time");
     double t = time, dt = 0.0;
     int done = 0;
-    check(swe_rk3_steps(ctx_, max_steps, &t, &dt, &done), "time loop");
-    check(swe_download(ctx_, un), "download");
+    check(swe_rk3_steps_host(ctx_, un, un, max_steps, &t, &dt, &done), "time loop");
     time = t;
     if (dt_last) *dt_last = dt;
     return done;
