@@ -21,6 +21,24 @@ def test_library_builds_and_exports_every_declared_symbol():
         assert hasattr(so, name), name
 
 
+@pytest.mark.parametrize("cc,std,body", [
+    ("gcc", "c99", "int main(void) { return swe_last_error(0) == 0; }"),
+    ("g++", "c++17", "int main() { return swe_last_error(nullptr) == nullptr; }"),
+])
+def test_header_is_plain_c(tmp_path, cc, std, body):
+    """The C ABI header stands alone (no CUDA or C++ types in the signatures):
+    it compiles as C99 and as C++17 with every warning an error."""
+    import shutil
+    import subprocess
+    if shutil.which(cc) is None:
+        pytest.skip(f"{cc} not found")
+    src = tmp_path / ("t.c" if cc == "gcc" else "t.cpp")
+    src.write_text('#include "swe_gpu.h"\n' + body + "\n")
+    r = subprocess.run([cc, f"-std={std}", "-Wall", "-Wextra", "-Werror", "-pedantic", "-fsyntax-only",
+                        f"-I{REPO / 'include'}", str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 def test_no_cpu_fallback_without_device():
     """Without a CUDA device the library refuses to create a context."""
     torch = pytest.importorskip("torch")
