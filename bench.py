@@ -642,26 +642,90 @@ def run_batch(args):
                       "looped_tuning": "default launch shapes"}), flush=True)
 
 
+def solitary_peak(rr, h):
+    """Crest of a wave travelling along x: position and height of the maximum
+    of h on the channel's centre line, refined by the parabola through the
+    largest nodal value and its two neighbours on that line."""
+    ymid = 0.5 * (rr[1].min() + rr[1].max())
+    yc = rr[1][np.argmin(np.abs(rr[1] - ymid))]
+    line = np.where(np.abs(rr[1] - yc) < 1e-9)[0]
+    line = line[np.argsort(rr[0][line])]
+    x, y = rr[0][line], h[line]
+    k = min(max(int(np.argmax(y)), 1), len(line) - 2)
+    den = y[k - 1] - 2.0 * y[k] + y[k + 1]
+    s = 0.5 * (y[k - 1] - y[k + 1]) / den if den != 0.0 else 0.0
+    return float(x[k] + s * 0.5 * (x[k + 1] - x[k - 1])), float(y[k] - 0.25 * (y[k - 1] - y[k + 1]) * s)
+
+
+def sgn_leg(case, steps):
+    """One configuration of the SGN solitary wave: FP64, mixed and
+    precision-split runs of `steps` steps from the exact wave, with their
+    rates, the time and last dt reached, min / max h, relative L1(h) against
+    FP64, the crest's amplitude and position against the exact travelling
+    wave, and the FP64 run's own sensitivity (initial state perturbed by 1e-7
+    relative, seeded)."""
+    rr = case.mesh["rr"]
+    names = {0: "fp64", 1: "mixed", 2: "mixed_f64_split"}
+    res, out = {}, {"cfl": case.params.cfl, "lambda_sgn": case.params.lambda_sgn}
+    for prec in (0, 1, 2):
+        u, v, n, upd = _run_case(case, prec, steps)
+        t, _, dt = upd.get_time()
+        res[prec] = (u, float(t[0]))
+        o = {"node_stage_per_s": v, "steps": n, "time": float(t[0]), "last_dt": float(dt[0]),
+             "min_h": float(u[0].min()), "max_h": float(u[0].max())}
+        if prec == 1:
+            o["tuning"] = upd.tuning
+            o["stage_kernels_ms"] = {k: round(x, 4) for k, x in upd.profile_kernels(3).items()}
+        out[names[prec]] = o
+        lump = upd.lumped
+        upd.close()
+
+    def l1(a, b):
+        return float(np.sum(lump * np.abs(a - b)) / np.sum(lump * np.abs(b)))
+
+    h1 = float(case.u0[0].min())
+    for prec, (u, t) in res.items():
+        xe, he = solitary_peak(rr, case.exact(1, rr, t))
+        xp, hp = solitary_peak(rr, u[0])
+        out[names[prec]]["crest_amplitude_rel_drift"] = (hp - h1) / (he - h1) - 1.0
+        out[names[prec]]["crest_position_drift"] = xp - xe
+        if prec:
+            out[names[prec]]["l1_h_vs_fp64"] = l1(u[0], res[0][0][0])
+    rng = np.random.default_rng(0)
+    pert = replace(case, u0=np.asfortranarray(case.u0 * (1 + 1e-7 * rng.uniform(-1, 1, case.u0.shape))))
+    u_p, _, _, upd = _run_case(pert, 0, steps)
+    upd.close()
+    out["fp64_sensitivity_l1_h_1e-7_perturbation"] = l1(u_p[0], res[0][0][0])
+    return out
+
+
 def run_single(args, which):
     from swe import cases as C
-    if which == "dam":
-        case = C.dam_break_case(n=101, tfinal=0.2)
-        steps = None
-    else:
-        case = C.sgn_case(nx=args.sgn_nx, ny=max(3, int(round(2.0 / (100.0 / (args.sgn_nx - 1)))) + 1),
-                          nsteps=1000)
-        steps = args.steps
+    if which == "sgn":
+        # the channel of the solitary wave at the requested resolution, as
+        # specified (CFL 0.1), and at the CFL that resolves the relaxation:
+        # the reference's lambda_max (and so its dt) leaves out the speed of
+        # the relaxation waves, which grows like lambda g h^3 / sqrt(m)
+        mesh = None
+        legs = {}
+        for name, cfl in (("as_specified", 0.1), ("relaxation_resolved", 5e-4)):
+            case = C.sgn_case(nx=args.sgn_nx, ny=max(3, int(round(2.0 / (100.0 / (args.sgn_nx - 1)))) + 1),
+                              nsteps=1000, cfl=cfl, mesh=mesh)
+            mesh = case.mesh
+            log(f"sgn {name}: {mesh['rr'].shape[1]} nodes, cfl {cfl}")
+            legs[name] = sgn_leg(case, args.steps)
+        print(json.dumps({"workload": "sgn_solitary", "nodes": mesh["rr"].shape[1], "steps": args.steps, **legs}),
+              flush=True)
+        return
+    case = C.dam_break_case(n=101, tfinal=0.2)
     log(f"{which}: {case.mesh['rr'].shape[1]} nodes")
     out = {"workload": case.name, "nodes": case.mesh["rr"].shape[1]}
     res = {}
     for prec in (0, 1):
-        u, v, n, upd = _run_case(case, prec, steps)
+        u, v, n, upd = _run_case(case, prec, None)
         res[prec] = u
         out[("fp64" if prec == 0 else "mixed") + "_node_stage_per_s"] = v
         out["steps"] = n
-        if prec == 1:
-            out["mixed_tuning"] = upd.tuning
-            out["mixed_stage_kernels_ms"] = {k: round(v, 4) for k, v in upd.profile_kernels(3).items()}
         lump = upd.lumped
         upd.close()
     out["mixed_vs_fp64_l1_h"] = float(np.sum(lump * np.abs(res[1][0] - res[0][0])) / np.sum(lump * np.abs(res[0][0])))
@@ -670,7 +734,7 @@ def run_single(args, which):
     # state perturbed by 1e-7 relative (seeded), after the same steps
     rng = np.random.default_rng(0)
     pert = replace(case, u0=np.asfortranarray(case.u0 * (1 + 1e-7 * rng.uniform(-1, 1, case.u0.shape))))
-    u_p, _, n_p, upd = _run_case(pert, 0, steps)
+    u_p, _, n_p, upd = _run_case(pert, 0, None)
     upd.close()
     out["fp64_sensitivity_l1_h_1e-7_perturbation"] = float(np.sum(lump * np.abs(u_p[0] - res[0][0]))
                                                            / np.sum(lump * np.abs(res[0][0])))
