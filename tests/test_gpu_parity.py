@@ -493,13 +493,14 @@ def test_wetdry_basin_full_size_against_oracle():
 def test_sgn_channel_full_size_against_oracle():
     """C5 at its full size: the 10001 x 201 SGN channel (2,010,201 nodes, five
     unknowns, mSGN_RHS source, walls on the long sides), the solitary wave,
-    three SSP-RK3 steps.  FP64 equals the oracle bit for bit.  The mixed
-    path is held to 3x the oracle's own sensitivity over the same steps (the
-    oracle from the initial state perturbed by 1e-7 relative, seeded), plus
-    1e-9: the stiff relaxation makes the case ill-conditioned over long
-    runs."""
-    case = C.sgn_case()
-    steps = 3
+    five SSP-RK3 steps at CFL 5e-4, which resolves the relaxation waves (at
+    the specified CFL 0.1 the reference's scheme itself collapses on this
+    mesh: its dt leaves out their speed, 200 times sqrt(g h) here).  FP64
+    equals the oracle bit for bit; the mixed path is within 1e-5 relative
+    L1(h) and within 3x the oracle's own sensitivity to a 1e-7 perturbation
+    of the initial state, plus 1e-9."""
+    case = C.sgn_case(cfl=5e-4)
+    steps = 5
     o = _oracle_for(case)
     u = case.u0.copy(order="F")
     t = 0.0
@@ -524,6 +525,7 @@ def test_sgn_channel_full_size_against_oracle():
             sens = _rel_l1(up[0], u[0], lump)
             print(f"C5 mixed vs oracle after {steps} steps: relative L1(h) {err:.3e} (oracle sensitivity {sens:.3e})")
             assert ug[0].min() >= 0.0
+            assert err <= MIXED_L1_TOL, err
             assert err <= 3 * sens + 1e-9, (err, sens)
 
 
